@@ -1,0 +1,192 @@
+/*
+ * wrs.h -- C ABI of the GB300-native weighted-random-sampling hot path.
+ *
+ * This is the drop-in boundary for kistenklaus/merian-wrs's operator facade
+ * `device::WRS` (src/device/wrs/WRS.hpp:91-172) and the kernels behind it.  Plain
+ * pointers and sizes only: device pointers are CUDA device addresses, `stream` is a
+ * cudaStream_t passed as void* (NULL = legacy default stream).  Every call is
+ * asynchronous on `stream` unless stated otherwise and returns a wrs_status.
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   wrs_config / wrs_config_init  WRSConfig = variant<ITS::Config, AliasTable::Config,
+ *                                 Cutpoint::Config>            src/device/wrs/WRS.hpp:14
+ *                                 PSAConfig                     src/device/wrs/alias/psa/PSA.hpp:19-41
+ *                                 SampleAliasTableConfig        src/device/wrs/alias/sampling/AliasTableSampling.hpp:26-32
+ *                                 InverseTransformSamplingConfig src/device/wrs/its/sampling/InverseTransformSampling.hpp:69-80
+ *   wrs_create / wrs_destroy      WRS::WRS(context, shaderCompiler, config)  src/device/wrs/WRS.hpp:116-119
+ *   wrs_buffers_create / _destroy WRSBuffers::allocate(alloc, mapping, N, S, config)
+ *                                                               src/device/wrs/WRS.hpp:60-88
+ *                                 (weights and samples stay caller-owned; the internals
+ *                                  -- mean, heavyCount, partition arrays, table or CMF,
+ *                                  lookback states -- live in wrs_buffers)
+ *   wrs_build                     WRS::build(cmd, buffers, N, profiler)  src/device/wrs/WRS.hpp:121-143
+ *   wrs_sample / wrs_sample_at    WRS::sample(cmd, buffers, N, S, seed = 12345)
+ *                                                               src/device/wrs/WRS.hpp:145-168
+ *   wrs_total_mass                Mean<float>::run              src/device/mean/Mean.hpp (AtomicMean::run)
+ *   wrs_prefix_sum                PrefixSum<float>::run / DecoupledPrefixSum::run
+ *                                                               src/device/prefix_sum/decoupled/DecoupledPrefixSum.hpp:174-199
+ *   wrs_prefix_partition          PrefixPartition<float>::run / DecoupledPrefixPartition::run
+ *                                                               src/device/prefix_partition/decoupled/DecoupledPrefixPartition.hpp:185-216
+ *   wrs_split_pack                SplitPack::run / InlineSplitPack::run
+ *                                                               src/device/wrs/alias/psa/splitpack/inline/InlineSplitPack.hpp:105-150
+ *   wrs_alias_sample              SampleAliasTable::run         src/device/wrs/alias/sampling/AliasTableSampling.hpp:75-84
+ *   wrs_its_sample                InverseTransformSampling::run src/device/wrs/its/sampling/InverseTransformSampling.hpp
+ *   wrs_batch_*                   no counterpart (the reference builds and samples one
+ *                                 distribution per call)
+ *
+ * Errors: the reference throws std::runtime_error("NOT-IMPLEMENTED") for unknown
+ * variants (src/device/wrs/WRS.hpp:40,111,141,166); here every entry point returns a
+ * status code instead, and wrs_last_error() gives the message of the calling thread's
+ * last failure.  Device-side conditions (a lookback wait that ran out of budget,
+ * overlapping PSA subproblems) are raised in a status word read by
+ * wrs_buffers_status().
+ *
+ * Threading: a handle and a buffers object are not thread-safe; distinct objects are
+ * independent.
+ */
+#ifndef WRS_GB300_H
+#define WRS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WRS_VERSION 100
+
+typedef enum wrs_status {
+    WRS_OK = 0,
+    WRS_ERR_INVALID_ARG = 1,
+    WRS_ERR_OOM = 2,
+    WRS_ERR_TIMEOUT = 3,         /* a lookback wait gave up (device status bit 1) */
+    WRS_ERR_CUDA = 4,
+    WRS_ERR_NOT_IMPLEMENTED = 5, /* e.g. the Cutpoint method */
+    WRS_ERR_CAPACITY = 6         /* N larger than the buffers were created for */
+} wrs_status;
+
+/* the WRSConfig alternatives */
+typedef enum wrs_method {
+    WRS_METHOD_ALIAS_TABLE = 0, /* AliasTable: PSA build + alias sampling */
+    WRS_METHOD_ITS = 1,         /* ITS: decoupled scan + inverse transform sampling */
+    WRS_METHOD_CUTPOINT = 2     /* Cutpoint: not implemented */
+} wrs_method;
+
+typedef enum wrs_rng {
+    WRS_RNG_REFERENCE = 0,     /* the shaders' streams: Philox2x32-7 (alias), wang_hash (ITS) */
+    WRS_RNG_PHILOX4X32_10 = 1  /* Philox4x32-10, key = seed, counter = sample index */
+} wrs_rng;
+
+typedef enum wrs_scan_precision {
+    WRS_SCAN_FP32 = 0,        /* FP32 carry through the lookback, as the reference */
+    WRS_SCAN_COMPENSATED = 1  /* FP32 with a two-sum (float-float) carry */
+} wrs_scan_precision;
+
+/* device status bits (wrs_buffers_status) */
+#define WRS_DEVICE_TIMEOUT 1u
+#define WRS_DEVICE_NONMONOTONE_SPLIT 2u
+
+typedef struct wrs_config {
+    uint32_t method;                 /* wrs_method */
+    uint32_t split_size;             /* PSA InlineSplitPackConfig(splitSize); reference default 2 */
+    uint32_t use_partition_elements; /* PSAConfig::usePartitionElements */
+    uint32_t coop_size;              /* alias: SampleAliasTableConfig::cooperativeSampleSize;
+                                        ITS: InverseTransformSamplingConfig::cooperativeSamplingSize
+                                        (0 = off; otherwise >= 32) */
+    uint32_t its_parray;             /* ITS: InverseTransformSamplingConfig::pArraySearch */
+    uint32_t rng;                    /* wrs_rng */
+    uint32_t scan_precision;         /* wrs_scan_precision */
+    uint32_t split_residual_f64;     /* PSA split target / sigma / spill in FP64 */
+    uint32_t split_full_light;       /* PSA split caps the light count at lightCount instead of
+                                        the shader's lightCount - 1
+                                        (splitpack/inline/shader.comp:90,104), which at the end
+                                        of the table can leave i + j < n and give the last
+                                        light bucket extra mass; 0 = reference behaviour */
+} wrs_config;
+
+typedef struct wrs_alias_entry {
+    float p;    /* keep-probability of the bucket (alias_table.hpp layout, 8 bytes) */
+    uint32_t a; /* alias index */
+} wrs_alias_entry;
+
+typedef struct wrs_handle wrs_handle;
+typedef struct wrs_buffers wrs_buffers;
+
+int wrs_version(void);
+const char* wrs_status_string(wrs_status s);
+const char* wrs_last_error(void);
+
+/* Defaults: alias = PSA split size 2, partition elements on, coop 0, reference RNG, FP32
+ * scan; ITS = coop 0, reference RNG, FP32 scan. */
+wrs_status wrs_config_init(wrs_config* cfg, uint32_t method);
+
+wrs_status wrs_create(const wrs_config* cfg, wrs_handle** out);
+void wrs_destroy(wrs_handle* h);
+
+/* Internals for distributions of up to max_n weights (one cudaMalloc). */
+size_t wrs_buffers_bytes(const wrs_handle* h, uint32_t max_n);
+wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers** out);
+void wrs_buffers_destroy(wrs_buffers* b);
+
+/* Build the sampler (alias table or CMF) of `weights[0..n)` (device, FP32, >= 0) into b. */
+wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, uint32_t n,
+                     wrs_buffers* b);
+/* Draw s samples (uint32 indices, device) for sample indices [0, s). */
+wrs_status wrs_sample(const wrs_handle* h, void* stream, const wrs_buffers* b, uint32_t n,
+                      uint64_t s, uint64_t seed, uint32_t* samples);
+/* Same for sample indices [offset, offset + s) of the stream. */
+wrs_status wrs_sample_at(const wrs_handle* h, void* stream, const wrs_buffers* b, uint32_t n,
+                         uint64_t s, uint64_t seed, uint64_t offset, uint32_t* samples);
+
+/* Synchronises `stream`, returns WRS_DEVICE_* bits raised since the last call (and clears
+ * them) in *device_status; WRS_ERR_TIMEOUT if a lookback wait gave up. */
+wrs_status wrs_buffers_status(wrs_buffers* b, void* stream, uint32_t* device_status);
+
+/* Device views of the internals (valid while b lives). */
+const wrs_alias_entry* wrs_buffers_alias_table(const wrs_buffers* b);
+const float* wrs_buffers_cmf(const wrs_buffers* b);
+const uint32_t* wrs_buffers_partition_indices(const wrs_buffers* b);
+const float* wrs_buffers_partition_prefix(const wrs_buffers* b);
+const float* wrs_buffers_partition_elements(const wrs_buffers* b);
+const float* wrs_buffers_mean(const wrs_buffers* b);        /* 1 float */
+const double* wrs_buffers_total(const wrs_buffers* b);      /* 1 double */
+const uint32_t* wrs_buffers_heavy_count(const wrs_buffers* b); /* 1 uint32 */
+
+/* ---- primitives (device pointers; b supplies control block and scratch) ---------- */
+wrs_status wrs_total_mass(const wrs_handle* h, void* stream, const float* weights, uint32_t n,
+                          wrs_buffers* b);
+wrs_status wrs_prefix_sum(const wrs_handle* h, void* stream, const float* in, uint32_t n,
+                          float* out, wrs_buffers* b);
+/* pivot = the mean held in b (run wrs_total_mass first); heavy count lands in b */
+wrs_status wrs_prefix_partition(const wrs_handle* h, void* stream, const float* weights,
+                                uint32_t n, uint32_t* partition_indices,
+                                float* partition_prefix, float* partition_elements,
+                                wrs_buffers* b);
+/* mean and heavy count are read from b */
+wrs_status wrs_split_pack(const wrs_handle* h, void* stream, const float* weights,
+                          const uint32_t* partition_indices, const float* partition_prefix,
+                          const float* partition_elements, uint32_t n, wrs_alias_entry* table,
+                          wrs_buffers* b);
+wrs_status wrs_alias_sample(const wrs_handle* h, void* stream, const wrs_alias_entry* table,
+                            uint32_t n, uint64_t s, uint64_t seed, uint64_t offset,
+                            uint32_t* samples);
+wrs_status wrs_its_sample(const wrs_handle* h, void* stream, const float* cmf, uint32_t n,
+                          uint64_t s, uint64_t seed, uint64_t offset, uint32_t* samples);
+/* Test hook for the bounded-wait path: runs the scan of wrs_prefix_sum with its first
+ * tile never scheduled (the tile ticket starts at 1) and a wait budget of `spin_limit`
+ * polls, so every other tile's lookback runs out of budget.  The kernel still ends;
+ * wrs_buffers_status then reports WRS_ERR_TIMEOUT and the context stays usable.
+ * No counterpart in the reference (its DecoupledMean lookback breaks silently after
+ * MAX_IT polls, src/device/mean/decoupled/float.comp:143). */
+wrs_status wrs_test_prefix_sum_stalled(const wrs_handle* h, void* stream, const float* in,
+                                       uint32_t n, float* out, wrs_buffers* b,
+                                       uint32_t spin_limit);
+/* Host helper: upload mean / heavy count into b (for driving wrs_split_pack directly). */
+wrs_status wrs_buffers_set_partition_info(wrs_buffers* b, void* stream, float mean,
+                                          uint32_t heavy_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WRS_GB300_H */

@@ -1,0 +1,416 @@
+// wrs_capi.cu -- host side of the C ABI declared in include/wrs.h.
+//
+// The handle holds the configuration (the reference's WRSConfig variant); a buffers
+// object holds the internals of one distribution (the reference's WRSBuffers minus the
+// caller-owned weights and samples) in a single device allocation.  Launch sequences:
+//   alias build : k_total_mass -> k_prefix_partition -> k_split_pack
+//                 (PSA::run, src/device/wrs/alias/psa/PSA.hpp:170-237)
+//   ITS build   : k_scan (ITS::build, src/device/wrs/its/ITS.hpp:90-108)
+//   sample      : k_alias_sample | k_its_sample (WRS::sample, src/device/wrs/WRS.hpp:145-168)
+// Stream order replaces the reference's pipeline barriers.
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/wrs.h"
+#include "wrs_device.cuh"
+#include "wrs_internal.cuh"
+
+using namespace wrs;
+
+struct wrs_handle {
+    wrs_config cfg;
+};
+
+struct wrs_buffers {
+    wrs_config cfg;
+    uint32_t max_n = 0;
+    uint32_t cap_tiles = 0;
+    void* base = nullptr;
+    size_t bytes = 0;
+    BuildCtrl* ctrl = nullptr;
+    double* partials = nullptr;
+    PartState* part_states = nullptr;
+    ScanState* scan_states = nullptr;
+    uint32_t* idx = nullptr;
+    float* prefix = nullptr;
+    float* elems = nullptr;
+    uint2* table = nullptr;
+    float* cmf = nullptr;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+wrs_status fail(wrs_status s, const char* what) {
+    g_last_error = what;
+    return s;
+}
+
+wrs_status cuda_fail(cudaError_t e, const char* where) {
+    g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return WRS_ERR_CUDA;
+}
+
+#define WRS_CUDA(call, where)                      \
+    do {                                           \
+        cudaError_t e_ = (call);                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_, where); \
+    } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct Layout {
+    size_t ctrl, partials, part_states, scan_states, idx, prefix, elems, table, cmf, total;
+};
+
+Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
+    const uint32_t cap_tiles = tiles_for(max_n) + 1;
+    Layout L{};
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = off;
+        off = align_up(off + bytes, 256);
+        return at;
+    };
+    L.ctrl = take(sizeof(BuildCtrl));
+    L.partials = take(sizeof(double) * kMassMaxBlocks);
+    const bool alias = cfg.method == WRS_METHOD_ALIAS_TABLE;
+    L.part_states = alias ? take(sizeof(PartState) * 2 * static_cast<size_t>(cap_tiles)) : 0;
+    L.scan_states = take(sizeof(ScanState) * 2 * static_cast<size_t>(cap_tiles));
+    const size_t zero_end = off;  // everything above starts zeroed
+    (void)zero_end;
+    if (alias) {
+        L.idx = take(sizeof(uint32_t) * static_cast<size_t>(max_n));
+        L.prefix = take(sizeof(float) * static_cast<size_t>(max_n));
+        L.elems = cfg.use_partition_elements ? take(sizeof(float) * static_cast<size_t>(max_n)) : 0;
+        L.table = take(sizeof(uint2) * static_cast<size_t>(max_n));
+    } else {
+        L.cmf = take(sizeof(float) * static_cast<size_t>(max_n));
+    }
+    L.total = off;
+    return L;
+}
+
+size_t zeroed_bytes(const wrs_config& cfg, uint32_t max_n) {
+    const Layout L = layout_for(cfg, max_n);
+    const uint32_t cap_tiles = tiles_for(max_n) + 1;
+    return L.scan_states + sizeof(ScanState) * 2 * static_cast<size_t>(cap_tiles);
+}
+
+wrs_status check_config(const wrs_config* c) {
+    if (!c) return fail(WRS_ERR_INVALID_ARG, "config is NULL");
+    if (c->method == WRS_METHOD_CUTPOINT)
+        return fail(WRS_ERR_NOT_IMPLEMENTED, "the Cutpoint method is not implemented");
+    if (c->method != WRS_METHOD_ALIAS_TABLE && c->method != WRS_METHOD_ITS)
+        return fail(WRS_ERR_INVALID_ARG, "unknown method");
+    if (c->method == WRS_METHOD_ALIAS_TABLE && c->split_size == 0)
+        return fail(WRS_ERR_INVALID_ARG, "split_size must be >= 1");
+    if (c->rng > WRS_RNG_PHILOX4X32_10) return fail(WRS_ERR_INVALID_ARG, "unknown rng");
+    if (c->scan_precision > WRS_SCAN_COMPENSATED)
+        return fail(WRS_ERR_INVALID_ARG, "unknown scan precision");
+    if (c->method == WRS_METHOD_ITS && c->coop_size != 0 && c->coop_size < 32)
+        return fail(WRS_ERR_INVALID_ARG, "ITS coop_size must be 0 or >= 32");
+    if (c->coop_size != 0 && c->rng != WRS_RNG_REFERENCE)
+        return fail(WRS_ERR_INVALID_ARG, "cooperative sampling exists only with the reference RNG");
+    if (c->coop_size > (1u << 30)) return fail(WRS_ERR_INVALID_ARG, "coop_size too large");
+    return WRS_OK;
+}
+
+constexpr uint32_t kMaxN = 0x7fffffffu;  // indices are handled as int where the shaders use int
+
+}  // namespace
+
+extern "C" {
+
+int wrs_version(void) { return WRS_VERSION; }
+
+const char* wrs_status_string(wrs_status s) {
+    switch (s) {
+        case WRS_OK: return "ok";
+        case WRS_ERR_INVALID_ARG: return "invalid argument";
+        case WRS_ERR_OOM: return "out of device memory";
+        case WRS_ERR_TIMEOUT: return "a lookback wait gave up";
+        case WRS_ERR_CUDA: return "CUDA error";
+        case WRS_ERR_NOT_IMPLEMENTED: return "not implemented";
+        case WRS_ERR_CAPACITY: return "n exceeds the buffers' capacity";
+    }
+    return "unknown status";
+}
+
+const char* wrs_last_error(void) { return g_last_error.c_str(); }
+
+wrs_status wrs_config_init(wrs_config* cfg, uint32_t method) {
+    if (!cfg) return fail(WRS_ERR_INVALID_ARG, "config is NULL");
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->method = method;
+    cfg->split_size = 2;
+    cfg->use_partition_elements = 1;
+    cfg->coop_size = 0;
+    cfg->its_parray = 0;
+    cfg->rng = WRS_RNG_REFERENCE;
+    cfg->scan_precision = WRS_SCAN_FP32;
+    cfg->split_residual_f64 = 0;
+    cfg->split_full_light = 0;
+    return check_config(cfg);
+}
+
+wrs_status wrs_create(const wrs_config* cfg, wrs_handle** out) {
+    if (!out) return fail(WRS_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    wrs_status s = check_config(cfg);
+    if (s != WRS_OK) return s;
+    wrs_handle* h = new (std::nothrow) wrs_handle;
+    if (!h) return fail(WRS_ERR_OOM, "host allocation failed");
+    h->cfg = *cfg;
+    *out = h;
+    return WRS_OK;
+}
+
+void wrs_destroy(wrs_handle* h) { delete h; }
+
+size_t wrs_buffers_bytes(const wrs_handle* h, uint32_t max_n) {
+    if (!h) return 0;
+    return layout_for(h->cfg, max_n).total;
+}
+
+wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers** out) {
+    if (!h || !out) return fail(WRS_ERR_INVALID_ARG, "handle or out is NULL");
+    *out = nullptr;
+    if (max_n == 0 || max_n > kMaxN) return fail(WRS_ERR_INVALID_ARG, "max_n out of range");
+    const Layout L = layout_for(h->cfg, max_n);
+    wrs_buffers* b = new (std::nothrow) wrs_buffers;
+    if (!b) return fail(WRS_ERR_OOM, "host allocation failed");
+    b->cfg = h->cfg;
+    b->max_n = max_n;
+    b->cap_tiles = tiles_for(max_n) + 1;
+    cudaError_t e = cudaMalloc(&b->base, L.total);
+    if (e != cudaSuccess) {
+        delete b;
+        (void)cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? fail(WRS_ERR_OOM, "cudaMalloc failed")
+                                              : cuda_fail(e, "cudaMalloc");
+    }
+    b->bytes = L.total;
+    char* p = static_cast<char*>(b->base);
+    b->ctrl = reinterpret_cast<BuildCtrl*>(p + L.ctrl);
+    b->partials = reinterpret_cast<double*>(p + L.partials);
+    const bool alias = h->cfg.method == WRS_METHOD_ALIAS_TABLE;
+    b->part_states = alias ? reinterpret_cast<PartState*>(p + L.part_states) : nullptr;
+    b->scan_states = reinterpret_cast<ScanState*>(p + L.scan_states);
+    if (alias) {
+        b->idx = reinterpret_cast<uint32_t*>(p + L.idx);
+        b->prefix = reinterpret_cast<float*>(p + L.prefix);
+        b->elems = h->cfg.use_partition_elements ? reinterpret_cast<float*>(p + L.elems) : nullptr;
+        b->table = reinterpret_cast<uint2*>(p + L.table);
+    } else {
+        b->cmf = reinterpret_cast<float*>(p + L.cmf);
+    }
+    e = cudaMemset(b->base, 0, zeroed_bytes(h->cfg, max_n));
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        cudaFree(b->base);
+        delete b;
+        return cuda_fail(e, "cudaMemset");
+    }
+    *out = b;
+    return WRS_OK;
+}
+
+void wrs_buffers_destroy(wrs_buffers* b) {
+    if (!b) return;
+    if (b->base) cudaFree(b->base);
+    delete b;
+}
+
+static wrs_status check_n(const wrs_buffers* b, uint32_t n) {
+    if (!b) return fail(WRS_ERR_INVALID_ARG, "buffers is NULL");
+    if (n == 0) return fail(WRS_ERR_INVALID_ARG, "n must be >= 1");
+    if (n > b->max_n) return fail(WRS_ERR_CAPACITY, "n exceeds the buffers' capacity");
+    return WRS_OK;
+}
+
+wrs_status wrs_total_mass(const wrs_handle* h, void* stream, const float* weights, uint32_t n,
+                          wrs_buffers* b) {
+    if (!h || !weights) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    wrs_status s = check_n(b, n);
+    if (s != WRS_OK) return s;
+    WRS_CUDA(launch_total_mass(as_stream(stream), weights, n, b->partials, b->ctrl), "total mass");
+    return WRS_OK;
+}
+
+wrs_status wrs_prefix_sum(const wrs_handle* h, void* stream, const float* in, uint32_t n,
+                          float* out, wrs_buffers* b) {
+    if (!h || !in || !out) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    wrs_status s = check_n(b, n);
+    if (s != WRS_OK) return s;
+    WRS_CUDA(launch_scan(as_stream(stream), h->cfg.scan_precision == WRS_SCAN_COMPENSATED, in, n,
+                         out, b->ctrl, b->scan_states, b->cap_tiles),
+             "prefix sum");
+    return WRS_OK;
+}
+
+wrs_status wrs_prefix_partition(const wrs_handle* h, void* stream, const float* weights,
+                                uint32_t n, uint32_t* partition_indices, float* partition_prefix,
+                                float* partition_elements, wrs_buffers* b) {
+    if (!h || !weights || !partition_indices || !partition_prefix)
+        return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    wrs_status s = check_n(b, n);
+    if (s != WRS_OK) return s;
+    if (!b->part_states) return fail(WRS_ERR_INVALID_ARG, "buffers were not created for the alias method");
+    WRS_CUDA(launch_prefix_partition(as_stream(stream), h->cfg.scan_precision == WRS_SCAN_COMPENSATED,
+                                     weights, n, b->ctrl, b->part_states, b->cap_tiles,
+                                     partition_indices, partition_prefix, partition_elements),
+             "prefix partition");
+    return WRS_OK;
+}
+
+wrs_status wrs_split_pack(const wrs_handle* h, void* stream, const float* weights,
+                          const uint32_t* partition_indices, const float* partition_prefix,
+                          const float* partition_elements, uint32_t n, wrs_alias_entry* table,
+                          wrs_buffers* b) {
+    if (!h || !weights || !partition_indices || !partition_prefix || !table)
+        return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    wrs_status s = check_n(b, n);
+    if (s != WRS_OK) return s;
+    if (h->cfg.split_size == 0) return fail(WRS_ERR_INVALID_ARG, "split_size must be >= 1");
+    WRS_CUDA(launch_split_pack(as_stream(stream), h->cfg.split_residual_f64 != 0,
+                               h->cfg.split_full_light != 0, weights,
+                               partition_indices, partition_elements, partition_prefix, b->ctrl,
+                               &b->ctrl->status, n, h->cfg.split_size,
+                               reinterpret_cast<uint2*>(table)),
+             "split pack");
+    return WRS_OK;
+}
+
+wrs_status wrs_alias_sample(const wrs_handle* h, void* stream, const wrs_alias_entry* table,
+                            uint32_t n, uint64_t s, uint64_t seed, uint64_t offset,
+                            uint32_t* samples) {
+    if (!h || !table || (!samples && s)) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    if (n == 0 || n > kMaxN) return fail(WRS_ERR_INVALID_ARG, "n out of range");
+    if (s == 0) return WRS_OK;
+    WRS_CUDA(launch_alias_sample(as_stream(stream), h->cfg.rng, h->cfg.coop_size,
+                                 reinterpret_cast<const uint2*>(table), n, s, seed, offset, samples),
+             "alias sample");
+    return WRS_OK;
+}
+
+wrs_status wrs_its_sample(const wrs_handle* h, void* stream, const float* cmf, uint32_t n,
+                          uint64_t s, uint64_t seed, uint64_t offset, uint32_t* samples) {
+    if (!h || !cmf || (!samples && s)) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    if (n == 0 || n > kMaxN) return fail(WRS_ERR_INVALID_ARG, "n out of range");
+    if (s == 0) return WRS_OK;
+    WRS_CUDA(launch_its_sample(as_stream(stream), h->cfg.rng, h->cfg.coop_size,
+                               h->cfg.its_parray != 0, cmf, n, s, seed, offset, samples),
+             "its sample");
+    return WRS_OK;
+}
+
+wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, uint32_t n,
+                     wrs_buffers* b) {
+    if (!h || !weights) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    wrs_status s = check_n(b, n);
+    if (s != WRS_OK) return s;
+    if (b->cfg.method != h->cfg.method)
+        return fail(WRS_ERR_INVALID_ARG, "buffers were created for another method");
+    const cudaStream_t st = as_stream(stream);
+    const bool comp = h->cfg.scan_precision == WRS_SCAN_COMPENSATED;
+    if (h->cfg.method == WRS_METHOD_ITS) {
+        WRS_CUDA(launch_scan(st, comp, weights, n, b->cmf, b->ctrl, b->scan_states, b->cap_tiles),
+                 "ITS build");
+        return WRS_OK;
+    }
+    if (h->cfg.use_partition_elements && !b->elems)
+        return fail(WRS_ERR_INVALID_ARG, "buffers were created without partition elements");
+    float* elems = h->cfg.use_partition_elements ? b->elems : nullptr;
+    WRS_CUDA(launch_total_mass(st, weights, n, b->partials, b->ctrl), "total mass");
+    WRS_CUDA(launch_prefix_partition(st, comp, weights, n, b->ctrl, b->part_states, b->cap_tiles,
+                                     b->idx, b->prefix, elems),
+             "prefix partition");
+    WRS_CUDA(launch_split_pack(st, h->cfg.split_residual_f64 != 0, h->cfg.split_full_light != 0,
+                               weights, b->idx, elems,
+                               b->prefix, b->ctrl, &b->ctrl->status, n, h->cfg.split_size,
+                               b->table),
+             "split pack");
+    return WRS_OK;
+}
+
+wrs_status wrs_sample_at(const wrs_handle* h, void* stream, const wrs_buffers* b, uint32_t n,
+                         uint64_t s, uint64_t seed, uint64_t offset, uint32_t* samples) {
+    if (!h) return fail(WRS_ERR_INVALID_ARG, "handle is NULL");
+    wrs_status st = check_n(b, n);
+    if (st != WRS_OK) return st;
+    if (b->cfg.method != h->cfg.method)
+        return fail(WRS_ERR_INVALID_ARG, "buffers were created for another method");
+    if (h->cfg.method == WRS_METHOD_ITS)
+        return wrs_its_sample(h, stream, b->cmf, n, s, seed, offset, samples);
+    return wrs_alias_sample(h, stream, reinterpret_cast<const wrs_alias_entry*>(b->table), n, s,
+                            seed, offset, samples);
+}
+
+wrs_status wrs_sample(const wrs_handle* h, void* stream, const wrs_buffers* b, uint32_t n,
+                      uint64_t s, uint64_t seed, uint32_t* samples) {
+    return wrs_sample_at(h, stream, b, n, s, seed, 0, samples);
+}
+
+wrs_status wrs_buffers_status(wrs_buffers* b, void* stream, uint32_t* device_status) {
+    if (!b) return fail(WRS_ERR_INVALID_ARG, "buffers is NULL");
+    const cudaStream_t st = as_stream(stream);
+    WRS_CUDA(cudaStreamSynchronize(st), "stream synchronize");
+    uint32_t v = 0;
+    WRS_CUDA(cudaMemcpy(&v, &b->ctrl->status, sizeof(v), cudaMemcpyDeviceToHost), "status read");
+    if (v) WRS_CUDA(cudaMemset(&b->ctrl->status, 0, sizeof(v)), "status clear");
+    if (device_status) *device_status = v;
+    if (v & kStatusTimeout) return fail(WRS_ERR_TIMEOUT, "a lookback wait gave up");
+    return WRS_OK;
+}
+
+wrs_status wrs_test_prefix_sum_stalled(const wrs_handle* h, void* stream, const float* in,
+                                       uint32_t n, float* out, wrs_buffers* b,
+                                       uint32_t spin_limit) {
+    if (!h || !in || !out) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    wrs_status s = check_n(b, n);
+    if (s != WRS_OK) return s;
+    if (spin_limit == 0 || spin_limit > kSpinLimit)
+        return fail(WRS_ERR_INVALID_ARG, "spin_limit out of range");
+    const cudaStream_t st = as_stream(stream);
+    const uint32_t one = 1;
+    WRS_CUDA(cudaMemcpyAsync(&b->ctrl->scan.ticket, &one, sizeof(one), cudaMemcpyHostToDevice, st),
+             "ticket preset");
+    WRS_CUDA(launch_scan(st, h->cfg.scan_precision == WRS_SCAN_COMPENSATED, in, n, out, b->ctrl,
+                         b->scan_states, b->cap_tiles, spin_limit),
+             "stalled prefix sum");
+    return WRS_OK;
+}
+
+wrs_status wrs_buffers_set_partition_info(wrs_buffers* b, void* stream, float mean,
+                                          uint32_t heavy_count) {
+    if (!b) return fail(WRS_ERR_INVALID_ARG, "buffers is NULL");
+    const cudaStream_t st = as_stream(stream);
+    WRS_CUDA(cudaMemcpyAsync(&b->ctrl->mean, &mean, sizeof(float), cudaMemcpyHostToDevice, st),
+             "mean upload");
+    WRS_CUDA(cudaMemcpyAsync(&b->ctrl->heavy_count, &heavy_count, sizeof(uint32_t),
+                             cudaMemcpyHostToDevice, st),
+             "heavy count upload");
+    WRS_CUDA(cudaStreamSynchronize(st), "stream synchronize");
+    return WRS_OK;
+}
+
+const wrs_alias_entry* wrs_buffers_alias_table(const wrs_buffers* b) {
+    return b ? reinterpret_cast<const wrs_alias_entry*>(b->table) : nullptr;
+}
+const float* wrs_buffers_cmf(const wrs_buffers* b) { return b ? b->cmf : nullptr; }
+const uint32_t* wrs_buffers_partition_indices(const wrs_buffers* b) { return b ? b->idx : nullptr; }
+const float* wrs_buffers_partition_prefix(const wrs_buffers* b) { return b ? b->prefix : nullptr; }
+const float* wrs_buffers_partition_elements(const wrs_buffers* b) { return b ? b->elems : nullptr; }
+const float* wrs_buffers_mean(const wrs_buffers* b) { return b ? &b->ctrl->mean : nullptr; }
+const double* wrs_buffers_total(const wrs_buffers* b) { return b ? &b->ctrl->total : nullptr; }
+const uint32_t* wrs_buffers_heavy_count(const wrs_buffers* b) {
+    return b ? &b->ctrl->heavy_count : nullptr;
+}
+
+}  // extern "C"

@@ -1,0 +1,184 @@
+// wrs_device.cuh -- device-side building blocks shared by the WRS kernels (sm_103a).
+//
+//  * float-float ("compensated") arithmetic for the carries of the decoupled lookback;
+//  * self-validating 64-bit lookback words (every word carries its own ready bit, so
+//    readers never see a torn state and writers need no fences);
+//  * the counter-based generators: the reference shaders' Philox2x32-7 variant and
+//    wang_hash (bit-exact restatements), and Random123 Philox4x32-10;
+//  * bounded spin helpers: every wait in this library gives up after a fixed budget
+//    and raises a status bit instead of hanging the GPU.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wrs {
+
+// bits of the per-build device status word
+constexpr uint32_t kStatusTimeout = 1u;      // a lookback spin exhausted its budget
+constexpr uint32_t kStatusNonMonotone = 2u;  // split k+1 < split k (overlapping subproblems)
+
+constexpr uint32_t kSpinLimit = 1u << 21;  // lookback polls before giving up (>= ~1 s)
+
+// ---------------------------------------------------------------------------
+// float-float arithmetic (Knuth two-sum); every operation rounds once.
+// ---------------------------------------------------------------------------
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    float s = __fadd_rn(a, b);
+    float bp = __fsub_rn(s, a);
+    float ap = __fsub_rn(s, bp);
+    float e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+    return {s, e};
+}
+
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {
+    float s = __fadd_rn(a, b);
+    float e = __fsub_rn(b, __fsub_rn(s, a));
+    return {s, e};
+}
+
+template <bool COMP>
+__device__ __forceinline__ ff carry_add(ff a, ff b) {
+    if constexpr (COMP) {
+        ff s = two_sum(a.hi, b.hi);
+        float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+        return fast_two_sum(s.hi, e);
+    } else {
+        return {__fadd_rn(a.hi, b.hi), 0.0f};
+    }
+}
+
+// round(carry + x) to FP32
+template <bool COMP>
+__device__ __forceinline__ float carry_apply(ff c, float x) {
+    if constexpr (COMP) {
+        ff s = two_sum(c.hi, x);
+        return __fadd_rn(s.hi, __fadd_rn(s.lo, c.lo));
+    } else {
+        return __fadd_rn(c.hi, x);
+    }
+}
+
+__device__ __forceinline__ ff shfl_xor_ff(ff v, int m) {
+    return {__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
+}
+
+// ---------------------------------------------------------------------------
+// lookback words.  An ff word is {hi bits, lo bits | 1}: the LSB of lo's
+// mantissa is the ready bit (the value loses at most one ulp of lo).  A count
+// word is {count, 1}.  State buffers are zero when a build starts.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long pack_ff(ff v) {
+    uint32_t hi = __float_as_uint(v.hi);
+    uint32_t lo = __float_as_uint(v.lo) | 1u;
+    return (static_cast<unsigned long long>(lo) << 32) | hi;
+}
+__device__ __forceinline__ bool ff_ready(unsigned long long w) { return (w >> 32) & 1ull; }
+__device__ __forceinline__ ff unpack_ff(unsigned long long w) {
+    return {__uint_as_float(static_cast<uint32_t>(w)),
+            __uint_as_float(static_cast<uint32_t>(w >> 32) & ~1u)};
+}
+__device__ __forceinline__ unsigned long long pack_cnt(uint32_t c) {
+    return (1ull << 32) | c;
+}
+__device__ __forceinline__ bool cnt_ready(unsigned long long w) { return (w >> 32) != 0; }
+
+__device__ __forceinline__ void st_relaxed_v2(unsigned long long* p, unsigned long long a,
+                                              unsigned long long b) {
+    asm volatile("st.relaxed.gpu.global.v2.b64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b)
+                 : "memory");
+}
+__device__ __forceinline__ void st_relaxed(unsigned long long* p, unsigned long long a) {
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(a) : "memory");
+}
+__device__ __forceinline__ void ld_relaxed_v2(const unsigned long long* p, unsigned long long& a,
+                                              unsigned long long& b) {
+    asm volatile("ld.relaxed.gpu.global.v2.b64 {%0, %1}, [%2];"
+                 : "=l"(a), "=l"(b)
+                 : "l"(p)
+                 : "memory");
+}
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// exponential back-off for spin loops (bounded: 32 ns .. 1 us)
+__device__ __forceinline__ void backoff(uint32_t spins) {
+    uint32_t ns = 32u << (spins < 5 ? spins : 5);
+    __nanosleep(ns);
+}
+
+// ---------------------------------------------------------------------------
+// generators
+// ---------------------------------------------------------------------------
+
+// src/device/wrs/alias/sampling/shader.comp:39-54 -- 7 rounds of
+//   (hi,lo) = mulExtended(x0, 0xD256D193); x0 = x1 ^ hi; x1 = lo + k; k += 0x9E3779B9
+__device__ __forceinline__ uint2 philox2x32_7(uint32_t x0, uint32_t x1, uint32_t key) {
+    uint32_t k = key;
+#pragma unroll
+    for (int r = 0; r < 7; ++r) {
+        uint32_t hi = __umulhi(x0, 0xD256D193u);
+        uint32_t lo = x0 * 0xD256D193u;
+        x0 = x1 ^ hi;
+        x1 = lo + k;
+        k += 0x9E3779B9u;
+    }
+    return make_uint2(x0, x1);
+}
+
+// Random123 Philox4x32-10 (Salmon et al., SC'11).  The key schedule is hoisted by
+// the caller: ks[r] = key + r * (0x9E3779B9, 0xBB67AE85).
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, const uint2* ks) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ ks[r].x, lo1, hi0 ^ c.w ^ ks[r].y, lo0);
+    }
+    return c;
+}
+
+__device__ __forceinline__ void philox4x32_10_keys(uint64_t seed, uint2* ks) {
+    uint32_t k0 = static_cast<uint32_t>(seed), k1 = static_cast<uint32_t>(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        ks[r] = make_uint2(k0, k1);
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+// src/device/wrs/its/sampling/shader.comp:70-78 (bits before the division by 2^32)
+__device__ __forceinline__ uint32_t wang_hash(uint32_t seed) {
+    seed = (seed ^ 61u) ^ (seed >> 16);
+    seed *= 9u;
+    seed = seed ^ (seed >> 4);
+    seed *= 0x27d4eb2du;
+    seed = seed ^ (seed >> 15);
+    return seed;
+}
+
+// float(x) / 4294967296.0 with a round-to-nearest conversion (the division is exact)
+__device__ __forceinline__ float unit_ref(uint32_t x) {
+    return __fmul_rn(__uint2float_rn(x), 2.3283064365386963e-10f);
+}
+
+// ---------------------------------------------------------------------------
+// memory helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint2 ld_entry(const uint2* p) {
+    uint2 v;
+    asm volatile("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];"
+                 : "=r"(v.x), "=r"(v.y)
+                 : "l"(p));
+    return v;
+}
+
+}  // namespace wrs

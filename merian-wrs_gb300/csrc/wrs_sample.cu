@@ -1,0 +1,230 @@
+// wrs_sample.cu -- sampling kernels of the WRS hot path for sm_103a.
+//
+//   k_alias_sample  alias-table sampling      (reference: src/device/wrs/alias/sampling/shader.comp:68-111)
+//   k_its_sample    inverse transform sampling by bisection over the CMF
+//                                             (reference: src/device/wrs/its/sampling/shader.comp:80-177)
+//
+// Two generator modes:
+//   RNG_REF      the shaders' own streams: Philox2x32-7 variant with counter (0, gid) and
+//                key = seed for the alias method; wang_hash(seed + gid) for ITS.  Indices
+//                are bit-exact with the shaders' arithmetic.
+//   RNG_PHILOX   Random123 Philox4x32-10, key = (seed lo, seed hi), counter = (sample
+//                index lo, hi, 0, 0).  Alias: ix = mulhi(x0, N), coin = (x1 >> 8) * 2^-24,
+//                alias when coin >= p.  ITS: u = (2*(x0 >> 9) + 1) * 2^-24 in (0,1),
+//                target = u * cmf[N-1], lower bound over the CMF.
+#include "wrs_device.cuh"
+#include "wrs_internal.cuh"
+
+namespace wrs {
+
+constexpr int kSampleThreads = 256;
+constexpr int kAliasPerThread = 4;
+constexpr uint32_t RNG_REF = 0, RNG_PHILOX = 1;
+
+// mix(x, y, a) evaluated as x*(1-a) + y*a, one rounding per operation
+__device__ __forceinline__ float mix_rn(float x, float y, float a) {
+    return __fadd_rn(__fmul_rn(x, __fsub_rn(1.0f, a)), __fmul_rn(y, a));
+}
+
+template <uint32_t RNG, bool COOP>
+__global__ __launch_bounds__(kSampleThreads) void k_alias_sample(const uint2* __restrict__ table,
+                                                                 uint32_t n, uint64_t S,
+                                                                 uint64_t seed, uint64_t offset,
+                                                                 uint32_t coop,
+                                                                 uint32_t* __restrict__ out) {
+    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const uint64_t s0 = t * kAliasPerThread;
+    if (s0 >= S) return;
+    uint32_t r[kAliasPerThread];
+    if constexpr (RNG == RNG_REF) {
+        const uint32_t key = static_cast<uint32_t>(seed);
+        const float fn = __uint2float_rn(n);
+        float sx = 0.f, sy = 0.f;
+        if constexpr (COOP) {
+            // narrowSection (shader.comp:68-76): the subgroup's elected lane is the first
+            // sample of its aligned group of 32; section = ix -/+ coop/2
+            const uint32_t g0 = static_cast<uint32_t>(offset + (s0 & ~31ull));
+            const uint2 u = philox2x32_7(0u, g0, key);
+            const int ix = __float2int_rz(__fmul_rn(fn, unit_ref(u.x)));
+            sx = __int2float_rn(ix - static_cast<int>(coop) / 2);
+            sy = __int2float_rn(ix + static_cast<int>(coop) / 2);
+        }
+        uint2 ent[kAliasPerThread];
+        int ixs[kAliasPerThread];
+        float uys[kAliasPerThread];
+#pragma unroll
+        for (int v = 0; v < kAliasPerThread; ++v) {
+            const uint32_t g = static_cast<uint32_t>(offset + s0 + v);
+            const uint2 u = philox2x32_7(0u, g, key);
+            const float ux = unit_ref(u.x);
+            uys[v] = unit_ref(u.y);
+            const float f = COOP ? mix_rn(sx, sy, ux) : __fmul_rn(fn, ux);
+            int ix = __float2int_rz(f);
+            ix = ix < 0 ? 0 : ix;
+            ix = ix > static_cast<int>(n - 1u) ? static_cast<int>(n - 1u) : ix;
+            ixs[v] = ix;
+        }
+#pragma unroll
+        for (int v = 0; v < kAliasPerThread; ++v) ent[v] = ld_entry(table + ixs[v]);
+#pragma unroll
+        for (int v = 0; v < kAliasPerThread; ++v)
+            r[v] = uys[v] >= __uint_as_float(ent[v].x) ? ent[v].y : static_cast<uint32_t>(ixs[v]);
+    } else {
+        uint2 ks[10];
+        philox4x32_10_keys(seed, ks);
+        uint2 ent[kAliasPerThread];
+        uint32_t ixs[kAliasPerThread];
+        float us[kAliasPerThread];
+#pragma unroll
+        for (int v = 0; v < kAliasPerThread; ++v) {
+            const uint64_t g = offset + s0 + v;
+            const uint4 x = philox4x32_10(
+                make_uint4(static_cast<uint32_t>(g), static_cast<uint32_t>(g >> 32), 0u, 0u), ks);
+            ixs[v] = __umulhi(x.x, n);
+            us[v] = __fmul_rn(__uint2float_rn(x.y >> 8), 5.9604644775390625e-08f);
+        }
+#pragma unroll
+        for (int v = 0; v < kAliasPerThread; ++v) ent[v] = ld_entry(table + ixs[v]);
+#pragma unroll
+        for (int v = 0; v < kAliasPerThread; ++v)
+            r[v] = us[v] >= __uint_as_float(ent[v].x) ? ent[v].y : ixs[v];
+    }
+    if (s0 + kAliasPerThread <= S && (reinterpret_cast<uintptr_t>(out) & 15u) == 0) {
+        __stcs(reinterpret_cast<uint4*>(out + s0), make_uint4(r[0], r[1], r[2], r[3]));
+    } else {
+#pragma unroll
+        for (int v = 0; v < kAliasPerThread; ++v)
+            if (s0 + v < S) out[s0 + v] = r[v];
+    }
+}
+
+// its/sampling/shader.comp:80-94
+__device__ __forceinline__ float search_range_u(const float* __restrict__ cmf, uint32_t x,
+                                                uint32_t y, float u) {
+    const float lo = x > 0 ? __ldg(cmf + x - 1) : 0.0f;
+    const float hi = __ldg(cmf + y);
+    return __fadd_rn(lo, __fmul_rn(__fsub_rn(hi, lo), u));
+}
+
+// its/sampling/shader.comp:131-140: lower bound with the shader's probe sequence
+__device__ __forceinline__ uint32_t bisect(const float* __restrict__ cmf, uint32_t x, uint32_t y,
+                                           float u) {
+    while (x < y) {
+        const uint32_t mid = x + ((y - x) >> 1);
+        if (u > __ldg(cmf + mid))
+            x = mid + 1;
+        else
+            y = mid;
+    }
+    return x;
+}
+
+// COOP: 0 = none, 1 = binary narrowing, 2 = p-array narrowing.  One sample per thread so a
+// warp is the shader's subgroup of 32 consecutive samples; every lane of the warp takes
+// part in the narrowing (also lanes past S in the last warp, which then store nothing).
+template <uint32_t RNG, int COOP>
+__global__ __launch_bounds__(kSampleThreads) void k_its_sample(const float* __restrict__ cmf,
+                                                               uint32_t n, uint64_t S,
+                                                               uint64_t seed, uint64_t offset,
+                                                               uint32_t coop,
+                                                               uint32_t* __restrict__ out) {
+    const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if constexpr (COOP == 0) {
+        if (s >= S) return;
+    } else {
+        if ((s & ~31ull) >= S) return;  // whole warps only
+    }
+    uint32_t res;
+    if constexpr (RNG == RNG_REF) {
+        const uint32_t seed32 = static_cast<uint32_t>(seed);
+        const uint32_t g = static_cast<uint32_t>(offset + s);
+        uint32_t x = 0, y = n - 1u;
+        if constexpr (COOP != 0) {
+            const int lane = threadIdx.x & 31;
+            const uint32_t g0 = __shfl_sync(0xffffffffu, g, 0);
+            const float u1 =
+                __shfl_sync(0xffffffffu, search_range_u(cmf, 0, n - 1u, unit_ref(wang_hash(seed32 + g0))), 0);
+            if constexpr (COOP == 2) {
+                uint32_t range = y - x + 1u;
+                while (range > coop) {
+                    const uint32_t base = range / 32u;
+                    const uint32_t start = x + lane * base;
+                    uint32_t end = start + base - 1u;
+                    end = end > y ? y : end;
+                    const unsigned b = __ballot_sync(0xffffffffu, u1 < __ldg(cmf + end));
+                    if (b) {
+                        const int id = __ffs(b) - 1;
+                        x = __shfl_sync(0xffffffffu, start, id);
+                        y = __shfl_sync(0xffffffffu, end, id);
+                    } else {
+                        // u1 beyond every partition end (the shader's ballot is empty there):
+                        // keep the remainder, at least the last item
+                        x = min(x + 32u * base, y);
+                    }
+                    range = y - x + 1u;
+                }
+            } else {
+                while (y - x + 1u > coop) {
+                    const uint32_t mid = x + ((y - x) >> 1);
+                    if (u1 > __ldg(cmf + mid))
+                        x = mid + 1;
+                    else
+                        y = mid;
+                }
+            }
+        }
+        const float u2 = search_range_u(cmf, x, y, unit_ref(wang_hash((seed32 ^ 0xA9EC5C80u) + g)));
+        res = bisect(cmf, x, y, u2);
+    } else {
+        uint2 ks[10];
+        philox4x32_10_keys(seed, ks);
+        const uint64_t g = offset + s;
+        const uint4 r = philox4x32_10(
+            make_uint4(static_cast<uint32_t>(g), static_cast<uint32_t>(g >> 32), 0u, 0u), ks);
+        const float u = __fmul_rn(__uint2float_rn((r.x >> 9) * 2u + 1u), 5.9604644775390625e-08f);
+        const float target = __fmul_rn(u, __ldg(cmf + n - 1u));
+        res = bisect(cmf, 0, n - 1u, target);
+    }
+    if (s < S) __stcs(out + s, res);
+}
+
+cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, const uint2* table,
+                                uint32_t n, uint64_t S, uint64_t seed, uint64_t offset,
+                                uint32_t* out) {
+    const uint64_t threads = (S + kAliasPerThread - 1) / kAliasPerThread;
+    const uint64_t blocks = (threads + kSampleThreads - 1) / kSampleThreads;
+    if (blocks == 0) return cudaSuccess;
+    if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
+    const dim3 grid(static_cast<unsigned>(blocks));
+    if (rng == RNG_REF) {
+        if (coop)
+            k_alias_sample<RNG_REF, true><<<grid, kSampleThreads, 0, st>>>(table, n, S, seed, offset, coop, out);
+        else
+            k_alias_sample<RNG_REF, false><<<grid, kSampleThreads, 0, st>>>(table, n, S, seed, offset, coop, out);
+    } else {
+        k_alias_sample<RNG_PHILOX, false><<<grid, kSampleThreads, 0, st>>>(table, n, S, seed, offset, coop, out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool parray,
+                              const float* cmf, uint32_t n, uint64_t S, uint64_t seed,
+                              uint64_t offset, uint32_t* out) {
+    const uint64_t blocks = (S + kSampleThreads - 1) / kSampleThreads;
+    if (blocks == 0) return cudaSuccess;
+    if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
+    const dim3 grid(static_cast<unsigned>(blocks));
+    if (rng == RNG_REF) {
+        if (coop == 0)
+            k_its_sample<RNG_REF, 0><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
+        else if (parray)
+            k_its_sample<RNG_REF, 2><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
+        else
+            k_its_sample<RNG_REF, 1><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
+    } else {
+        k_its_sample<RNG_PHILOX, 0><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace wrs

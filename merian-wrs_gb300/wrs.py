@@ -1,0 +1,277 @@
+"""Host-side mirror of merian-wrs's operator facade over the C ABI (include/wrs.h).
+
+Mirrors (paths relative to the reference project):
+  WRSConfig / AliasTableConfig / ITSConfig   src/device/wrs/WRS.hpp:14,
+                                             src/device/wrs/alias/AliasTable.hpp:10-22,
+                                             src/device/wrs/its/ITS.hpp:68-77
+  WRSBuffers.allocate(N, S, config)          src/device/wrs/WRS.hpp:60-88
+  WRS(config).build(stream, buffers, N)      src/device/wrs/WRS.hpp:121-143
+  WRS.sample(stream, buffers, N, S, seed)    src/device/wrs/WRS.hpp:145-168 (seed = 12345)
+
+Device memory and streams come from PyTorch (plumbing only); all compute runs in
+libwrs_gb300.so.  There is no fallback: if the library cannot be loaded, every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libwrs_gb300.so")
+
+METHOD_ALIAS_TABLE = 0
+METHOD_ITS = 1
+METHOD_CUTPOINT = 2
+RNG_REFERENCE = 0
+RNG_PHILOX4X32_10 = 1
+SCAN_FP32 = 0
+SCAN_COMPENSATED = 1
+
+DEVICE_TIMEOUT = 1
+DEVICE_NONMONOTONE_SPLIT = 2
+
+
+class WRSError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"wrs status {status}: {message}")
+        self.status = status
+
+
+class _Config(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in (
+        "method", "split_size", "use_partition_elements", "coop_size", "its_parray", "rng",
+        "scan_precision", "split_residual_f64", "split_full_light")]
+
+
+_lib: C.CDLL | None = None
+
+
+def lib() -> C.CDLL:
+    """Load libwrs_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with merian-wrs_gb300/build.py "
+                               "(there is no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        vp, u32, u64, f32, i32, sz = (C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_int,
+                                      C.c_size_t)
+        cfgp = C.POINTER(_Config)
+        sig = {
+            "wrs_version": (i32, []),
+            "wrs_status_string": (C.c_char_p, [i32]),
+            "wrs_last_error": (C.c_char_p, []),
+            "wrs_config_init": (i32, [cfgp, u32]),
+            "wrs_create": (i32, [cfgp, C.POINTER(vp)]),
+            "wrs_destroy": (None, [vp]),
+            "wrs_buffers_bytes": (sz, [vp, u32]),
+            "wrs_buffers_create": (i32, [vp, u32, C.POINTER(vp)]),
+            "wrs_buffers_destroy": (None, [vp]),
+            "wrs_build": (i32, [vp, vp, vp, u32, vp]),
+            "wrs_sample": (i32, [vp, vp, vp, u32, u64, u64, vp]),
+            "wrs_sample_at": (i32, [vp, vp, vp, u32, u64, u64, u64, vp]),
+            "wrs_buffers_status": (i32, [vp, vp, C.POINTER(u32)]),
+            "wrs_buffers_alias_table": (vp, [vp]),
+            "wrs_buffers_cmf": (vp, [vp]),
+            "wrs_buffers_partition_indices": (vp, [vp]),
+            "wrs_buffers_partition_prefix": (vp, [vp]),
+            "wrs_buffers_partition_elements": (vp, [vp]),
+            "wrs_buffers_mean": (vp, [vp]),
+            "wrs_buffers_total": (vp, [vp]),
+            "wrs_buffers_heavy_count": (vp, [vp]),
+            "wrs_total_mass": (i32, [vp, vp, vp, u32, vp]),
+            "wrs_prefix_sum": (i32, [vp, vp, vp, u32, vp, vp]),
+            "wrs_prefix_partition": (i32, [vp, vp, vp, u32, vp, vp, vp, vp]),
+            "wrs_split_pack": (i32, [vp, vp, vp, vp, vp, vp, u32, vp, vp]),
+            "wrs_alias_sample": (i32, [vp, vp, vp, u32, u64, u64, u64, vp]),
+            "wrs_its_sample": (i32, [vp, vp, vp, u32, u64, u64, u64, vp]),
+            "wrs_buffers_set_partition_info": (i32, [vp, vp, f32, u32]),
+            "wrs_test_prefix_sum_stalled": (i32, [vp, vp, vp, u32, vp, vp, u32]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise WRSError(status, lib().wrs_last_error().decode())
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+def _dev_ptr(t) -> int | None:
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("device tensors must be contiguous CUDA tensors")
+    return t.data_ptr()
+
+
+@dataclass
+class WRSConfig:
+    """The WRSConfig variant: method plus the knobs of its sub-configs."""
+    method: int = METHOD_ALIAS_TABLE
+    split_size: int = 2
+    use_partition_elements: bool = True
+    coop_size: int = 0
+    its_parray: bool = False
+    rng: int = RNG_REFERENCE
+    scan_precision: int = SCAN_FP32
+    split_residual_f64: bool = False
+    split_full_light: bool = False
+
+    def c(self) -> _Config:
+        return _Config(self.method, self.split_size, int(self.use_partition_elements),
+                       self.coop_size, int(self.its_parray), self.rng, self.scan_precision,
+                       int(self.split_residual_f64), int(self.split_full_light))
+
+    def split_flags(self) -> int:
+        """The oracle's split flags for this configuration."""
+        return (1 if self.split_residual_f64 else 0) | (2 if self.split_full_light else 0)
+
+    def name(self) -> str:
+        if self.method == METHOD_ITS:
+            coop = f"-COOP-{self.coop_size}-{'PARRAY' if self.its_parray else 'BINARY'}" \
+                if self.coop_size else ""
+            return f"ITS{coop}"
+        return f"AliasTable-PSA-split{self.split_size}-coop{self.coop_size}"
+
+
+def AliasTableConfig(split_size: int = 2, use_partition_elements: bool = True,
+                     coop_size: int = 0, **kw) -> WRSConfig:
+    """AliasTableConfig(PSAConfig(..., InlineSplitPackConfig(split_size), usePartitionElements),
+    SampleAliasTableConfig(coop_size))."""
+    return WRSConfig(METHOD_ALIAS_TABLE, split_size, use_partition_elements, coop_size, **kw)
+
+
+def ITSConfig(coop_size: int = 0, parray: bool = False, **kw) -> WRSConfig:
+    """ITSConfig(DecoupledPrefixSumConfig(), InverseTransformSamplingConfig(512, coop, parray))."""
+    return WRSConfig(METHOD_ITS, coop_size=coop_size, its_parray=parray, **kw)
+
+
+class Handle:
+    """Owns a wrs_handle."""
+
+    def __init__(self, config: WRSConfig):
+        self.config = config
+        self._cfg = config.c()
+        h = C.c_void_p()
+        check(lib().wrs_create(C.byref(self._cfg), C.byref(h)))
+        self.ptr = h.value
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and _lib is not None:
+            _lib.wrs_destroy(self.ptr)
+            self.ptr = None
+
+
+class Internals:
+    """Owns a wrs_buffers (the method's internal device buffers)."""
+
+    def __init__(self, handle: Handle, max_n: int):
+        b = C.c_void_p()
+        check(lib().wrs_buffers_create(handle.ptr, max_n, C.byref(b)))
+        self.ptr = b.value
+        self.max_n = max_n
+        self.handle = handle
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and _lib is not None:
+            _lib.wrs_buffers_destroy(self.ptr)
+            self.ptr = None
+
+    def status(self, stream=None) -> int:
+        v = C.c_uint32(0)
+        st = lib().wrs_buffers_status(self.ptr, _stream_ptr(stream), C.byref(v))
+        if st not in (0, 3):
+            check(st)
+        return int(v.value)
+
+    def views(self) -> dict:
+        L = lib()
+        return {
+            "alias_table": L.wrs_buffers_alias_table(self.ptr),
+            "cmf": L.wrs_buffers_cmf(self.ptr),
+            "partition_indices": L.wrs_buffers_partition_indices(self.ptr),
+            "partition_prefix": L.wrs_buffers_partition_prefix(self.ptr),
+            "partition_elements": L.wrs_buffers_partition_elements(self.ptr),
+            "mean": L.wrs_buffers_mean(self.ptr),
+            "total": L.wrs_buffers_total(self.ptr),
+            "heavy_count": L.wrs_buffers_heavy_count(self.ptr),
+        }
+
+
+@dataclass
+class WRSBuffers:
+    """weights [N] float32 and samples [S] (uint32 stored as int32) are caller-owned device
+    tensors; `internals` holds the method's buffers."""
+    weights: object
+    samples: object
+    internals: Internals = field(repr=False)
+
+    @classmethod
+    def allocate(cls, N: int, S: int, config: WRSConfig, device="cuda", handle=None):
+        import torch
+        handle = handle or Handle(config)
+        w = torch.empty(N, dtype=torch.float32, device=device)
+        s = torch.empty(S, dtype=torch.int32, device=device)
+        return cls(w, s, Internals(handle, N))
+
+
+class WRS:
+    """device::WRS: build() records the construction of the sampler of buffers.weights[:N],
+    sample() draws S samples into buffers.samples.  Both are asynchronous on `stream`."""
+
+    def __init__(self, config: WRSConfig):
+        self.config = config
+        self.handle = Handle(config)
+
+    def build(self, stream, buffers: WRSBuffers, N: int) -> None:
+        check(lib().wrs_build(self.handle.ptr, _stream_ptr(stream), _dev_ptr(buffers.weights),
+                              N, buffers.internals.ptr))
+
+    def sample(self, stream, buffers: WRSBuffers, N: int, S: int, seed: int = 12345,
+               offset: int = 0) -> None:
+        check(lib().wrs_sample_at(self.handle.ptr, _stream_ptr(stream), buffers.internals.ptr,
+                                  N, S, seed, offset, _dev_ptr(buffers.samples)))
+
+    # primitives -----------------------------------------------------------------
+    def total_mass(self, stream, weights, N, internals: Internals) -> None:
+        check(lib().wrs_total_mass(self.handle.ptr, _stream_ptr(stream), _dev_ptr(weights), N,
+                                   internals.ptr))
+
+    def prefix_sum(self, stream, inp, N, out, internals: Internals) -> None:
+        check(lib().wrs_prefix_sum(self.handle.ptr, _stream_ptr(stream), _dev_ptr(inp), N,
+                                   _dev_ptr(out), internals.ptr))
+
+    def prefix_partition(self, stream, weights, N, idx, prefix, elems, internals) -> None:
+        check(lib().wrs_prefix_partition(self.handle.ptr, _stream_ptr(stream), _dev_ptr(weights),
+                                         N, _dev_ptr(idx), _dev_ptr(prefix), _dev_ptr(elems),
+                                         internals.ptr))
+
+    def split_pack(self, stream, weights, idx, prefix, elems, N, table, internals) -> None:
+        check(lib().wrs_split_pack(self.handle.ptr, _stream_ptr(stream), _dev_ptr(weights),
+                                   _dev_ptr(idx), _dev_ptr(prefix), _dev_ptr(elems), N,
+                                   _dev_ptr(table), internals.ptr))
+
+    def alias_sample(self, stream, table, N, S, seed, offset, out) -> None:
+        check(lib().wrs_alias_sample(self.handle.ptr, _stream_ptr(stream), _dev_ptr(table), N, S,
+                                     seed, offset, _dev_ptr(out)))
+
+    def its_sample(self, stream, cmf, N, S, seed, offset, out) -> None:
+        check(lib().wrs_its_sample(self.handle.ptr, _stream_ptr(stream), _dev_ptr(cmf), N, S,
+                                   seed, offset, _dev_ptr(out)))

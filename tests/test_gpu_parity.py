@@ -1,0 +1,319 @@
+"""GPU parity tests: the CUDA path, driven through the C ABI, against the oracle.
+
+Bar (stated per test):
+  * integer / index outputs -- partition indices, heavy count, split points, alias indices
+    and samples -- are bit-exact against the oracle given the same upstream values (the
+    GPU's own mean, partition prefix, alias table or CMF, as "given the same scanned
+    weights" in the reference's test strategy);
+  * FP32 values computed by the same operations (alias probabilities p) are bit-exact too;
+  * scans and the total mass are within stated relative tolerances of an FP64 oracle.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import (weights_lognormal, weights_precision, weights_uniform, weights_zipf)
+from gpu_util import d2h, empty, h2d, t2h
+from oracle.oracle import ENTRY_DTYPE, RNG_PHILOX4X32_10, RNG_REFERENCE
+
+pytestmark = pytest.mark.gpu
+
+GENS = {"uniform": weights_uniform, "zipf": weights_zipf, "lognormal": weights_lognormal}
+EDGE_N = [1, 2, 3, 31, 32, 33, 4095, 4096, 4097]
+
+
+class Built:
+    """wrs_build through the public API, with the internals read back."""
+
+    def __init__(self, pkg, w: np.ndarray, cfg):
+        W = pkg.wrs
+        self.wrs = W.WRS(cfg)
+        self.N = w.size
+        self.buffers = W.WRSBuffers.allocate(self.N, 1, cfg, handle=self.wrs.handle)
+        self.buffers.weights.copy_(h2d(w))
+        self.wrs.build(None, self.buffers, self.N)
+        v = self.buffers.internals.views()
+        self.status = self.buffers.internals.status()
+        if cfg.method == W.METHOD_ALIAS_TABLE:
+            self.mean = float(d2h(v["mean"], 1, np.float32)[0])
+            self.total = float(d2h(v["total"], 1, np.float64)[0])
+            self.hc = int(d2h(v["heavy_count"], 1, np.uint32)[0])
+            self.idx = d2h(v["partition_indices"], self.N, np.uint32)
+            self.prefix = d2h(v["partition_prefix"], self.N, np.float32)
+            self.elems = (d2h(v["partition_elements"], self.N, np.float32)
+                          if cfg.use_partition_elements else None)
+            self.table = d2h(v["alias_table"], self.N, ENTRY_DTYPE)
+        else:
+            self.cmf = d2h(v["cmf"], self.N, np.float32)
+
+    def sample(self, S, seed, offset=0):
+        import torch
+        out = torch.empty(S, dtype=torch.int32, device="cuda")
+        self.buffers.samples = out
+        self.wrs.sample(None, self.buffers, self.N, S, seed, offset=offset)
+        return t2h(out, np.uint32)
+
+
+def same_table(a: np.ndarray, b: np.ndarray) -> bool:
+    return np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+# ------------------------------------------------------------------ total mass ---
+
+@pytest.mark.parametrize("N", [1, 5, 4097, 1 << 20, (1 << 22) + 3])
+@pytest.mark.parametrize("gen", ["uniform", "lognormal"])
+def test_total_mass(pkg, cuda, oracle, N, gen):
+    """FP64 total mass: relative error <= 1e-12 against a sequential FP64 sum; the mean
+    (rounded once to FP32) equals the oracle's."""
+    w = GENS[gen](N, N)
+    b = Built(pkg, w, pkg.AliasTableConfig())
+    ref = oracle.total_mass(w)
+    assert abs(b.total - ref) <= 1e-12 * ref
+    assert np.float32(b.mean) == np.float32(oracle.mean(w))
+
+
+def test_total_mass_unaligned_view(pkg, cuda, oracle):
+    """A weights pointer that is not 16-byte aligned (a view into a larger array)."""
+    W = pkg.wrs
+    w = weights_uniform(100003, 1)
+    dw = h2d(w)
+    wrs = W.WRS(pkg.AliasTableConfig())
+    internals = W.Internals(wrs.handle, w.size)
+    wrs.total_mass(None, dw[1:], w.size - 1, internals)
+    total = d2h(internals.views()["total"], 1, np.float64)[0]
+    assert abs(total - oracle.total_mass(w[1:])) <= 1e-12 * total
+
+
+# ------------------------------------------------------------- prefix partition ---
+
+@pytest.mark.parametrize("N", EDGE_N + [65536, (1 << 20) + 77])
+@pytest.mark.parametrize("gen", list(GENS))
+@pytest.mark.parametrize("comp", [False, True])
+def test_prefix_partition(pkg, cuda, oracle, N, gen, comp):
+    """Partition indices, elements and heavy count bit-exact against the stable partition
+    of shader.comp:329-361 at the GPU's mean; heavy / light prefixes within 1e-6
+    (compensated carry) or 1e-4 (FP32 carry) relative to the FP64 prefix."""
+    w = GENS[gen](N, 7 * N + 1)
+    cfg = pkg.AliasTableConfig(scan_precision=1 if comp else 0)
+    b = Built(pkg, w, cfg)
+    assert b.status == 0
+    idx, elems, hc = oracle.partition(w, b.mean)
+    assert b.hc == hc
+    assert np.array_equal(b.idx, idx)
+    assert np.array_equal(b.elems.view(np.uint32), elems.view(np.uint32))
+    ref = oracle.partition_prefix_f64(w, b.mean)
+    err = np.abs(b.prefix.astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-30)
+    assert err.max() <= (1e-6 if comp else 1e-4), err.max()
+
+
+# --------------------------------------------------------------- split + pack ---
+
+@pytest.mark.parametrize("split_size", [1, 2, 3, 32])
+@pytest.mark.parametrize("flags", [0, 1, 2, 3])
+@pytest.mark.parametrize("gen", list(GENS))
+def test_split_pack_bit_exact(pkg, cuda, oracle, split_size, flags, gen):
+    """The GPU alias table equals the oracle's split+pack (shader.comp:81-223) fed the GPU's
+    own partition, prefix, heavy count and mean: p bits and alias indices identical."""
+    N = 65536 + 123
+    w = GENS[gen](N, split_size * 10 + flags)
+    cfg = pkg.AliasTableConfig(split_size=split_size, split_residual_f64=bool(flags & 1),
+                               split_full_light=bool(flags & 2))
+    b = Built(pkg, w, cfg)
+    assert b.status & pkg.wrs.DEVICE_TIMEOUT == 0
+    ref = oracle.split_pack(w, b.idx, b.prefix, b.hc, b.mean, split_size, flags=flags,
+                            elems=b.elems)
+    assert same_table(b.table, ref)
+
+
+@pytest.mark.parametrize("use_elems", [False, True])
+def test_split_pack_partition_elements_switch(pkg, cuda, oracle, use_elems):
+    """PSAConfig::usePartitionElements changes where pack reads weights, not the result."""
+    w = weights_lognormal(200001, 3)
+    b = Built(pkg, w, pkg.AliasTableConfig(use_partition_elements=use_elems))
+    ref = oracle.split_pack(w, b.idx, b.prefix, b.hc, b.mean, 2)
+    assert same_table(b.table, ref)
+
+
+def test_split_pack_primitive_on_oracle_inputs(pkg, cuda, oracle):
+    """wrs_split_pack on inputs made entirely by the oracle (FP64-rounded prefix)."""
+    W = pkg.wrs
+    w = weights_zipf(30001, 9)
+    mean = np.float32(oracle.mean(w))
+    idx, elems, hc = oracle.partition(w, mean)
+    prefix = oracle.partition_prefix_f64(w, mean).astype(np.float32)
+    wrs = W.WRS(pkg.AliasTableConfig(split_size=4))
+    internals = W.Internals(wrs.handle, w.size)
+    W.check(W.lib().wrs_buffers_set_partition_info(internals.ptr, None, float(mean), hc))
+    table = empty(2 * w.size, "i32")
+    wrs.split_pack(None, h2d(w), h2d(idx), h2d(prefix), h2d(elems), w.size, table, internals)
+    got = t2h(table, np.uint32).view(ENTRY_DTYPE)
+    assert same_table(got, oracle.split_pack(w, idx, prefix, hc, mean, 4, elems=elems))
+
+
+@pytest.mark.parametrize("N", EDGE_N)
+def test_edge_sizes_build_and_sample(pkg, cuda, oracle, N):
+    w = weights_uniform(N, 5)
+    b = Built(pkg, w, pkg.AliasTableConfig())
+    idx, _, hc = oracle.partition(w, b.mean)
+    assert np.array_equal(b.idx, idx) and b.hc == hc
+    assert same_table(b.table, oracle.split_pack(w, b.idx, b.prefix, b.hc, b.mean, 2))
+    S = 1000 + N
+    assert np.array_equal(b.sample(S, 77), oracle.alias_sample(b.table, S, 77))
+
+
+@pytest.mark.parametrize("case", ["all_equal", "zeros", "single_nonzero", "two_values"])
+def test_degenerate_weights(pkg, cuda, oracle, case):
+    N = 10000
+    w = {"all_equal": np.full(N, 0.3, np.float32),
+         "zeros": np.where(np.arange(N) % 3 == 0, 0.0, weights_uniform(N, 2)).astype(np.float32),
+         "single_nonzero": np.where(np.arange(N) == 4321, 2.5, 0.0).astype(np.float32),
+         "two_values": np.where(np.arange(N) % 2 == 0, 1.0, 3.0).astype(np.float32)}[case]
+    cfg = pkg.AliasTableConfig(split_full_light=True)
+    b = Built(pkg, w, cfg)
+    idx, _, hc = oracle.partition(w, b.mean)
+    assert np.array_equal(b.idx, idx) and b.hc == hc
+    assert same_table(b.table, oracle.split_pack(w, b.idx, b.prefix, b.hc, b.mean, 2, flags=2))
+    s = b.sample(200000, 3)
+    assert np.array_equal(s, oracle.alias_sample(b.table, 200000, 3))
+    if case in ("zeros", "single_nonzero"):
+        assert np.all(w[s] > 0), "a zero-weight item was sampled"
+    if case == "single_nonzero":
+        assert np.all(s == 4321)
+
+
+# ------------------------------------------------------------------- sampling ---
+
+@pytest.mark.parametrize("rng,coop", [(RNG_REFERENCE, 0), (RNG_REFERENCE, 128),
+                                      (RNG_REFERENCE, 32), (RNG_PHILOX4X32_10, 0)])
+@pytest.mark.parametrize("offset", [0, 12345])
+def test_alias_sample_bit_exact(pkg, cuda, oracle, rng, coop, offset):
+    """Alias samples equal the oracle's restatement of alias/sampling/shader.comp:68-111
+    (reference streams) or of the Philox4x32-10 mode, given the GPU's table."""
+    w = weights_zipf(100000, 4)
+    b = Built(pkg, w, pkg.AliasTableConfig(rng=rng, coop_size=coop))
+    S = (1 << 20) + 13
+    got = b.sample(S, 0xDEADBEEF12345, offset)
+    ref = oracle.alias_sample(b.table, S, 0xDEADBEEF12345, rng=rng, coop=coop, offset=offset,
+                              nthreads=8)
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("N", [1, 3, 4097, (1 << 20) + 1, 1 << 22])
+@pytest.mark.parametrize("comp", [False, True])
+def test_scan_precision(pkg, cuda, oracle, N, comp):
+    """Inclusive scan against FP64: max relative error <= 1e-6 with the compensated carry,
+    <= 1e-4 with the FP32 carry; the reference's own prefix checker accepts it."""
+    w = weights_lognormal(N, N)
+    b = Built(pkg, w, pkg.ITSConfig(scan_precision=1 if comp else 0))
+    assert b.status == 0
+    ref = oracle.prefix_f64(w)
+    err = np.abs(b.cmf.astype(np.float64) - ref) / np.maximum(ref, 1e-30)
+    assert err.max() <= (1e-6 if comp else 1e-4), err.max()
+
+
+@pytest.mark.parametrize("rng,coop,parray", [(RNG_REFERENCE, 0, False),
+                                             (RNG_REFERENCE, 128, False),
+                                             (RNG_REFERENCE, 4096, True),
+                                             (RNG_REFERENCE, 64, True),
+                                             (RNG_PHILOX4X32_10, 0, False)])
+def test_its_sample_bit_exact(pkg, cuda, oracle, rng, coop, parray):
+    """ITS samples equal the oracle's restatement of its/sampling/shader.comp:80-177 (or the
+    Philox4x32-10 mode) given the GPU's CMF."""
+    w = weights_uniform(300001, 8)
+    b = Built(pkg, w, pkg.ITSConfig(coop_size=coop, parray=parray, rng=rng))
+    S = (1 << 20) + 5
+    got = b.sample(S, 4242, 99)
+    ref = oracle.its_sample(b.cmf, S, 4242, rng=rng, coop=coop, parray=parray, offset=99,
+                            nthreads=8)
+    assert np.array_equal(got, ref)
+
+
+# ----------------------------------------------------------------- statistics ---
+
+@pytest.mark.parametrize("gen", list(GENS))
+def test_sampling_statistics(pkg, cuda, oracle, gen):
+    """Alias (PSA with the light-cap fix) and ITS samples pass a binned chi-square test
+    against the target distribution (p > 1e-4) with small RMSE."""
+    N, S = 65536, 1 << 24
+    w = GENS[gen](N, 21)
+    for cfg in (pkg.AliasTableConfig(rng=RNG_PHILOX4X32_10, split_full_light=True,
+                                     scan_precision=1),
+                pkg.ITSConfig(rng=RNG_PHILOX4X32_10, scan_precision=1)):
+        b = Built(pkg, w, cfg)
+        st = oracle.sample_stats(b.sample(S, 31337), w)
+        assert st["p_value"] > 1e-4, (cfg.name(), st)
+        assert st["rmse"] < 5.0 / np.sqrt(float(S) * N), (cfg.name(), st)
+
+
+def test_precision_weights_never_sample_zero(pkg, cuda, oracle):
+    """Log-normal(0,3) with 1% zeros and 0.01% scaled by 1e6: no zero-weight item is drawn
+    (alias with the light-cap fix, and ITS with Philox4x32-10)."""
+    N = 1 << 20
+    w = weights_precision(N, 5)
+    for cfg in (pkg.AliasTableConfig(rng=RNG_PHILOX4X32_10, split_full_light=True,
+                                     scan_precision=1, split_residual_f64=True),
+                pkg.ITSConfig(rng=RNG_PHILOX4X32_10, scan_precision=1)):
+        b = Built(pkg, w, cfg)
+        s = b.sample(1 << 22, 5)
+        assert np.all(w[s] > 0), cfg.name()
+
+
+# ------------------------------------------------------------ determinism, status ---
+
+def test_build_is_deterministic(pkg, cuda):
+    """Repeated builds of one input give identical tables (compensated carry)."""
+    w = weights_lognormal((1 << 21) + 9, 12)
+    cfg = pkg.AliasTableConfig(scan_precision=1)
+    a = Built(pkg, w, cfg)
+    for _ in range(2):
+        b = Built(pkg, w, cfg)
+        assert np.array_equal(a.prefix.view(np.uint32), b.prefix.view(np.uint32))
+        assert same_table(a.table, b.table)
+
+
+def test_repeated_builds_reuse_buffers(pkg, cuda, oracle):
+    """One buffers object serves many builds of different sizes (self-cleaning lookback
+    state), for both the partition and the scan kernels."""
+    W = pkg.wrs
+    cfg = pkg.AliasTableConfig()
+    wrs = W.WRS(cfg)
+    bufs = W.WRSBuffers.allocate(1 << 20, 1, cfg, handle=wrs.handle)
+    its = W.WRS(pkg.ITSConfig())
+    for k, N in enumerate([1 << 20, 5000, 777777, 1 << 20, 4096, 123456]):
+        w = weights_uniform(N, k)
+        bufs.weights[:N].copy_(h2d(w))
+        wrs.build(None, bufs, N)
+        v = bufs.internals.views()
+        idx = d2h(v["partition_indices"], N, np.uint32)
+        mean = d2h(v["mean"], 1, np.float32)[0]
+        assert np.array_equal(idx, oracle.partition(w, mean)[0])
+        out = empty(N)
+        its.prefix_sum(None, bufs.weights, N, out, bufs.internals)
+        ref = oracle.prefix_f64(w)
+        assert np.abs(t2h(out, np.float32) - ref).max() <= 1e-4 * ref[-1]
+    assert bufs.internals.status() == 0
+
+
+def test_lookback_wait_runs_out_and_reports(pkg, cuda):
+    """A scan whose first tile is never scheduled: every other tile's lookback wait runs out
+    of its budget, the kernel still ends, the status reports a timeout, and the context
+    stays usable for a normal build afterwards."""
+    import ctypes as C
+    W = pkg.wrs
+    N = 64 * 4096
+    w = weights_uniform(N, 1)
+    wrs = W.WRS(pkg.ITSConfig())
+    internals = W.Internals(wrs.handle, N)
+    dw, out = h2d(w), empty(N)
+    W.check(W.lib().wrs_test_prefix_sum_stalled(wrs.handle.ptr, None, dw.data_ptr(), N,
+                                                out.data_ptr(), internals.ptr, 2000))
+    v = C.c_uint32(0)
+    assert W.lib().wrs_buffers_status(internals.ptr, None, C.byref(v)) == 3  # WRS_ERR_TIMEOUT
+    assert v.value & W.DEVICE_TIMEOUT
+    # the context and the buffers are still good
+    wrs.prefix_sum(None, dw, N, out, internals)
+    assert internals.status() == 0
+    got = t2h(out, np.float32).astype(np.float64)
+    ref = np.cumsum(w.astype(np.float64))
+    assert np.abs(got - ref).max() <= 1e-4 * ref[-1]
