@@ -1,0 +1,424 @@
+#!/usr/bin/env python3
+"""Benchmark of the WRS hot path on GB300 (one JSON line on stdout, rank 0).
+
+Workload (the single-large-distribution configuration): N = 2^26 FP32 weights in three
+seeded distributions -- uniform(0,1], Zipf-like (i+1)^-1.1 randomly permuted, log-normal
+(0, 2).  One step = PSA alias-table build (total mass -> fused prefix-partition ->
+split+pack) of one distribution (cycling through the three) + S = 2^28 alias samples
+(Philox4x32-10, key = seed, counter = sample index, uint32 indices).  Inputs (256 MB of
+weights, a 512 MB table, 1 GB of samples) are larger than the 126 MB L2, so no flush is
+needed between steps.
+
+  value   samples/s over the timed steps (build included), inputs resident in HBM
+  e2e     the same through the C ABI with host buffers: pinned H2D of the weights and D2H
+          of the samples inside every timed step
+  roofline  the dominant kernel (alias sampling): algorithmic 12 B/sample (8 B entry + 4 B
+          index) / its mean CUDA-event duration, against the measured HBM copy bandwidth
+  cpu_baseline  the CPU port of the same path (oracle/, single thread) on a bounded sample
+
+Extra keys measure the rest of the configuration with the same events: per-kernel times
+and bandwidths, the decoupled scan (weights scanned/s) and ITS sampling (samples/s).
+
+`--impl reference` times the reference path's CPU implementation (the oracle port of
+the reference's CPU code; its own compiled CPU code when that loads here) on all host
+cores, on the same workload, and prints the same line with "impl": "reference".
+Multi-GPU runs are independent replicas (the path does not shard one distribution).
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LOG2_N = 26
+LOG2_S = 28
+SEEDS = (2, 3, 4)
+DISTS = ("uniform(0,1]", "zipf(s=1.1, permuted)", "lognormal(0,2)")
+WORKLOAD = ("single large distribution: N=2^26 FP32 weights x 3 seeded distributions "
+            "(uniform(0,1], Zipf s=1.1 permuted, log-normal(0,2)); step = PSA alias build + "
+            "S=2^28 alias samples (Philox4x32-10, uint32 indices)")
+METRIC = "samples/s"
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "alias_sample_n26_s28.md")
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--log2n", type=int, default=LOG2_N)
+    p.add_argument("--log2s", type=int, default=LOG2_S)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true", help="skip the per-kernel breakdown")
+    return p.parse_args()
+
+
+def peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profiled_traffic() -> float | None:
+    """DRAM bytes per alias-sampling launch from the committed ncu summary, if present."""
+    if not os.path.exists(PROFILE_TRAFFIC):
+        return None
+    for line in open(PROFILE_TRAFFIC):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+# ------------------------------------------------------------------ inputs ---
+
+def make_weights(dist: int, n: int, seed: int, device):
+    """Seeded synthetic weights of the configuration's three shapes (generated on the GPU
+    with PyTorch's Philox generator; the CPU legs copy them back)."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    if dist == 0:   # uniform(0,1]: ((x >> 40) + 1) * 2^-24
+        x = torch.randint(0, 1 << 24, (n,), generator=g, device=device, dtype=torch.int64)
+        return ((x + 1).to(torch.float64) * 2.0 ** -24).to(torch.float32)
+    if dist == 1:   # Zipf-like, permuted
+        w = torch.arange(1, n + 1, device=device, dtype=torch.float64).pow(-1.1).to(torch.float32)
+        return w[torch.randperm(n, generator=g, device=device)]
+    z = torch.randn(n, generator=g, device=device, dtype=torch.float32)
+    return torch.exp(2.0 * z)
+
+
+# ------------------------------------------------------------------ clocks ---
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.2)
+        self.proc.terminate()
+        self.proc.wait()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((float(r[3]) for r in rows
+                                    if r[3].replace(".", "").isdigit()), default=None)}
+
+
+# ------------------------------------------------------------------ CPU legs ---
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_step(w_host, n: int, s: int, nthreads: int, s_sample: int) -> tuple[float, dict]:
+    """One step of the CPU path: full PSA build of n weights + s_sample alias samples,
+    extrapolated to s samples.  Returns (seconds per step, description)."""
+    from oracle.oracle import RNG_PHILOX4X32_10, SPLIT_F64, SPLIT_FULL_LIGHT, Oracle
+    orc = Oracle()
+    t0 = time.perf_counter()
+    table, _, _ = orc.psa_build(w_host, 2, nthreads=nthreads, flags=SPLIT_F64 | SPLIT_FULL_LIGHT)
+    t1 = time.perf_counter()
+    orc.alias_sample(table, s_sample, 7, rng=RNG_PHILOX4X32_10, nthreads=nthreads)
+    t2 = time.perf_counter()
+    t_step = (t1 - t0) + (t2 - t1) * (s / s_sample)
+    return t_step, {"build_s": t1 - t0, "sample_s": t2 - t1, "samples_timed": s_sample}
+
+
+def cpu_kind() -> str:
+    from oracle.oracle import Reference
+    return "reference" if Reference.available() else "port"
+
+
+def run_reference(args) -> None:
+    """--impl reference: the reference path's CPU implementation on all host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+    import torch
+    n, s = 1 << args.log2n, 1 << args.log2s
+    nthreads = cpu_threads()
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    hosts = [make_weights(d, n, SEEDS[d], dev).cpu().numpy() for d in range(3)]
+    s_sample = 1 << min(args.log2s, 25)
+    for k in range(args.warmup):
+        cpu_step(hosts[k % 3], n, s, nthreads, s_sample)
+    times, descs = [], []
+    for k in range(args.steps):
+        t, d = cpu_step(hosts[k % 3], n, s, nthreads, s_sample)
+        times.append(t)
+        descs.append(d)
+    total = sum(times)
+    value = args.steps * s / total
+    kind = "port"  # the oracle's restatement; the reference's CPU code has no sampler API
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "samples/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "N": n, "S": s, "split_size": 2,
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": "samples/s", "cores": nthreads, "kind": kind,
+                         "sample": f"per step: full PSA build of N=2^{args.log2n} + "
+                                   f"{s_sample} alias samples timed, sampling extrapolated to "
+                                   f"S=2^{args.log2s}; {nthreads} threads"},
+        "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "cpu_build_s_mean": statistics.mean(d["build_s"] for d in descs),
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU ---
+
+def main() -> None:
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    pkg = importlib.import_module("merian-wrs_gb300")
+    pkg.build()
+    W = pkg.wrs
+    n, s = 1 << args.log2n, 1 << args.log2s
+    cfg = W.AliasTableConfig(split_size=2, rng=W.RNG_PHILOX4X32_10,
+                             scan_precision=W.SCAN_COMPENSATED, split_residual_f64=True,
+                             split_full_light=True)
+    wrs = W.WRS(cfg)
+    stream = torch.cuda.current_stream()
+    dev = torch.device("cuda", local)
+    weights = [make_weights(d, n, SEEDS[d] + 1000 * rank, dev) for d in range(3)]
+    internals = W.Internals(wrs.handle, n)
+    samples = torch.empty(s, dtype=torch.int32, device=dev)
+    bufs = [W.WRSBuffers(weights[d], samples, internals) for d in range(3)]
+
+    def step(k: int, ev=None):
+        b = bufs[k % 3]
+        if ev is not None:
+            ev[0].record(stream)
+        wrs.build(stream, b, n)
+        if ev is not None:
+            ev[1].record(stream)
+        wrs.sample(stream, b, n, s, seed=1234 + k)
+        if ev is not None:
+            ev[2].record(stream)
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    assert internals.status() == 0, "device status raised during warm-up"
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    clocks = Clocks(local)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    clocks.start()
+    e_start.record(stream)
+    for k in range(args.steps):
+        step(k, evs[k])
+    e_end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier()
+    elapsed_ms = e_start.elapsed_time(e_end)
+    build_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    sample_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    if dist is not None:
+        t = torch.tensor([elapsed_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    value = world * args.steps * s / (elapsed_ms / 1e3)
+    status = internals.status()
+    assert status == 0, f"device status {status} after the timed region"
+
+    # ---- end to end through the C ABI with host buffers
+    host_w = [weights[d].cpu().pin_memory() for d in range(3)]
+    host_s = torch.empty(s, dtype=torch.int32).pin_memory()
+    dev_w = torch.empty(n, dtype=torch.float32, device=dev)
+    e2e_bufs = W.WRSBuffers(dev_w, samples, internals)
+
+    def e2e_step(k: int):
+        dev_w.copy_(host_w[k % 3], non_blocking=True)
+        wrs.build(stream, e2e_bufs, n)
+        wrs.sample(stream, e2e_bufs, n, s, seed=1234 + k)
+        host_s.copy_(samples, non_blocking=True)
+
+    for k in range(min(args.warmup, 2)):
+        e2e_step(k)
+    barrier()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(args.steps):
+        e2e_step(k)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = t0.elapsed_time(t1)
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * args.steps * s / (e2e_ms / 1e3)
+
+    # ---- roofline of the dominant kernel (alias sampling)
+    pk = peaks()
+    samp_s = statistics.mean(sample_ms) / 1e3
+    achieved = 12.0 * s / samp_s / 1e9
+    traffic = profiled_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+                "kernel": "k_alias_sample", "bytes_model": "12 B/sample (8 B entry + 4 B index)",
+                "peak_source": pk["source"],
+                "sector_model_frac": (36.0 * s / samp_s / 1e9) / pk["hbm_gbs"]}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "N": n, "S": s, "split_size": 2,
+                   "rng": "philox4x32-10", "scan": "fp32 + two-sum carry",
+                   "split": "fp64 residual, light cap fixed",
+                   "l2": "inputs larger than L2 (256 MB weights, 512 MB table, 1 GB samples)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 4 * n,
+                "d2h_bytes_per_step": 4 * s},
+        "roofline": roofline,
+        "alias_builds_per_s": world / (statistics.mean(build_ms) / 1e3),
+        "build_ms_mean": statistics.mean(build_ms),
+        "sample_ms_mean": statistics.mean(sample_ms),
+        "clocks": clk,
+        "gpu_launches": 4 * args.steps,
+    }
+
+    if not args.no_extras:
+        line["kernels"] = kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s,
+                                           stream, pk["hbm_gbs"], args)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        w0 = weights[0].cpu().numpy()
+        s_sample = 1 << min(args.log2s, 25)
+        t_step, desc = cpu_step(w0, n, s, 1, s_sample)
+        line["cpu_baseline"] = {
+            "value": s / t_step, "unit": "samples/s", "cores": 1, "kind": "port",
+            "sample": f"PSA build of N=2^{args.log2n} uniform weights ({desc['build_s']:.2f} s) "
+                      f"+ {s_sample} alias samples ({desc['sample_s']:.2f} s), sampling "
+                      f"extrapolated to S=2^{args.log2s}; 1 thread"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, peak, args):
+    """Each kernel of the path timed alone (CUDA events, mean of 5 launches after 2 warm-up
+    launches) with its algorithmic bytes."""
+    import torch
+    v = internals.views()
+    reps = 5
+    out = {}
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps / 1e3
+
+    w = weights[0]
+    idx, prefix, elems, table = (v["partition_indices"], v["partition_prefix"],
+                                 v["partition_elements"], v["alias_table"])
+
+    def rec(name, sec, nbytes, units, unit_name):
+        out[name] = {"ms": sec * 1e3, "GB/s": nbytes / sec / 1e9, "frac": nbytes / sec / 1e9 / peak,
+                     f"{unit_name}/s": units / sec, "bytes_per_unit": nbytes / units}
+
+    rec("total_mass", timed(lambda: wrs.total_mass(stream, w, n, internals)), 4 * n, n, "weights")
+    rec("prefix_partition",
+        timed(lambda: wrs.prefix_partition(stream, w, n, idx, prefix, elems, internals)),
+        16 * n, n, "weights")
+    rec("split_pack",
+        timed(lambda: wrs.split_pack(stream, w, idx, prefix, elems, n, table, internals)),
+        16 * n, n, "weights")
+    rec("alias_sample",
+        timed(lambda: wrs.alias_sample(stream, table, n, s, 99, 0, samples)), 12 * s, s,
+        "samples")
+    its = W.WRS(W.ITSConfig(rng=W.RNG_PHILOX4X32_10, scan_precision=W.SCAN_COMPENSATED))
+    cmf = torch.empty(n, dtype=torch.float32, device=w.device)
+    rec("scan", timed(lambda: its.prefix_sum(stream, w, n, cmf, internals)), 8 * n, n, "weights")
+    rec("its_sample", timed(lambda: its.its_sample(stream, cmf, n, s, 99, 0, samples)), 4 * s, s,
+        "samples")
+    assert internals.status() == 0
+    return out
+
+
+if __name__ == "__main__":
+    main()

@@ -97,7 +97,8 @@ typedef struct wrs_config {
     uint32_t its_parray;             /* ITS: InverseTransformSamplingConfig::pArraySearch */
     uint32_t rng;                    /* wrs_rng */
     uint32_t scan_precision;         /* wrs_scan_precision */
-    uint32_t split_residual_f64;     /* PSA split target / sigma / spill in FP64 */
+    uint32_t split_residual_f64;     /* PSA split-point residual (spill) in FP64; the search
+                                        keeps the shader's FP32 comparisons */
     uint32_t split_full_light;       /* PSA split caps the light count at lightCount instead of
                                         the shader's lightCount - 1
                                         (splitpack/inline/shader.comp:90,104), which at the end

@@ -599,27 +599,23 @@ __device__ __forceinline__ float elem_at(const PackIn& c, uint32_t pos) {
 }
 
 // splitpack/inline/shader.comp:81-114: bisection over the number of heavy items with the
-// shader's probe sequence (a = 0, b = heavyCount - 1, j = (a + b) / 2).  R64 evaluates
-// target, sigma and spill in FP64.  The light count is capped at c.lcap: lightCount - 1 as
-// in the shader, or lightCount (which keeps i + j = n at the end of the table).  If every
-// probe exceeds the target (the shader's b would wrap), j = 0.
+// shader's probe sequence (a = 0, b = heavyCount - 1, j = (a + b) / 2) and its FP32
+// comparisons, so split points match the shader's.  R64 evaluates the split-point
+// residual (the spill) in FP64 and rounds it once.  The light count is capped at c.lcap:
+// lightCount - 1 as in the shader, or lightCount (which keeps i + j = n at the end of the
+// table).  If every probe exceeds the target (the shader's b would wrap), j = 0.
 template <bool R64>
 __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, uint32_t& io,
                                               uint32_t& jo, float& spill) {
     int64_t a = 0, b = static_cast<int64_t>(c.hc) - 1;
     const float target = __fmul_rn(c.mean, __uint2float_rn(nsplit));
-    const double target64 = __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit));
     const uint32_t lcm1 = c.lcap;
     while (a <= b) {
         const uint32_t j = static_cast<uint32_t>((a + b) >> 1);
         const uint32_t i = j > nsplit ? lcm1 : min(nsplit - j, lcm1);
         const float heavy = j == 0 ? 0.f : __ldg(c.prefix + j - 1);
         const float light = i == 0 ? 0.f : __ldg(c.prefix + c.n - i);
-        bool le;
-        if constexpr (R64)
-            le = __dadd_rn(static_cast<double>(light), static_cast<double>(heavy)) <= target64;
-        else
-            le = __fadd_rn(light, heavy) <= target;
+        const bool le = __fadd_rn(light, heavy) <= target;
         if (le)
             a = static_cast<int64_t>(j) + 1;
         else
@@ -629,10 +625,12 @@ __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, 
     const uint32_t i = j > nsplit ? lcm1 : min(nsplit - j, lcm1);
     const float light = i == 0 ? 0.f : __ldg(c.prefix + c.n - i);
     const float heavy2 = __ldg(c.prefix + j);
-    if constexpr (R64)
+    if constexpr (R64) {
+        const double target64 =
+            __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit));
         spill = __double2float_rn(
             __dsub_rn(__dadd_rn(static_cast<double>(heavy2), static_cast<double>(light)), target64));
-    else
+    } else
         spill = __fsub_rn(__fadd_rn(heavy2, light), target);
     io = i;
     jo = j;

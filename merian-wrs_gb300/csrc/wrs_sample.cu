@@ -9,9 +9,13 @@
 //                key = seed for the alias method; wang_hash(seed + gid) for ITS.  Indices
 //                are bit-exact with the shaders' arithmetic.
 //   RNG_PHILOX   Random123 Philox4x32-10, key = (seed lo, seed hi), counter = (sample
-//                index lo, hi, 0, 0).  Alias: ix = mulhi(x0, N), coin = (x1 >> 8) * 2^-24,
-//                alias when coin >= p.  ITS: u = (2*(x0 >> 9) + 1) * 2^-24 in (0,1),
-//                target = u * cmf[N-1], lower bound over the CMF.
+//                index lo, hi, 0, 0).  Alias: ix = mulhi(x0, N); the bucket keeps ix when
+//                p >= 1 or x1 < ceil(p * 2^32), else returns its alias (32-bit coin).
+//                ITS: target T = (2*x0 + 1) * cmf[N-1] * 2^-33 in (0, total), formed
+//                exactly in 64-bit integers and kept as its FP32 rounding plus the sign of
+//                the rounding residual, so every probe "T > cmf[mid]" is decided exactly
+//                with one FP32 compare; result = first index with cmf >= T.  Zero-weight
+//                items can never be drawn.
 #include "wrs_device.cuh"
 #include "wrs_internal.cuh"
 
@@ -74,20 +78,23 @@ __global__ __launch_bounds__(kSampleThreads) void k_alias_sample(const uint2* __
         philox4x32_10_keys(seed, ks);
         uint2 ent[kAliasPerThread];
         uint32_t ixs[kAliasPerThread];
-        float us[kAliasPerThread];
+        uint32_t coin[kAliasPerThread];
 #pragma unroll
         for (int v = 0; v < kAliasPerThread; ++v) {
             const uint64_t g = offset + s0 + v;
             const uint4 x = philox4x32_10(
                 make_uint4(static_cast<uint32_t>(g), static_cast<uint32_t>(g >> 32), 0u, 0u), ks);
             ixs[v] = __umulhi(x.x, n);
-            us[v] = __fmul_rn(__uint2float_rn(x.y >> 8), 5.9604644775390625e-08f);
+            coin[v] = x.y;
         }
 #pragma unroll
         for (int v = 0; v < kAliasPerThread; ++v) ent[v] = ld_entry(table + ixs[v]);
 #pragma unroll
-        for (int v = 0; v < kAliasPerThread; ++v)
-            r[v] = us[v] >= __uint_as_float(ent[v].x) ? ent[v].y : ixs[v];
+        for (int v = 0; v < kAliasPerThread; ++v) {
+            const float p = __uint_as_float(ent[v].x);
+            const bool keep = p >= 1.0f || coin[v] < __float2uint_ru(__fmul_rn(p, 4294967296.0f));
+            r[v] = keep ? ixs[v] : ent[v].y;
+        }
     }
     if (s0 + kAliasPerThread <= S && (reinterpret_cast<uintptr_t>(out) & 15u) == 0) {
         __stcs(reinterpret_cast<uint4*>(out + s0), make_uint4(r[0], r[1], r[2], r[3]));
@@ -112,6 +119,55 @@ __device__ __forceinline__ uint32_t bisect(const float* __restrict__ cmf, uint32
     while (x < y) {
         const uint32_t mid = x + ((y - x) >> 1);
         if (u > __ldg(cmf + mid))
+            x = mid + 1;
+        else
+            y = mid;
+    }
+    return x;
+}
+
+// T = (2x + 1) * total * 2^-33 as (t_hi = T rounded to nearest FP32, t_sgn = sign(T - t_hi)).
+// total = Mt * 2^Et with a 24-bit integer Mt; P = (2x + 1) * Mt < 2^57 is exact in 64 bits.
+__device__ __forceinline__ void exact_target(uint32_t x, float total, float& t_hi, int& t_sgn) {
+    const uint32_t tb = __float_as_uint(total);
+    const int e = static_cast<int>((tb >> 23) & 0xffu);
+    const uint64_t mt = e ? ((tb & 0x7fffffu) | 0x800000u) : (tb & 0x7fffffu);
+    const int et = (e ? e : 1) - 150;
+    const uint64_t P = (2ull * x + 1ull) * mt;
+    if (P == 0) {
+        t_hi = 0.0f;
+        t_sgn = 0;
+        return;
+    }
+    const int bits = 64 - __clzll(static_cast<long long>(P));
+    int sh = bits > 24 ? bits - 24 : 0;
+    uint64_t mant = P >> sh;
+    int sgn = 0;
+    if (sh > 0) {
+        const uint64_t rem = P & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (mant & 1ull))) {
+            ++mant;
+            sgn = -1;
+        } else {
+            sgn = rem ? 1 : 0;
+        }
+        if (mant == (1ull << 24)) {
+            mant >>= 1;
+            ++sh;
+        }
+    }
+    t_hi = ldexpf(static_cast<float>(mant), et - 33 + sh);
+    t_sgn = sgn;
+}
+
+// first index in [0, last] with cmf >= T, bisecting like its/sampling/shader.comp:131-140
+__device__ __forceinline__ uint32_t bisect_exact(const float* __restrict__ cmf, uint32_t last,
+                                                 float t_hi, int t_sgn) {
+    uint32_t x = 0, y = last;
+    while (x < y) {
+        const uint32_t mid = x + ((y - x) >> 1);
+        const float c = __ldg(cmf + mid);
+        if (t_hi > c || (t_hi == c && t_sgn > 0))
             x = mid + 1;
         else
             y = mid;
@@ -181,9 +237,10 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample(const float* __re
         const uint64_t g = offset + s;
         const uint4 r = philox4x32_10(
             make_uint4(static_cast<uint32_t>(g), static_cast<uint32_t>(g >> 32), 0u, 0u), ks);
-        const float u = __fmul_rn(__uint2float_rn((r.x >> 9) * 2u + 1u), 5.9604644775390625e-08f);
-        const float target = __fmul_rn(u, __ldg(cmf + n - 1u));
-        res = bisect(cmf, 0, n - 1u, target);
+        float t_hi;
+        int t_sgn;
+        exact_target(r.x, __ldg(cmf + n - 1u), t_hi, t_sgn);
+        res = bisect_exact(cmf, n - 1u, t_hi, t_sgn);
     }
     if (s < S) __stcs(out + s, res);
 }

@@ -27,6 +27,7 @@
  */
 #include "wrs_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
@@ -217,9 +218,10 @@ void wrso_prefix_seq_f32(const float* w, uint64_t N, float* out) {
 }
 
 /* splitpack/inline/shader.comp:81-114 (computeSplit).  Bisection over the number
- * of heavy items j in [0, heavyCount-1] with the shader's exact probe sequence.
- * flags & WRSO_SPLIT_F64: evaluate target, sigma and spill in FP64 (the spill is then
- * rounded once to FP32) instead of the shader's FP32.
+ * of heavy items j in [0, heavyCount-1] with the shader's exact probe sequence and FP32
+ * comparisons.
+ * flags & WRSO_SPLIT_F64: evaluate the split-point residual (the spill) in FP64 and round
+ * it once to FP32, instead of the shader's FP32 spill.
  * flags & WRSO_SPLIT_FULL_LIGHT: cap the light count at lightCount instead of the
  * shader's lightCount - 1 (shader.comp:90,104).  With the shader's cap a split near the
  * end of the table can have i + j < n, after which the last heavy bucket aliases a light
@@ -239,14 +241,8 @@ void wrso_split(const float* prefix, uint32_t N, uint32_t hc, float mean, uint32
         uint32_t i = (j > n) ? lcap : ((n - j) < lcap ? (n - j) : lcap);
         float heavy = j == 0 ? 0.0f : prefix[j - 1];
         float light = i == 0 ? 0.0f : prefix[N - i];
-        int le;
-        if (residual_f64) {
-            le = ((double)light + (double)heavy) <= target64;
-        } else {
-            volatile float sigma = light + heavy;
-            le = sigma <= target;
-        }
-        if (le)
+        volatile float sigma = light + heavy;
+        if (sigma <= target)
             a = (int64_t)j + 1;
         else
             b = (int64_t)j - 1;
@@ -617,8 +613,11 @@ static void alias_task(void* p, int t, int nt) {
                 uint32_t ctr[4] = {(uint32_t)g, (uint32_t)(g >> 32), 0u, 0u}, r[4];
                 wrso_philox4x32_10(ctr, key, r);
                 uint32_t ix = (uint32_t)(((uint64_t)r[0] * (uint64_t)N) >> 32);
-                float u = (float)(r[1] >> 8) * 5.9604644775390625e-08f;
-                c->out[s] = u >= table[ix].p ? table[ix].a : ix;
+                /* keep ix when p >= 1 or x1 < ceil(p * 2^32) (32-bit coin) */
+                float p = table[ix].p;
+                int keep = p >= 1.0f;
+                if (!keep && p > 0.0f) keep = (double)r[1] < ceil((double)p * 4294967296.0);
+                c->out[s] = keep ? ix : table[ix].a;
             }
         }
     }
@@ -644,6 +643,22 @@ static inline uint32_t wrso_bisect(const float* cmf, uint32_t x, uint32_t y, flo
     while (x < y) {
         uint32_t mid = (uint32_t)(((uint64_t)x + y) / 2);
         if (u > cmf[mid])
+            x = mid + 1;
+        else
+            y = mid;
+    }
+    return x;
+}
+
+/* Philox ITS: first index with cmf >= T for the exact target T = (2 x0 + 1) * total * 2^-33,
+ * bisecting like its/sampling/shader.comp:131-140.  T has at most 57 significant bits and
+ * is held exactly in long double (64-bit significand on x86-64, 113-bit on aarch64). */
+_Static_assert(LDBL_MANT_DIG >= 57, "the exact ITS target needs a >= 57-bit long double");
+static uint32_t wrso_bisect_exact(const float* cmf, uint32_t last, long double T) {
+    uint32_t x = 0, y = last;
+    while (x < y) {
+        uint32_t mid = (uint32_t)(((uint64_t)x + y) / 2);
+        if (T > (long double)cmf[mid])
             x = mid + 1;
         else
             y = mid;
@@ -713,10 +728,7 @@ static void its_task(void* p, int t, int nt) {
                 uint64_t g = c->offset + s;
                 uint32_t ctr[4] = {(uint32_t)g, (uint32_t)(g >> 32), 0u, 0u}, r[4];
                 wrso_philox4x32_10(ctr, key, r);
-                /* u in (0,1): odd multiples of 2^-24, exact in FP32 */
-                float u = (float)((r[0] >> 9) * 2u + 1u) * 5.9604644775390625e-08f;
-                volatile float tgt = u * total;
-                c->out[s] = wrso_bisect(cmf, 0, N - 1, tgt);
+                c->out[s] = wrso_bisect_exact(cmf, N - 1, (2.0L * r[0] + 1.0L) * total / 8589934592.0L);
             }
         }
     }
