@@ -640,8 +640,30 @@ __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, 
 // write (:212-222) is not performed: in subproblem order it is always overwritten by the
 // final subproblem, which packs the last heavy item itself (the oracle keeps the write and
 // the parity tests confirm the tables agree).
+//
+// Subproblems normally cover disjoint items.  Where FP32 rounding makes a split step back
+// (split_{k+1} < split_k, one or two items at N >= 2^22), two subproblems pack the same
+// items and, in subproblem order, the later one's write stands.  `later` (null when the
+// next kSplitLook splits do not step back into this subproblem's range) lists the splits of
+// the following subproblems; an entry is then written only if none of them covers it.
+struct LaterSplits {
+    const uint32_t* si;  // shared-memory split arrays of the CTA
+    const uint32_t* sj;
+    int t;               // this subproblem's slot
+    int count;           // later subproblems inside the window
+};
+
+__device__ __forceinline__ bool covered_later(const LaterSplits& L, uint32_t item, bool light) {
+    const uint32_t* s = light ? L.si : L.sj;
+    for (int d = 1; d <= L.count; ++d) {
+        const uint32_t a = s[L.t + d], b = max(s[L.t + d + 1], a);
+        if (a <= item && item < b) return true;
+    }
+    return false;
+}
+
 __device__ void pack(const PackIn& c, uint2* __restrict__ table, uint32_t i0, uint32_t i1,
-                     uint32_t j0, uint32_t j1, float spill) {
+                     uint32_t j0, uint32_t j1, float spill, const LaterSplits* later) {
     uint32_t i = i0, j = j0;
     float wv = spill;
     if (wv == 0.0f) wv = elem_at(c, j);
@@ -662,25 +684,32 @@ __device__ void pack(const PackIn& c, uint2* __restrict__ table, uint32_t i0, ui
         const float weight = c.elems ? __ldg(c.elems + pos) : (widx < c.n ? __ldg(c.w + widx) : 0.f);
         float p;
         uint32_t tidx, al;
+        bool owned = true;
         if (heavy_step) {
             p = __fdiv_rn(wv, c.mean);
             al = widx;
             tidx = h;
+            if (later) owned = !covered_later(*later, j, false);
             ++j;
         } else {
             p = __fdiv_rn(weight, c.mean);
             al = h;
             tidx = widx;
+            if (later) owned = !covered_later(*later, i, true);
             ++i;
         }
-        if (tidx < c.n) table[tidx] = make_uint2(__float_as_uint(p), al);
+        if (owned && tidx < c.n) table[tidx] = make_uint2(__float_as_uint(p), al);
         wv = __fsub_rn(__fadd_rn(wv, weight), c.mean);
     }
 }
 
-// Thread t of CTA b computes split k = b*(kSplitThreads-1) + t (k in [0, K]) and packs
-// subproblem k = [split_k, split_{k+1}) for t < kSplitThreads-1, k < K; split_{k+1} comes
-// from the neighbouring thread through shared memory (shader.comp:225-270).
+// Thread t of CTA b computes split k = b*kSplitPack + t (k in [0, K]) and packs subproblem
+// k = [split_k, split_{k+1}) for t < kSplitPack, k < K; split_{k+1} comes from the
+// neighbouring thread through shared memory (shader.comp:225-270).  The last
+// kSplitLook + 1 threads only compute look-ahead splits for the ownership window.
+constexpr int kSplitLook = 8;
+constexpr int kSplitPack = kSplitThreads - kSplitLook - 1;
+
 template <bool R64>
 __global__ __launch_bounds__(kSplitThreads) void k_split_pack(
     const float* __restrict__ w, const uint32_t* __restrict__ idx,
@@ -698,17 +727,12 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(
         return;
     }
     PackIn c{w, idx, elems, prefix, n, hc, n - hc, full_light ? n - hc : n - hc - 1u, ctrl->mean};
-    const uint32_t k = blockIdx.x * (kSplitThreads - 1) + threadIdx.x;
-    uint32_t si = 0, sj = 0;
+    const uint32_t k = blockIdx.x * kSplitPack + threadIdx.x;
+    uint32_t si = c.lc, sj = hc;  // past split K: the final split
     float sp = 0.f;
     if (k == 0u) {
         si = 0;
         sj = 0;
-        sp = 0.f;
-    } else if (k == K) {
-        si = c.lc;
-        sj = hc;
-        sp = 0.f;
     } else if (k < K) {
         compute_split<R64>(c, k * split_size, si, sj, sp);
     }
@@ -716,10 +740,18 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(
     s_j[threadIdx.x] = sj;
     s_spill[threadIdx.x] = sp;
     __syncthreads();
-    if (threadIdx.x == kSplitThreads - 1 || k >= K) return;
-    const uint32_t ni = s_i[threadIdx.x + 1], nj = s_j[threadIdx.x + 1];
-    if (ni < si || nj < sj) atomicOr(status, kStatusNonMonotone);
-    pack(c, table, si, max(ni, si), sj, max(nj, sj), sp);
+    const int t = threadIdx.x;
+    if (t >= kSplitPack || k >= K) return;
+    const uint32_t i1 = max(s_i[t + 1], si), j1 = max(s_j[t + 1], sj);
+    const int count = static_cast<int>(min(static_cast<uint32_t>(kSplitLook), K - 1u - k));
+    bool clean = true;
+    for (int d = 1; d <= count; ++d)
+        clean = clean && s_i[t + d] >= i1 && s_j[t + d] >= j1;
+    // a step back reaching past the window cannot be resolved here: report it
+    if (k + kSplitLook + 1u < K && (s_i[t + kSplitLook + 1] < i1 || s_j[t + kSplitLook + 1] < j1))
+        atomicOr(status, kStatusNonMonotone);
+    const LaterSplits later{s_i, s_j, t, count};
+    pack(c, table, si, i1, sj, j1, sp, clean ? nullptr : &later);
 }
 
 cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const float* w,
@@ -728,7 +760,7 @@ cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const 
                               uint32_t split_size, uint2* table) {
     uint32_t K = n / split_size;
     if (K == 0) K = 1;
-    const uint32_t blocks = (K + kSplitThreads - 2) / (kSplitThreads - 1);
+    const uint32_t blocks = (K + kSplitPack - 1) / kSplitPack;
     if (r64)
         k_split_pack<true><<<blocks, kSplitThreads, 0, st>>>(w, idx, elems, prefix, ctrl, status,
                                                              n, K, split_size, full_light, table);

@@ -120,10 +120,28 @@ def test_split_pack_bit_exact(pkg, cuda, oracle, split_size, flags, gen):
     cfg = pkg.AliasTableConfig(split_size=split_size, split_residual_f64=bool(flags & 1),
                                split_full_light=bool(flags & 2))
     b = Built(pkg, w, cfg)
-    assert b.status & pkg.wrs.DEVICE_TIMEOUT == 0
+    assert b.status == 0
     ref = oracle.split_pack(w, b.idx, b.prefix, b.hc, b.mean, split_size, flags=flags,
                             elems=b.elems)
     assert same_table(b.table, ref)
+
+
+@pytest.mark.parametrize("gen", list(GENS))
+@pytest.mark.parametrize("comp", [False, True])
+def test_split_pack_overlapping_subproblems(pkg, cuda, oracle, gen, comp):
+    """At N ~ 2^22 with split size 2, FP32 rounding makes some splits step back so that two
+    subproblems pack the same items; the table still equals the oracle's sequential
+    subproblem order (the later subproblem's write stands) and no unresolved overlap is
+    reported."""
+    N = (1 << 22) + 17
+    w = GENS[gen](N, 99)
+    b = Built(pkg, w, pkg.AliasTableConfig(scan_precision=1 if comp else 0))
+    assert b.status == 0
+    ref, (si, sj, _) = oracle.split_pack(w, b.idx, b.prefix, b.hc, b.mean, 2, elems=b.elems,
+                                         return_splits=True)
+    steps_back = np.count_nonzero((np.diff(si.astype(np.int64)) < 0) |
+                                  (np.diff(sj.astype(np.int64)) < 0))
+    assert same_table(b.table, ref), f"{steps_back} splits step back"
 
 
 @pytest.mark.parametrize("use_elems", [False, True])
