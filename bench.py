@@ -265,7 +265,8 @@ def main() -> None:
     for k in range(args.warmup):
         step(k)
     torch.cuda.synchronize()
-    assert internals.status() == 0, "device status raised during warm-up"
+    dev_status = internals.status()
+    assert not dev_status & W.DEVICE_TIMEOUT, "a lookback wait gave up during warm-up"
 
     def barrier():
         if dist is not None:
@@ -293,8 +294,8 @@ def main() -> None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed_ms = float(t.item())
     value = world * args.steps * s / (elapsed_ms / 1e3)
-    status = internals.status()
-    assert status == 0, f"device status {status} after the timed region"
+    dev_status |= internals.status()
+    assert not dev_status & W.DEVICE_TIMEOUT, "a lookback wait gave up in the timed region"
 
     # ---- end to end through the C ABI with host buffers
     host_w = [weights[d].cpu().pin_memory() for d in range(3)]
@@ -354,6 +355,8 @@ def main() -> None:
         "sample_ms_mean": statistics.mean(sample_ms),
         "clocks": clk,
         "gpu_launches": 4 * args.steps,
+        "device_status": {"timeout": bool(dev_status & W.DEVICE_TIMEOUT),
+                          "split_overlap_beyond_window": bool(dev_status & W.DEVICE_NONMONOTONE_SPLIT)},
     }
 
     if not args.no_extras:
@@ -416,7 +419,7 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
     rec("scan", timed(lambda: its.prefix_sum(stream, w, n, cmf, internals)), 8 * n, n, "weights")
     rec("its_sample", timed(lambda: its.its_sample(stream, cmf, n, s, 99, 0, samples)), 4 * s, s,
         "samples")
-    assert internals.status() == 0
+    assert not internals.status() & W.DEVICE_TIMEOUT
     return out
 
 
