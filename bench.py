@@ -241,7 +241,7 @@ def main() -> None:
     W = pkg.wrs
     n, s = 1 << args.log2n, 1 << args.log2s
     cfg = W.AliasTableConfig(split_size=2, rng=W.RNG_PHILOX4X32_10,
-                             scan_precision=W.SCAN_COMPENSATED, split_residual_f64=True,
+                             scan_precision=W.SCAN_FLOAT_FLOAT, split_residual_f64=True,
                              split_full_light=True)
     wrs = W.WRS(cfg)
     stream = torch.cuda.current_stream()
@@ -397,19 +397,22 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
         return e0.elapsed_time(e1) / reps / 1e3
 
     w = weights[0]
-    idx, prefix, elems, table = (v["partition_indices"], v["partition_prefix"],
-                                 v["partition_elements"], v["alias_table"])
+    idx, prefix, elems, table, lo = (v["partition_indices"], v["partition_prefix"],
+                                     v["partition_elements"], v["alias_table"],
+                                     v["partition_prefix_lo"])
 
     def rec(name, sec, nbytes, units, unit_name):
         out[name] = {"ms": sec * 1e3, "GB/s": nbytes / sec / 1e9, "frac": nbytes / sec / 1e9 / peak,
                      f"{unit_name}/s": units / sec, "bytes_per_unit": nbytes / units}
 
     rec("total_mass", timed(lambda: wrs.total_mass(stream, w, n, internals)), 4 * n, n, "weights")
+    # read w 4 + write index 4 + prefix 4 + element 4 + prefix low word 4
     rec("prefix_partition",
-        timed(lambda: wrs.prefix_partition(stream, w, n, idx, prefix, elems, internals)),
-        16 * n, n, "weights")
+        timed(lambda: wrs.prefix_partition(stream, w, n, idx, prefix, elems, internals, lo)),
+        20 * n, n, "weights")
+    # read index 4 + element 4 + write entry 8 (split probes assumed L2-resident)
     rec("split_pack",
-        timed(lambda: wrs.split_pack(stream, w, idx, prefix, elems, n, table, internals)),
+        timed(lambda: wrs.split_pack(stream, w, idx, prefix, elems, n, table, internals, lo)),
         16 * n, n, "weights")
     rec("alias_sample",
         timed(lambda: wrs.alias_sample(stream, table, n, s, 99, 0, samples)), 12 * s, s,

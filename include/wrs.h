@@ -79,8 +79,12 @@ typedef enum wrs_rng {
 } wrs_rng;
 
 typedef enum wrs_scan_precision {
-    WRS_SCAN_FP32 = 0,        /* FP32 carry through the lookback, as the reference */
-    WRS_SCAN_COMPENSATED = 1  /* FP32 with a two-sum (float-float) carry */
+    WRS_SCAN_FP32 = 0,         /* FP32 carry through the lookback, as the reference */
+    WRS_SCAN_COMPENSATED = 1,  /* FP32 with a two-sum (float-float) carry */
+    WRS_SCAN_FLOAT_FLOAT = 2   /* alias method: compensated carry, and the partition prefix is
+                                  kept as a float-float pair (an extra low-word array) so the
+                                  split search decides on exact sums and the split residual
+                                  is exact to FP64 rounding; ITS: as COMPENSATED */
 } wrs_scan_precision;
 
 /* device status bits (wrs_buffers_status) */
@@ -150,6 +154,7 @@ const float* wrs_buffers_cmf(const wrs_buffers* b);
 const uint32_t* wrs_buffers_partition_indices(const wrs_buffers* b);
 const float* wrs_buffers_partition_prefix(const wrs_buffers* b);
 const float* wrs_buffers_partition_elements(const wrs_buffers* b);
+const float* wrs_buffers_partition_prefix_lo(const wrs_buffers* b); /* FLOAT_FLOAT only */
 const float* wrs_buffers_mean(const wrs_buffers* b);        /* 1 float */
 const double* wrs_buffers_total(const wrs_buffers* b);      /* 1 double */
 const uint32_t* wrs_buffers_heavy_count(const wrs_buffers* b); /* 1 uint32 */
@@ -159,16 +164,18 @@ wrs_status wrs_total_mass(const wrs_handle* h, void* stream, const float* weight
                           wrs_buffers* b);
 wrs_status wrs_prefix_sum(const wrs_handle* h, void* stream, const float* in, uint32_t n,
                           float* out, wrs_buffers* b);
-/* pivot = the mean held in b (run wrs_total_mass first); heavy count lands in b */
+/* pivot = the mean held in b (run wrs_total_mass first); heavy count lands in b.
+ * partition_elements may be NULL; partition_prefix_lo (the low words of the float-float
+ * prefix) must be non-NULL exactly when the handle's precision is WRS_SCAN_FLOAT_FLOAT. */
 wrs_status wrs_prefix_partition(const wrs_handle* h, void* stream, const float* weights,
                                 uint32_t n, uint32_t* partition_indices,
                                 float* partition_prefix, float* partition_elements,
-                                wrs_buffers* b);
-/* mean and heavy count are read from b */
+                                float* partition_prefix_lo, wrs_buffers* b);
+/* mean and heavy count are read from b; pointers as for wrs_prefix_partition */
 wrs_status wrs_split_pack(const wrs_handle* h, void* stream, const float* weights,
                           const uint32_t* partition_indices, const float* partition_prefix,
-                          const float* partition_elements, uint32_t n, wrs_alias_entry* table,
-                          wrs_buffers* b);
+                          const float* partition_elements, const float* partition_prefix_lo,
+                          uint32_t n, wrs_alias_entry* table, wrs_buffers* b);
 wrs_status wrs_alias_sample(const wrs_handle* h, void* stream, const wrs_alias_entry* table,
                             uint32_t n, uint64_t s, uint64_t seed, uint64_t offset,
                             uint32_t* samples);

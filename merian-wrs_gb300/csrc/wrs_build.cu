@@ -254,12 +254,14 @@ __device__ __forceinline__ void part_publish_pre(PartState* s, const PartCarry& 
 // lane L holds, for v = 0..3, the 4 consecutive items at v*128 + L*4 (16-byte loads, fully
 // coalesced).  Heavy (w > mean) items go to idx[heavyRank], light items to
 // idx[N-1-lightRank]; prefix[] holds the inclusive heavy resp. light prefix sum, elems[] the
-// weight (shader.comp:329-361).
-template <bool COMP>
+// weight (shader.comp:329-361).  FFOUT (with the compensated carry) also writes prefix_lo[],
+// the low word of the prefix as a float-float pair (prefix[] is its high word).
+template <bool COMP, bool FFOUT>
 __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
     const float* __restrict__ w, uint32_t n, BuildCtrl* __restrict__ ctrl,
     PartState* __restrict__ states, uint32_t cap_tiles, uint32_t* __restrict__ idx_out,
-    float* __restrict__ prefix_out, float* __restrict__ elems_out, uint32_t spin_limit) {
+    float* __restrict__ prefix_out, float* __restrict__ elems_out,
+    float* __restrict__ prefix_lo_out, uint32_t spin_limit) {
     __shared__ float s_wh[kTileWarps], s_wl[kTileWarps];
     __shared__ uint32_t s_wc[kTileWarps];
     __shared__ PartCarry s_ex;
@@ -383,20 +385,27 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
             if (e < n) {
                 const float xv = x[v][c];
                 uint32_t pos;
-                float val;
+                ff val;
                 if (xv > pivot) {
                     rh = __fadd_rn(rh, xv);
                     pos = ex.c + rc;
-                    val = carry_apply<COMP>(ex.h, rh);
+                    if constexpr (FFOUT)
+                        val = carry_apply_ff(ex.h, rh);
+                    else
+                        val = {carry_apply<COMP>(ex.h, rh), 0.f};
                     ++rc;
                 } else {
                     rl = __fadd_rn(rl, xv);
                     pos = n - 1u - (light_before + (local - rc));
-                    val = carry_apply<COMP>(ex.l, rl);
+                    if constexpr (FFOUT)
+                        val = carry_apply_ff(ex.l, rl);
+                    else
+                        val = {carry_apply<COMP>(ex.l, rl), 0.f};
                 }
                 if (pos < n) {  // always true unless a lookback wait gave up
                     idx_out[pos] = e;
-                    prefix_out[pos] = val;
+                    prefix_out[pos] = val.hi;
+                    if constexpr (FFOUT) prefix_lo_out[pos] = val.lo;
                     if (elems_out) elems_out[pos] = xv;
                 }
             }
@@ -408,14 +417,19 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
 
 cudaError_t launch_prefix_partition(cudaStream_t st, bool comp, const float* w, uint32_t n,
                                     BuildCtrl* ctrl, PartState* states, uint32_t cap_tiles,
-                                    uint32_t* idx_out, float* prefix_out, float* elems_out) {
+                                    uint32_t* idx_out, float* prefix_out, float* elems_out,
+                                    float* prefix_lo_out) {
     const uint32_t tiles = tiles_for(n);
-    if (comp)
-        k_prefix_partition<true><<<tiles, kTileThreads, 0, st>>>(
-            w, n, ctrl, states, cap_tiles, idx_out, prefix_out, elems_out, kSpinLimit);
+    if (prefix_lo_out)
+        k_prefix_partition<true, true><<<tiles, kTileThreads, 0, st>>>(
+            w, n, ctrl, states, cap_tiles, idx_out, prefix_out, elems_out, prefix_lo_out,
+            kSpinLimit);
+    else if (comp)
+        k_prefix_partition<true, false><<<tiles, kTileThreads, 0, st>>>(
+            w, n, ctrl, states, cap_tiles, idx_out, prefix_out, elems_out, nullptr, kSpinLimit);
     else
-        k_prefix_partition<false><<<tiles, kTileThreads, 0, st>>>(
-            w, n, ctrl, states, cap_tiles, idx_out, prefix_out, elems_out, kSpinLimit);
+        k_prefix_partition<false, false><<<tiles, kTileThreads, 0, st>>>(
+            w, n, ctrl, states, cap_tiles, idx_out, prefix_out, elems_out, nullptr, kSpinLimit);
     return cudaGetLastError();
 }
 
@@ -587,10 +601,20 @@ struct PackIn {
     const uint32_t* idx;
     const float* elems;  // partition-ordered weights, or nullptr (then w[idx[pos]])
     const float* prefix;
+    const float* prefix_lo;  // low words of a float-float prefix, or nullptr
     uint32_t n, hc, lc;
     uint32_t lcap;  // largest light count a split may take: lc - 1 (shader) or lc
     float mean;
 };
+
+// prefix value at position pos as a double: hi only, or hi + lo of the float-float prefix
+template <bool FF>
+__device__ __forceinline__ double prefix64(const PackIn& c, float hi, uint32_t pos) {
+    if constexpr (FF)
+        return __dadd_rn(static_cast<double>(hi), static_cast<double>(__ldg(c.prefix_lo + pos)));
+    else
+        return static_cast<double>(hi);
+}
 
 __device__ __forceinline__ float elem_at(const PackIn& c, uint32_t pos) {
     if (c.elems) return __ldg(c.elems + pos);
@@ -604,18 +628,42 @@ __device__ __forceinline__ float elem_at(const PackIn& c, uint32_t pos) {
 // residual (the spill) in FP64 and rounds it once.  The light count is capped at c.lcap:
 // lightCount - 1 as in the shader, or lightCount (which keeps i + j = n at the end of the
 // table).  If every probe exceeds the target (the shader's b would wrap), j = 0.
-template <bool R64>
+//
+// FF (float-float prefix): the comparison sigma <= target is decided on the exact values --
+// sigma = (hi + lo of the heavy prefix) + (hi + lo of the light prefix) and target = mean * n,
+// both evaluated in FP64 -- instead of on the FP32 high words.  An FP32 pre-test settles every
+// probe whose high words differ by more than a few ulps (bound m = (s + t) * 2^-21), so FP64
+// runs only near the crossing; the spill is then computed from the float-float prefix in
+// FP64 as well.  Split points become monotone in k up to exact ties.
+template <bool R64, bool FF>
 __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, uint32_t& io,
                                               uint32_t& jo, float& spill) {
     int64_t a = 0, b = static_cast<int64_t>(c.hc) - 1;
     const float target = __fmul_rn(c.mean, __uint2float_rn(nsplit));
+    const double target64 = __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit));
     const uint32_t lcm1 = c.lcap;
     while (a <= b) {
         const uint32_t j = static_cast<uint32_t>((a + b) >> 1);
         const uint32_t i = j > nsplit ? lcm1 : min(nsplit - j, lcm1);
         const float heavy = j == 0 ? 0.f : __ldg(c.prefix + j - 1);
         const float light = i == 0 ? 0.f : __ldg(c.prefix + c.n - i);
-        const bool le = __fadd_rn(light, heavy) <= target;
+        const float s32 = __fadd_rn(light, heavy);
+        bool le;
+        if constexpr (FF) {
+            const float d = __fsub_rn(s32, target);
+            const float m = __fmul_rn(__fadd_rn(s32, target), 4.76837158203125e-07f);
+            if (d > m) {
+                le = false;
+            } else if (d < -m) {
+                le = true;
+            } else {
+                const double h64 = j == 0 ? 0.0 : prefix64<true>(c, heavy, j - 1);
+                const double l64 = i == 0 ? 0.0 : prefix64<true>(c, light, c.n - i);
+                le = __dadd_rn(h64, l64) <= target64;
+            }
+        } else {
+            le = s32 <= target;
+        }
         if (le)
             a = static_cast<int64_t>(j) + 1;
         else
@@ -625,13 +673,13 @@ __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, 
     const uint32_t i = j > nsplit ? lcm1 : min(nsplit - j, lcm1);
     const float light = i == 0 ? 0.f : __ldg(c.prefix + c.n - i);
     const float heavy2 = __ldg(c.prefix + j);
-    if constexpr (R64) {
-        const double target64 =
-            __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit));
-        spill = __double2float_rn(
-            __dsub_rn(__dadd_rn(static_cast<double>(heavy2), static_cast<double>(light)), target64));
-    } else
+    if constexpr (R64 || FF) {
+        const double h64 = prefix64<FF>(c, heavy2, j);
+        const double l64 = i == 0 ? 0.0 : prefix64<FF>(c, light, c.n - i);
+        spill = __double2float_rn(__dsub_rn(__dadd_rn(h64, l64), target64));
+    } else {
         spill = __fsub_rn(__fadd_rn(heavy2, light), target);
+    }
     io = i;
     jo = j;
 }
@@ -707,15 +755,15 @@ __device__ void pack(const PackIn& c, uint2* __restrict__ table, uint32_t i0, ui
 // k = [split_k, split_{k+1}) for t < kSplitPack, k < K; split_{k+1} comes from the
 // neighbouring thread through shared memory (shader.comp:225-270).  The last
 // kSplitLook + 1 threads only compute look-ahead splits for the ownership window.
-constexpr int kSplitLook = 8;
 constexpr int kSplitPack = kSplitThreads - kSplitLook - 1;
 
-template <bool R64>
+template <bool R64, bool FF>
 __global__ __launch_bounds__(kSplitThreads) void k_split_pack(
     const float* __restrict__ w, const uint32_t* __restrict__ idx,
     const float* __restrict__ elems, const float* __restrict__ prefix,
-    const BuildCtrl* __restrict__ ctrl, uint32_t* status, uint32_t n, uint32_t K,
-    uint32_t split_size, uint32_t full_light, uint2* __restrict__ table) {
+    const float* __restrict__ prefix_lo, const BuildCtrl* __restrict__ ctrl, uint32_t* status,
+    uint32_t n, uint32_t K, uint32_t split_size, uint32_t full_light,
+    uint2* __restrict__ table) {
     __shared__ uint32_t s_i[kSplitThreads], s_j[kSplitThreads];
     __shared__ float s_spill[kSplitThreads];
     const uint32_t hc = ctrl->heavy_count;
@@ -726,7 +774,8 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(
             table[e] = make_uint2(__float_as_uint(1.0f), e);
         return;
     }
-    PackIn c{w, idx, elems, prefix, n, hc, n - hc, full_light ? n - hc : n - hc - 1u, ctrl->mean};
+    PackIn c{w,  idx,    elems,  prefix, prefix_lo, n, hc,
+             n - hc, full_light ? n - hc : n - hc - 1u, ctrl->mean};
     const uint32_t k = blockIdx.x * kSplitPack + threadIdx.x;
     uint32_t si = c.lc, sj = hc;  // past split K: the final split
     float sp = 0.f;
@@ -734,7 +783,7 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(
         si = 0;
         sj = 0;
     } else if (k < K) {
-        compute_split<R64>(c, k * split_size, si, sj, sp);
+        compute_split<R64, FF>(c, k * split_size, si, sj, sp);
     }
     s_i[threadIdx.x] = si;
     s_j[threadIdx.x] = sj;
@@ -756,17 +805,20 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(
 
 cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const float* w,
                               const uint32_t* idx, const float* elems, const float* prefix,
-                              const BuildCtrl* ctrl, uint32_t* status, uint32_t n,
-                              uint32_t split_size, uint2* table) {
+                              const float* prefix_lo, const BuildCtrl* ctrl, uint32_t* status,
+                              uint32_t n, uint32_t split_size, uint2* table) {
     uint32_t K = n / split_size;
     if (K == 0) K = 1;
     const uint32_t blocks = (K + kSplitPack - 1) / kSplitPack;
-    if (r64)
-        k_split_pack<true><<<blocks, kSplitThreads, 0, st>>>(w, idx, elems, prefix, ctrl, status,
-                                                             n, K, split_size, full_light, table);
+    if (prefix_lo)
+        k_split_pack<true, true><<<blocks, kSplitThreads, 0, st>>>(
+            w, idx, elems, prefix, prefix_lo, ctrl, status, n, K, split_size, full_light, table);
+    else if (r64)
+        k_split_pack<true, false><<<blocks, kSplitThreads, 0, st>>>(
+            w, idx, elems, prefix, nullptr, ctrl, status, n, K, split_size, full_light, table);
     else
-        k_split_pack<false><<<blocks, kSplitThreads, 0, st>>>(w, idx, elems, prefix, ctrl, status,
-                                                              n, K, split_size, full_light, table);
+        k_split_pack<false, false><<<blocks, kSplitThreads, 0, st>>>(
+            w, idx, elems, prefix, nullptr, ctrl, status, n, K, split_size, full_light, table);
     return cudaGetLastError();
 }
 

@@ -36,6 +36,7 @@ struct wrs_buffers {
     uint32_t* idx = nullptr;
     float* prefix = nullptr;
     float* elems = nullptr;
+    float* prefix_lo = nullptr;
     uint2* table = nullptr;
     float* cmf = nullptr;
 };
@@ -65,7 +66,8 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct Layout {
-    size_t ctrl, partials, part_states, scan_states, idx, prefix, elems, table, cmf, total;
+    size_t ctrl, partials, part_states, scan_states, idx, prefix, elems, prefix_lo, table, cmf,
+        total;
 };
 
 Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
@@ -88,6 +90,9 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
         L.idx = take(sizeof(uint32_t) * static_cast<size_t>(max_n));
         L.prefix = take(sizeof(float) * static_cast<size_t>(max_n));
         L.elems = cfg.use_partition_elements ? take(sizeof(float) * static_cast<size_t>(max_n)) : 0;
+        L.prefix_lo = cfg.scan_precision == WRS_SCAN_FLOAT_FLOAT
+                          ? take(sizeof(float) * static_cast<size_t>(max_n))
+                          : 0;
         L.table = take(sizeof(uint2) * static_cast<size_t>(max_n));
     } else {
         L.cmf = take(sizeof(float) * static_cast<size_t>(max_n));
@@ -111,7 +116,7 @@ wrs_status check_config(const wrs_config* c) {
     if (c->method == WRS_METHOD_ALIAS_TABLE && c->split_size == 0)
         return fail(WRS_ERR_INVALID_ARG, "split_size must be >= 1");
     if (c->rng > WRS_RNG_PHILOX4X32_10) return fail(WRS_ERR_INVALID_ARG, "unknown rng");
-    if (c->scan_precision > WRS_SCAN_COMPENSATED)
+    if (c->scan_precision > WRS_SCAN_FLOAT_FLOAT)
         return fail(WRS_ERR_INVALID_ARG, "unknown scan precision");
     if (c->method == WRS_METHOD_ITS && c->coop_size != 0 && c->coop_size < 32)
         return fail(WRS_ERR_INVALID_ARG, "ITS coop_size must be 0 or >= 32");
@@ -206,6 +211,9 @@ wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers**
         b->idx = reinterpret_cast<uint32_t*>(p + L.idx);
         b->prefix = reinterpret_cast<float*>(p + L.prefix);
         b->elems = h->cfg.use_partition_elements ? reinterpret_cast<float*>(p + L.elems) : nullptr;
+        b->prefix_lo = h->cfg.scan_precision == WRS_SCAN_FLOAT_FLOAT
+                           ? reinterpret_cast<float*>(p + L.prefix_lo)
+                           : nullptr;
         b->table = reinterpret_cast<uint2*>(p + L.table);
     } else {
         b->cmf = reinterpret_cast<float*>(p + L.cmf);
@@ -248,39 +256,53 @@ wrs_status wrs_prefix_sum(const wrs_handle* h, void* stream, const float* in, ui
     if (!h || !in || !out) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
     wrs_status s = check_n(b, n);
     if (s != WRS_OK) return s;
-    WRS_CUDA(launch_scan(as_stream(stream), h->cfg.scan_precision == WRS_SCAN_COMPENSATED, in, n,
+    WRS_CUDA(launch_scan(as_stream(stream), h->cfg.scan_precision != WRS_SCAN_FP32, in, n,
                          out, b->ctrl, b->scan_states, b->cap_tiles),
              "prefix sum");
     return WRS_OK;
 }
 
+static bool float_float(const wrs_handle* h) {
+    return h->cfg.scan_precision == WRS_SCAN_FLOAT_FLOAT;
+}
+static bool compensated(const wrs_handle* h) {
+    return h->cfg.scan_precision != WRS_SCAN_FP32;
+}
+
 wrs_status wrs_prefix_partition(const wrs_handle* h, void* stream, const float* weights,
                                 uint32_t n, uint32_t* partition_indices, float* partition_prefix,
-                                float* partition_elements, wrs_buffers* b) {
+                                float* partition_elements, float* partition_prefix_lo,
+                                wrs_buffers* b) {
     if (!h || !weights || !partition_indices || !partition_prefix)
         return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    if ((partition_prefix_lo != nullptr) != float_float(h))
+        return fail(WRS_ERR_INVALID_ARG,
+                    "partition_prefix_lo is required exactly with WRS_SCAN_FLOAT_FLOAT");
     wrs_status s = check_n(b, n);
     if (s != WRS_OK) return s;
     if (!b->part_states) return fail(WRS_ERR_INVALID_ARG, "buffers were not created for the alias method");
-    WRS_CUDA(launch_prefix_partition(as_stream(stream), h->cfg.scan_precision == WRS_SCAN_COMPENSATED,
-                                     weights, n, b->ctrl, b->part_states, b->cap_tiles,
-                                     partition_indices, partition_prefix, partition_elements),
+    WRS_CUDA(launch_prefix_partition(as_stream(stream), compensated(h), weights, n, b->ctrl,
+                                     b->part_states, b->cap_tiles, partition_indices,
+                                     partition_prefix, partition_elements, partition_prefix_lo),
              "prefix partition");
     return WRS_OK;
 }
 
 wrs_status wrs_split_pack(const wrs_handle* h, void* stream, const float* weights,
                           const uint32_t* partition_indices, const float* partition_prefix,
-                          const float* partition_elements, uint32_t n, wrs_alias_entry* table,
-                          wrs_buffers* b) {
+                          const float* partition_elements, const float* partition_prefix_lo,
+                          uint32_t n, wrs_alias_entry* table, wrs_buffers* b) {
     if (!h || !weights || !partition_indices || !partition_prefix || !table)
         return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    if ((partition_prefix_lo != nullptr) != float_float(h))
+        return fail(WRS_ERR_INVALID_ARG,
+                    "partition_prefix_lo is required exactly with WRS_SCAN_FLOAT_FLOAT");
     wrs_status s = check_n(b, n);
     if (s != WRS_OK) return s;
     if (h->cfg.split_size == 0) return fail(WRS_ERR_INVALID_ARG, "split_size must be >= 1");
     WRS_CUDA(launch_split_pack(as_stream(stream), h->cfg.split_residual_f64 != 0,
-                               h->cfg.split_full_light != 0, weights,
-                               partition_indices, partition_elements, partition_prefix, b->ctrl,
+                               h->cfg.split_full_light != 0, weights, partition_indices,
+                               partition_elements, partition_prefix, partition_prefix_lo, b->ctrl,
                                &b->ctrl->status, n, h->cfg.split_size,
                                reinterpret_cast<uint2*>(table)),
              "split pack");
@@ -318,7 +340,7 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
     if (b->cfg.method != h->cfg.method)
         return fail(WRS_ERR_INVALID_ARG, "buffers were created for another method");
     const cudaStream_t st = as_stream(stream);
-    const bool comp = h->cfg.scan_precision == WRS_SCAN_COMPENSATED;
+    const bool comp = compensated(h);
     if (h->cfg.method == WRS_METHOD_ITS) {
         WRS_CUDA(launch_scan(st, comp, weights, n, b->cmf, b->ctrl, b->scan_states, b->cap_tiles),
                  "ITS build");
@@ -326,15 +348,17 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
     }
     if (h->cfg.use_partition_elements && !b->elems)
         return fail(WRS_ERR_INVALID_ARG, "buffers were created without partition elements");
+    if (float_float(h) && !b->prefix_lo)
+        return fail(WRS_ERR_INVALID_ARG, "buffers were created without the float-float prefix");
     float* elems = h->cfg.use_partition_elements ? b->elems : nullptr;
+    float* lo = float_float(h) ? b->prefix_lo : nullptr;
     WRS_CUDA(launch_total_mass(st, weights, n, b->partials, b->ctrl), "total mass");
     WRS_CUDA(launch_prefix_partition(st, comp, weights, n, b->ctrl, b->part_states, b->cap_tiles,
-                                     b->idx, b->prefix, elems),
+                                     b->idx, b->prefix, elems, lo),
              "prefix partition");
     WRS_CUDA(launch_split_pack(st, h->cfg.split_residual_f64 != 0, h->cfg.split_full_light != 0,
-                               weights, b->idx, elems,
-                               b->prefix, b->ctrl, &b->ctrl->status, n, h->cfg.split_size,
-                               b->table),
+                               weights, b->idx, elems, b->prefix, lo, b->ctrl, &b->ctrl->status, n,
+                               h->cfg.split_size, b->table),
              "split pack");
     return WRS_OK;
 }
@@ -381,7 +405,7 @@ wrs_status wrs_test_prefix_sum_stalled(const wrs_handle* h, void* stream, const 
     const uint32_t one = 1;
     WRS_CUDA(cudaMemcpyAsync(&b->ctrl->scan.ticket, &one, sizeof(one), cudaMemcpyHostToDevice, st),
              "ticket preset");
-    WRS_CUDA(launch_scan(st, h->cfg.scan_precision == WRS_SCAN_COMPENSATED, in, n, out, b->ctrl,
+    WRS_CUDA(launch_scan(st, h->cfg.scan_precision != WRS_SCAN_FP32, in, n, out, b->ctrl,
                          b->scan_states, b->cap_tiles, spin_limit),
              "stalled prefix sum");
     return WRS_OK;
@@ -407,6 +431,9 @@ const float* wrs_buffers_cmf(const wrs_buffers* b) { return b ? b->cmf : nullptr
 const uint32_t* wrs_buffers_partition_indices(const wrs_buffers* b) { return b ? b->idx : nullptr; }
 const float* wrs_buffers_partition_prefix(const wrs_buffers* b) { return b ? b->prefix : nullptr; }
 const float* wrs_buffers_partition_elements(const wrs_buffers* b) { return b ? b->elems : nullptr; }
+const float* wrs_buffers_partition_prefix_lo(const wrs_buffers* b) {
+    return b ? b->prefix_lo : nullptr;
+}
 const float* wrs_buffers_mean(const wrs_buffers* b) { return b ? &b->ctrl->mean : nullptr; }
 const double* wrs_buffers_total(const wrs_buffers* b) { return b ? &b->ctrl->total : nullptr; }
 const uint32_t* wrs_buffers_heavy_count(const wrs_buffers* b) {

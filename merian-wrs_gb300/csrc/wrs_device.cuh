@@ -63,6 +63,12 @@ __device__ __forceinline__ float carry_apply(ff c, float x) {
     }
 }
 
+// carry + x as a float-float pair; .hi equals carry_apply<true>(c, x)
+__device__ __forceinline__ ff carry_apply_ff(ff c, float x) {
+    ff s = two_sum(c.hi, x);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, c.lo));
+}
+
 __device__ __forceinline__ ff shfl_xor_ff(ff v, int m) {
     return {__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
 }

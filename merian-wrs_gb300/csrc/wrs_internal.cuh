@@ -19,8 +19,10 @@ constexpr int kWarpItems = kTileItems / kTileWarps;  // 512 contiguous items per
 constexpr int kMassThreads = 256;
 constexpr int kMassMaxBlocks = 152 * 8;
 
-// Split+pack: one thread per split, kSplitThreads-1 subproblems packed per CTA.
-constexpr int kSplitThreads = 256;
+// Split+pack: one thread per split; kSplitThreads - kSplitLook - 1 subproblems packed per CTA,
+// the remaining threads compute look-ahead splits (see k_split_pack).
+constexpr int kSplitThreads = 512;
+constexpr int kSplitLook = 32;
 
 // Ticket / completion / epoch of one lookback kernel kind.  The epoch selects which half
 // of that kernel's double-buffered state array is live in the current launch.
@@ -63,14 +65,15 @@ cudaError_t launch_total_mass(cudaStream_t st, const float* w, uint32_t n, doubl
                               BuildCtrl* ctrl);
 cudaError_t launch_prefix_partition(cudaStream_t st, bool comp, const float* w, uint32_t n,
                                     BuildCtrl* ctrl, PartState* states, uint32_t cap_tiles,
-                                    uint32_t* idx_out, float* prefix_out, float* elems_out);
+                                    uint32_t* idx_out, float* prefix_out, float* elems_out,
+                                    float* prefix_lo_out);
 cudaError_t launch_scan(cudaStream_t st, bool comp, const float* in, uint32_t n, float* out,
                         BuildCtrl* ctrl, ScanState* states, uint32_t cap_tiles,
                         uint32_t spin_limit = kSpinLimit);
 cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const float* w,
                               const uint32_t* idx, const float* elems, const float* prefix,
-                              const BuildCtrl* ctrl, uint32_t* status, uint32_t n,
-                              uint32_t split_size, uint2* table);
+                              const float* prefix_lo, const BuildCtrl* ctrl, uint32_t* status,
+                              uint32_t n, uint32_t split_size, uint2* table);
 cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, const uint2* table,
                                 uint32_t n, uint64_t s, uint64_t seed, uint64_t offset,
                                 uint32_t* out);

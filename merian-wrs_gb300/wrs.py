@@ -28,6 +28,7 @@ RNG_REFERENCE = 0
 RNG_PHILOX4X32_10 = 1
 SCAN_FP32 = 0
 SCAN_COMPENSATED = 1
+SCAN_FLOAT_FLOAT = 2
 
 DEVICE_TIMEOUT = 1
 DEVICE_NONMONOTONE_SPLIT = 2
@@ -78,13 +79,14 @@ def lib() -> C.CDLL:
             "wrs_buffers_partition_indices": (vp, [vp]),
             "wrs_buffers_partition_prefix": (vp, [vp]),
             "wrs_buffers_partition_elements": (vp, [vp]),
+            "wrs_buffers_partition_prefix_lo": (vp, [vp]),
             "wrs_buffers_mean": (vp, [vp]),
             "wrs_buffers_total": (vp, [vp]),
             "wrs_buffers_heavy_count": (vp, [vp]),
             "wrs_total_mass": (i32, [vp, vp, vp, u32, vp]),
             "wrs_prefix_sum": (i32, [vp, vp, vp, u32, vp, vp]),
-            "wrs_prefix_partition": (i32, [vp, vp, vp, u32, vp, vp, vp, vp]),
-            "wrs_split_pack": (i32, [vp, vp, vp, vp, vp, vp, u32, vp, vp]),
+            "wrs_prefix_partition": (i32, [vp, vp, vp, u32, vp, vp, vp, vp, vp]),
+            "wrs_split_pack": (i32, [vp, vp, vp, vp, vp, vp, vp, u32, vp, vp]),
             "wrs_alias_sample": (i32, [vp, vp, vp, u32, u64, u64, u64, vp]),
             "wrs_its_sample": (i32, [vp, vp, vp, u32, u64, u64, u64, vp]),
             "wrs_buffers_set_partition_info": (i32, [vp, vp, f32, u32]),
@@ -209,6 +211,7 @@ class Internals:
             "partition_indices": L.wrs_buffers_partition_indices(self.ptr),
             "partition_prefix": L.wrs_buffers_partition_prefix(self.ptr),
             "partition_elements": L.wrs_buffers_partition_elements(self.ptr),
+            "partition_prefix_lo": L.wrs_buffers_partition_prefix_lo(self.ptr),
             "mean": L.wrs_buffers_mean(self.ptr),
             "total": L.wrs_buffers_total(self.ptr),
             "heavy_count": L.wrs_buffers_heavy_count(self.ptr),
@@ -258,15 +261,17 @@ class WRS:
         check(lib().wrs_prefix_sum(self.handle.ptr, _stream_ptr(stream), _dev_ptr(inp), N,
                                    _dev_ptr(out), internals.ptr))
 
-    def prefix_partition(self, stream, weights, N, idx, prefix, elems, internals) -> None:
+    def prefix_partition(self, stream, weights, N, idx, prefix, elems, internals,
+                         prefix_lo=None) -> None:
         check(lib().wrs_prefix_partition(self.handle.ptr, _stream_ptr(stream), _dev_ptr(weights),
                                          N, _dev_ptr(idx), _dev_ptr(prefix), _dev_ptr(elems),
-                                         internals.ptr))
+                                         _dev_ptr(prefix_lo), internals.ptr))
 
-    def split_pack(self, stream, weights, idx, prefix, elems, N, table, internals) -> None:
+    def split_pack(self, stream, weights, idx, prefix, elems, N, table, internals,
+                   prefix_lo=None) -> None:
         check(lib().wrs_split_pack(self.handle.ptr, _stream_ptr(stream), _dev_ptr(weights),
-                                   _dev_ptr(idx), _dev_ptr(prefix), _dev_ptr(elems), N,
-                                   _dev_ptr(table), internals.ptr))
+                                   _dev_ptr(idx), _dev_ptr(prefix), _dev_ptr(elems),
+                                   _dev_ptr(prefix_lo), N, _dev_ptr(table), internals.ptr))
 
     def alias_sample(self, stream, table, N, S, seed, offset, out) -> None:
         check(lib().wrs_alias_sample(self.handle.ptr, _stream_ptr(stream), _dev_ptr(table), N, S,

@@ -19,8 +19,9 @@ ENTRY_DTYPE = np.dtype([("p", "<f4"), ("a", "<u4")])
 
 RNG_REFERENCE = 0
 RNG_PHILOX4X32_10 = 1
-SPLIT_F64 = 1         # split target / sigma / spill in FP64
-SPLIT_FULL_LIGHT = 2  # light count capped at lightCount (not the shader's lightCount - 1)
+SPLIT_F64 = 1          # split-point residual (spill) in FP64
+SPLIT_FULL_LIGHT = 2   # light count capped at lightCount (not the shader's lightCount - 1)
+SPLIT_FLOAT_FLOAT = 4  # psa_build: float-float partition prefix for the split search
 
 
 def _ptr(a: np.ndarray | None):
@@ -66,8 +67,8 @@ class Oracle:
                 "wrso_prefix_f64": (None, [vp, u64, vp]),
                 "wrso_prefix_kahan": (None, [vp, u64, vp]),
                 "wrso_prefix_seq_f32": (None, [vp, u64, vp]),
-                "wrso_split": (None, [vp, u32, u32, f32, u32, i32, vp, vp, vp]),
-                "wrso_split_pack": (None, [vp, vp, vp, vp, u32, f32, u32, u32, i32, vp, vp]),
+                "wrso_split": (None, [vp, vp, u32, u32, f32, u32, i32, vp, vp, vp]),
+                "wrso_split_pack": (None, [vp, vp, vp, vp, vp, u32, f32, u32, u32, i32, vp, vp]),
                 "wrso_psa_build": (None, [vp, u32, u32, i32, i32, vp, vp, vp]),
                 "wrso_alias_sample": (None, [vp, u32, u64, u64, u64, u32, u32, i32, vp]),
                 "wrso_its_sample": (None, [vp, u32, u64, u64, u64, u32, u32, i32, i32, vp]),
@@ -144,20 +145,23 @@ class Oracle:
         self.lib.wrso_prefix_seq_f32(_ptr(w), w.size, _ptr(out))
         return out
 
-    def split(self, prefix: np.ndarray, heavy_count: int, mean: float, n: int, flags: int = 0):
+    def split(self, prefix: np.ndarray, heavy_count: int, mean: float, n: int, flags: int = 0,
+              prefix_lo: np.ndarray | None = None):
         prefix = np.ascontiguousarray(prefix, np.float32)
+        lo = None if prefix_lo is None else np.ascontiguousarray(prefix_lo, np.float32)
         i = np.zeros(1, np.uint32)
         j = np.zeros(1, np.uint32)
         s = np.zeros(1, np.float32)
-        self.lib.wrso_split(_ptr(prefix), prefix.size, heavy_count, np.float32(mean), n, flags,
-                            _ptr(i), _ptr(j), _ptr(s))
+        self.lib.wrso_split(_ptr(prefix), _ptr(lo), prefix.size, heavy_count, np.float32(mean), n,
+                            flags, _ptr(i), _ptr(j), _ptr(s))
         return int(i[0]), int(j[0]), np.float32(s[0])
 
     def split_pack(self, w, idx, prefix, heavy_count, mean, split_size, flags=0, elems=None,
-                   return_splits=False):
+                   return_splits=False, prefix_lo=None):
         w = np.ascontiguousarray(w, np.float32)
         idx = np.ascontiguousarray(idx, np.uint32)
         prefix = np.ascontiguousarray(prefix, np.float32)
+        lo = None if prefix_lo is None else np.ascontiguousarray(prefix_lo, np.float32)
         N = w.size
         table = np.zeros(N, ENTRY_DTYPE)
         K = max(N // split_size, 1)
@@ -165,8 +169,8 @@ class Oracle:
         self.lib.wrso_split_pack(_ptr(w), _ptr(idx),
                                  _ptr(np.ascontiguousarray(elems, np.float32))
                                  if elems is not None else None,
-                                 _ptr(prefix), heavy_count, np.float32(mean), N, split_size,
-                                 flags, _ptr(table), _ptr(splits))
+                                 _ptr(prefix), _ptr(lo), heavy_count, np.float32(mean), N,
+                                 split_size, flags, _ptr(table), _ptr(splits))
         if return_splits:
             sp = splits.reshape(K + 1, 3)
             return table, (sp[:, 0].copy(), sp[:, 1].copy(), sp[:, 2].view(np.float32).copy())

@@ -226,13 +226,22 @@ void wrso_prefix_seq_f32(const float* w, uint64_t N, float* out) {
  * shader's lightCount - 1 (shader.comp:90,104).  With the shader's cap a split near the
  * end of the table can have i + j < n, after which the last heavy bucket aliases a light
  * item that then gains mass; the full range keeps i + j = n.
+ * prefix_lo != NULL (float-float prefix, prefix[] holding the high words): each comparison
+ * sigma <= target is decided on sigma = (hi + lo of the heavy prefix) + (hi + lo of the
+ * light prefix) and target = mean * n in FP64, after an FP32 pre-test on the high words
+ * that settles probes differing by more than m = (s + t) * 2^-21; the spill is computed from
+ * the float-float values in FP64.  This is the kernel's decision procedure step for step.
  * Guard beyond the shader: if every probe exceeds the target (b would wrap to
  * 0xFFFFFFFF in the shader), j = 0 is used. */
-void wrso_split(const float* prefix, uint32_t N, uint32_t hc, float mean, uint32_t n,
-                int flags, uint32_t* i_out, uint32_t* j_out, float* spill_out) {
+static inline double wrso_prefix64(const float* prefix_lo, float hi, uint32_t pos) {
+    return prefix_lo ? (double)hi + (double)prefix_lo[pos] : (double)hi;
+}
+
+void wrso_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_t hc, float mean,
+                uint32_t n, int flags, uint32_t* i_out, uint32_t* j_out, float* spill_out) {
     const uint32_t lc = N - hc;
     const uint32_t lcap = (flags & WRSO_SPLIT_FULL_LIGHT) ? lc : lc - 1;
-    const int residual_f64 = (flags & WRSO_SPLIT_F64) != 0;
+    const int residual_f64 = (flags & WRSO_SPLIT_F64) != 0 || prefix_lo != NULL;
     int64_t a = 0, b = (int64_t)hc - 1;
     const float target = mean * (float)n;
     const double target64 = (double)mean * (double)n;
@@ -242,7 +251,24 @@ void wrso_split(const float* prefix, uint32_t N, uint32_t hc, float mean, uint32
         float heavy = j == 0 ? 0.0f : prefix[j - 1];
         float light = i == 0 ? 0.0f : prefix[N - i];
         volatile float sigma = light + heavy;
-        if (sigma <= target)
+        int le;
+        if (prefix_lo) {
+            volatile float d = sigma - target;
+            volatile float st = sigma + target;
+            volatile float m = st * 4.76837158203125e-07f;
+            if (d > m) {
+                le = 0;
+            } else if (d < -m) {
+                le = 1;
+            } else {
+                double h64 = j == 0 ? 0.0 : wrso_prefix64(prefix_lo, heavy, j - 1);
+                double l64 = i == 0 ? 0.0 : wrso_prefix64(prefix_lo, light, N - i);
+                le = (h64 + l64) <= target64;
+            }
+        } else {
+            le = sigma <= target;
+        }
+        if (le)
             a = (int64_t)j + 1;
         else
             b = (int64_t)j - 1;
@@ -253,7 +279,9 @@ void wrso_split(const float* prefix, uint32_t N, uint32_t hc, float mean, uint32
     float heavy2 = prefix[j];
     float spill;
     if (residual_f64) {
-        spill = (float)(((double)heavy2 + (double)light) - target64);
+        double h64 = wrso_prefix64(prefix_lo, heavy2, j);
+        double l64 = i == 0 ? 0.0 : wrso_prefix64(prefix_lo, light, N - i);
+        spill = (float)((h64 + l64) - target64);
     } else {
         volatile float sigma2 = heavy2 + light;
         spill = sigma2 - target;
@@ -335,8 +363,8 @@ static void wrso_pack(const wrso_pack_ctx* c, uint32_t i0, uint32_t i1, uint32_t
  * Guards beyond the shader (which is undefined there): heavyCount == 0 or N gives
  * table[i] = (1, i); K == 0 (N < splitSize) is treated as K = 1. */
 void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, const float* prefix,
-                     uint32_t hc, float mean, uint32_t N, uint32_t split_size, int flags,
-                     wrso_entry* table, uint32_t* splits) {
+                     const float* prefix_lo, uint32_t hc, float mean, uint32_t N,
+                     uint32_t split_size, int flags, wrso_entry* table, uint32_t* splits) {
     if (N == 0) return;
     if (hc == 0 || hc == N) {
         for (uint32_t i = 0; i < N; ++i) {
@@ -363,7 +391,7 @@ void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, co
             nj = hc;
             nspill = 0.0f;
         } else {
-            wrso_split(prefix, N, hc, mean, k * split_size, flags, &ni, &nj, &nspill);
+            wrso_split(prefix, prefix_lo, N, hc, mean, k * split_size, flags, &ni, &nj, &nspill);
         }
         if (splits) {
             splits[3 * k + 0] = ni;
@@ -394,6 +422,7 @@ typedef struct {
     uint32_t* idx;
     float* elems;
     float* prefix;
+    float* prefix_lo; /* the FP64 prefix kept as a float-float pair (prefix = high word) */
     uint32_t hc;
     uint32_t K;
     wrso_entry* table;
@@ -450,12 +479,14 @@ static void psa_scatter_task(void* p, int t, int nt) {
             c->idx[h] = (uint32_t)i;
             c->elems[h] = x;
             c->prefix[h] = (float)hs;
+            c->prefix_lo[h] = (float)(hs - (double)c->prefix[h]);
             ++h;
         } else {
             ls += (double)x;
             c->idx[N - 1 - l] = (uint32_t)i;
             c->elems[N - 1 - l] = x;
             c->prefix[N - 1 - l] = (float)ls;
+            c->prefix_lo[N - 1 - l] = (float)(ls - (double)c->prefix[N - 1 - l]);
             ++l;
         }
     }
@@ -474,8 +505,8 @@ static void psa_splitpack_task(void* p, int t, int nt) {
         pj = 0;
         pspill = 0.0f;
     } else {
-        wrso_split(c->prefix, c->N, c->hc, c->mean, (uint32_t)lo * c->split_size, c->flags, &pi, &pj,
-                   &pspill);
+        wrso_split(c->prefix, c->prefix_lo, c->N, c->hc, c->mean, (uint32_t)lo * c->split_size,
+                   c->flags, &pi, &pj, &pspill);
     }
     for (uint64_t k = lo + 1; k <= hi; ++k) {
         uint32_t ni, nj;
@@ -485,8 +516,8 @@ static void psa_splitpack_task(void* p, int t, int nt) {
             nj = c->hc;
             nspill = 0.0f;
         } else {
-            wrso_split(c->prefix, c->N, c->hc, c->mean, (uint32_t)k * c->split_size, c->flags, &ni, &nj,
-                       &nspill);
+            wrso_split(c->prefix, c->prefix_lo, c->N, c->hc, c->mean,
+                       (uint32_t)k * c->split_size, c->flags, &ni, &nj, &nspill);
         }
         uint32_t i1 = ni > pi ? ni : pi;
         uint32_t j1 = nj > pj ? nj : pj;
@@ -518,11 +549,16 @@ void wrso_psa_build(const float* w, uint32_t N, uint32_t split_size, int flags, 
     c.idx = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)N);
     c.elems = (float*)malloc(sizeof(float) * (size_t)N);
     c.prefix = (float*)malloc(sizeof(float) * (size_t)N);
+    c.prefix_lo = (float*)malloc(sizeof(float) * (size_t)N);
     wrso_parallel(psa_count_task, &c, nthreads);
     uint32_t hc = 0;
     for (int t = 0; t < nthreads; ++t) hc += c.part_heavy[t];
     c.hc = hc;
     wrso_parallel(psa_scatter_task, &c, nthreads);
+    if (!(flags & WRSO_SPLIT_FLOAT_FLOAT)) {
+        free(c.prefix_lo);
+        c.prefix_lo = NULL;
+    }
     if (hc == 0 || hc == N) {
         for (uint32_t i = 0; i < N; ++i) {
             table[i].p = 1.0f;
@@ -538,6 +574,7 @@ void wrso_psa_build(const float* w, uint32_t N, uint32_t split_size, int flags, 
     free(c.idx);
     free(c.elems);
     free(c.prefix);
+    free(c.prefix_lo);
     free(c.part_sum);
     free(c.part_heavy);
     free(c.part_hsum);

@@ -44,14 +44,18 @@ void wrso_prefix_kahan(const float* w, uint64_t N, float* out);
 void wrso_prefix_seq_f32(const float* w, uint64_t N, float* out);
 
 /* split flags */
-#define WRSO_SPLIT_F64 1        /* target / sigma / spill in FP64 */
-#define WRSO_SPLIT_FULL_LIGHT 2 /* light count capped at lightCount, not lightCount - 1 */
+#define WRSO_SPLIT_F64 1          /* split-point residual (spill) in FP64 */
+#define WRSO_SPLIT_FULL_LIGHT 2   /* light count capped at lightCount, not lightCount - 1 */
+#define WRSO_SPLIT_FLOAT_FLOAT 4  /* wrso_psa_build: float-float prefix for the split search */
 
-void wrso_split(const float* prefix, uint32_t N, uint32_t heavy_count, float mean, uint32_t n,
-                int flags, uint32_t* i_out, uint32_t* j_out, float* spill_out);
+/* prefix_lo: low words of a float-float prefix (prefix = high words), or NULL */
+void wrso_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_t heavy_count,
+                float mean, uint32_t n, int flags, uint32_t* i_out, uint32_t* j_out,
+                float* spill_out);
 void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, const float* prefix,
-                     uint32_t heavy_count, float mean, uint32_t N, uint32_t split_size,
-                     int flags, wrso_entry* table, uint32_t* splits /* 3*(K+1) or NULL */);
+                     const float* prefix_lo, uint32_t heavy_count, float mean, uint32_t N,
+                     uint32_t split_size, int flags, wrso_entry* table,
+                     uint32_t* splits /* 3*(K+1) or NULL */);
 /* Full PSA build on the CPU (mean -> partition -> prefix -> split+pack) with nthreads
  * worker threads.  Used as the timed CPU port of the reference path. */
 void wrso_psa_build(const float* w, uint32_t N, uint32_t split_size, int flags, int nthreads,

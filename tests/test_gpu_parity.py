@@ -43,6 +43,8 @@ class Built:
             self.prefix = d2h(v["partition_prefix"], self.N, np.float32)
             self.elems = (d2h(v["partition_elements"], self.N, np.float32)
                           if cfg.use_partition_elements else None)
+            self.prefix_lo = (d2h(v["partition_prefix_lo"], self.N, np.float32)
+                              if cfg.scan_precision == W.SCAN_FLOAT_FLOAT else None)
             self.table = d2h(v["alias_table"], self.N, ENTRY_DTYPE)
         else:
             self.cmf = d2h(v["cmf"], self.N, np.float32)
@@ -124,6 +126,31 @@ def test_split_pack_bit_exact(pkg, cuda, oracle, split_size, flags, gen):
     ref = oracle.split_pack(w, b.idx, b.prefix, b.hc, b.mean, split_size, flags=flags,
                             elems=b.elems)
     assert same_table(b.table, ref)
+
+
+@pytest.mark.parametrize("N", [(1 << 20) + 5, (1 << 22) + 17])
+@pytest.mark.parametrize("gen", list(GENS))
+@pytest.mark.parametrize("split_size", [2, 32])
+def test_float_float_prefix_mode(pkg, cuda, oracle, N, gen, split_size):
+    """WRS_SCAN_FLOAT_FLOAT: high + low words of the partition prefix carry only the
+    tile-local FP32 rounding (<= 4096 * max w * 2^-20 absolute), the table equals the oracle's
+    float-float split+pack given the GPU's arrays, no overlap escapes the ownership window,
+    and the table encodes w/mean to 1e-3 (FP32 prefixes alone give ~1e-2 at 2^20 and whole
+    mean-units at 2^26)."""
+    W = pkg.wrs
+    w = GENS[gen](N, 5 * split_size)
+    cfg = pkg.AliasTableConfig(split_size=split_size, scan_precision=W.SCAN_FLOAT_FLOAT,
+                               split_full_light=True)
+    b = Built(pkg, w, cfg)
+    assert b.status == 0
+    ref64 = oracle.partition_prefix_f64(w, b.mean)
+    got64 = b.prefix.astype(np.float64) + b.prefix_lo.astype(np.float64)
+    assert np.abs(got64 - ref64).max() <= 4096 * float(w.max()) * 2.0 ** -20
+    ref = oracle.split_pack(w, b.idx, b.prefix, b.hc, b.mean, split_size, flags=2,
+                            elems=b.elems, prefix_lo=b.prefix_lo)
+    assert same_table(b.table, ref)
+    implied = oracle.alias_to_weights(b.table)
+    assert np.abs(implied - w / w.astype(np.float64).mean()).max() < 1e-3
 
 
 @pytest.mark.parametrize("gen", list(GENS))
