@@ -190,9 +190,12 @@ wrs_status wrs_its_sample(const wrs_handle* h, void* stream, const float* cmf, u
 wrs_status wrs_test_prefix_sum_stalled(const wrs_handle* h, void* stream, const float* in,
                                        uint32_t n, float* out, wrs_buffers* b,
                                        uint32_t spin_limit);
-/* Host helper: upload mean / heavy count into b (for driving wrs_split_pack directly). */
+/* Host helper: upload the FP32 mean, the FP64 mean (total / N, used by the float-float
+ * mode's split targets) and the heavy count into b, for driving wrs_split_pack directly. */
 wrs_status wrs_buffers_set_partition_info(wrs_buffers* b, void* stream, float mean,
-                                          uint32_t heavy_count);
+                                          double mean64, uint32_t heavy_count);
+/* device view of the FP64 mean (1 double) */
+const double* wrs_buffers_mean64(const wrs_buffers* b);
 
 #ifdef __cplusplus
 }

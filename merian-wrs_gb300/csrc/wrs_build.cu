@@ -90,7 +90,8 @@ __global__ __launch_bounds__(kMassThreads) void k_total_mass(const float* __rest
         double total = 0.0;
         for (int k = 0; k < kMassThreads / 32; ++k) total = __dadd_rn(total, s_red[k]);
         ctrl->total = total;
-        ctrl->mean = n ? __double2float_rn(__ddiv_rn(total, static_cast<double>(n))) : 0.0f;
+        ctrl->mean64 = n ? __ddiv_rn(total, static_cast<double>(n)) : 0.0;
+        ctrl->mean = __double2float_rn(ctrl->mean64);
         ctrl->mass_done = 0u;
     }
 }
@@ -605,6 +606,7 @@ struct PackIn {
     uint32_t n, hc, lc;
     uint32_t lcap;  // largest light count a split may take: lc - 1 (shader) or lc
     float mean;
+    double mean64;  // total / N in FP64 (float-float mode)
 };
 
 // prefix value at position pos as a double: hi only, or hi + lo of the float-float prefix
@@ -614,6 +616,15 @@ __device__ __forceinline__ double prefix64(const PackIn& c, float hi, uint32_t p
         return __dadd_rn(static_cast<double>(hi), static_cast<double>(__ldg(c.prefix_lo + pos)));
     else
         return static_cast<double>(hi);
+}
+
+// The float-float mode's exact decision for a probe near the crossing.  Kept out of line so
+// that the compiler cannot if-convert it into every probe (it runs on the slow FP64 pipe).
+__device__ __noinline__ bool ff_le(const PackIn& c, uint32_t j, uint32_t i, float heavy,
+                                   float light, double target64) {
+    const double h64 = j == 0 ? 0.0 : prefix64<true>(c, heavy, j - 1);
+    const double l64 = i == 0 ? 0.0 : prefix64<true>(c, light, c.n - i);
+    return __dadd_rn(h64, l64) <= target64;
 }
 
 __device__ __forceinline__ float elem_at(const PackIn& c, uint32_t pos) {
@@ -630,17 +641,19 @@ __device__ __forceinline__ float elem_at(const PackIn& c, uint32_t pos) {
 // table).  If every probe exceeds the target (the shader's b would wrap), j = 0.
 //
 // FF (float-float prefix): the comparison sigma <= target is decided on the exact values --
-// sigma = (hi + lo of the heavy prefix) + (hi + lo of the light prefix) and target = mean * n,
-// both evaluated in FP64 -- instead of on the FP32 high words.  An FP32 pre-test settles every
-// probe whose high words differ by more than a few ulps (bound m = (s + t) * 2^-21), so FP64
-// runs only near the crossing; the spill is then computed from the float-float prefix in
-// FP64 as well.  Split points become monotone in k up to exact ties.
+// sigma = (hi + lo of the heavy prefix) + (hi + lo of the light prefix) and target =
+// (total / N) * n, evaluated in FP64 -- instead of on FP32 high words and the FP32 mean.  An
+// FP32 pre-test settles every probe whose high words differ by more than a few ulps (bound
+// m = (s + t) * 2^-21), so FP64 runs only near the crossing; the spill is then computed from
+// the float-float prefix in FP64 as well.  Measuring targets against the FP64 mean keeps the
+// FP32 rounding of the mean from piling up in the last heavy bucket.
 template <bool R64, bool FF>
 __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, uint32_t& io,
                                               uint32_t& jo, float& spill) {
     int64_t a = 0, b = static_cast<int64_t>(c.hc) - 1;
     const float target = __fmul_rn(c.mean, __uint2float_rn(nsplit));
-    const double target64 = __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit));
+    const double target64 = FF ? __dmul_rn(c.mean64, static_cast<double>(nsplit))
+                               : __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit));
     const uint32_t lcm1 = c.lcap;
     while (a <= b) {
         const uint32_t j = static_cast<uint32_t>((a + b) >> 1);
@@ -652,15 +665,12 @@ __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, 
         if constexpr (FF) {
             const float d = __fsub_rn(s32, target);
             const float m = __fmul_rn(__fadd_rn(s32, target), 4.76837158203125e-07f);
-            if (d > m) {
+            if (d > m)
                 le = false;
-            } else if (d < -m) {
+            else if (d < -m)
                 le = true;
-            } else {
-                const double h64 = j == 0 ? 0.0 : prefix64<true>(c, heavy, j - 1);
-                const double l64 = i == 0 ? 0.0 : prefix64<true>(c, light, c.n - i);
-                le = __dadd_rn(h64, l64) <= target64;
-            }
+            else
+                le = ff_le(c, j, i, heavy, light, target64);
         } else {
             le = s32 <= target;
         }
@@ -774,8 +784,8 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(
             table[e] = make_uint2(__float_as_uint(1.0f), e);
         return;
     }
-    PackIn c{w,  idx,    elems,  prefix, prefix_lo, n, hc,
-             n - hc, full_light ? n - hc : n - hc - 1u, ctrl->mean};
+    PackIn c{w,      idx,    elems,  prefix, prefix_lo, n, hc,
+             n - hc, full_light ? n - hc : n - hc - 1u, ctrl->mean, ctrl->mean64};
     const uint32_t k = blockIdx.x * kSplitPack + threadIdx.x;
     uint32_t si = c.lc, sj = hc;  // past split K: the final split
     float sp = 0.f;

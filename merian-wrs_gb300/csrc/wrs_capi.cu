@@ -412,17 +412,22 @@ wrs_status wrs_test_prefix_sum_stalled(const wrs_handle* h, void* stream, const 
 }
 
 wrs_status wrs_buffers_set_partition_info(wrs_buffers* b, void* stream, float mean,
-                                          uint32_t heavy_count) {
+                                          double mean64, uint32_t heavy_count) {
     if (!b) return fail(WRS_ERR_INVALID_ARG, "buffers is NULL");
     const cudaStream_t st = as_stream(stream);
     WRS_CUDA(cudaMemcpyAsync(&b->ctrl->mean, &mean, sizeof(float), cudaMemcpyHostToDevice, st),
              "mean upload");
+    WRS_CUDA(cudaMemcpyAsync(&b->ctrl->mean64, &mean64, sizeof(double), cudaMemcpyHostToDevice,
+                             st),
+             "mean64 upload");
     WRS_CUDA(cudaMemcpyAsync(&b->ctrl->heavy_count, &heavy_count, sizeof(uint32_t),
                              cudaMemcpyHostToDevice, st),
              "heavy count upload");
     WRS_CUDA(cudaStreamSynchronize(st), "stream synchronize");
     return WRS_OK;
 }
+
+const double* wrs_buffers_mean64(const wrs_buffers* b) { return b ? &b->ctrl->mean64 : nullptr; }
 
 const wrs_alias_entry* wrs_buffers_alias_table(const wrs_buffers* b) {
     return b ? reinterpret_cast<const wrs_alias_entry*>(b->table) : nullptr;

@@ -44,7 +44,7 @@ struct alignas(64) BuildCtrl {
     double total;        // FP64 total mass
     LbCtrl part;         // prefix-partition launches
     LbCtrl scan;         // scan launches
-    uint32_t pad[2];
+    double mean64;       // total / N in FP64 (split targets of the float-float mode)
 };
 static_assert(sizeof(BuildCtrl) == 64, "BuildCtrl layout");
 

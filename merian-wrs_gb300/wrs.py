@@ -89,7 +89,8 @@ def lib() -> C.CDLL:
             "wrs_split_pack": (i32, [vp, vp, vp, vp, vp, vp, vp, u32, vp, vp]),
             "wrs_alias_sample": (i32, [vp, vp, vp, u32, u64, u64, u64, vp]),
             "wrs_its_sample": (i32, [vp, vp, vp, u32, u64, u64, u64, vp]),
-            "wrs_buffers_set_partition_info": (i32, [vp, vp, f32, u32]),
+            "wrs_buffers_set_partition_info": (i32, [vp, vp, f32, C.c_double, u32]),
+            "wrs_buffers_mean64": (vp, [vp]),
             "wrs_test_prefix_sum_stalled": (i32, [vp, vp, vp, u32, vp, vp, u32]),
         }
         for name, (res, args) in sig.items():
@@ -213,6 +214,7 @@ class Internals:
             "partition_elements": L.wrs_buffers_partition_elements(self.ptr),
             "partition_prefix_lo": L.wrs_buffers_partition_prefix_lo(self.ptr),
             "mean": L.wrs_buffers_mean(self.ptr),
+            "mean64": L.wrs_buffers_mean64(self.ptr),
             "total": L.wrs_buffers_total(self.ptr),
             "heavy_count": L.wrs_buffers_heavy_count(self.ptr),
         }

@@ -67,8 +67,9 @@ class Oracle:
                 "wrso_prefix_f64": (None, [vp, u64, vp]),
                 "wrso_prefix_kahan": (None, [vp, u64, vp]),
                 "wrso_prefix_seq_f32": (None, [vp, u64, vp]),
-                "wrso_split": (None, [vp, vp, u32, u32, f32, u32, i32, vp, vp, vp]),
-                "wrso_split_pack": (None, [vp, vp, vp, vp, vp, u32, f32, u32, u32, i32, vp, vp]),
+                "wrso_split": (None, [vp, vp, u32, u32, f32, f64, u32, i32, vp, vp, vp]),
+                "wrso_split_pack": (None, [vp, vp, vp, vp, vp, u32, f32, f64, u32, u32, i32, vp,
+                                           vp]),
                 "wrso_psa_build": (None, [vp, u32, u32, i32, i32, vp, vp, vp]),
                 "wrso_alias_sample": (None, [vp, u32, u64, u64, u64, u32, u32, i32, vp]),
                 "wrso_its_sample": (None, [vp, u32, u64, u64, u64, u32, u32, i32, i32, vp]),
@@ -146,18 +147,19 @@ class Oracle:
         return out
 
     def split(self, prefix: np.ndarray, heavy_count: int, mean: float, n: int, flags: int = 0,
-              prefix_lo: np.ndarray | None = None):
+              prefix_lo: np.ndarray | None = None, mean64: float = 0.0):
         prefix = np.ascontiguousarray(prefix, np.float32)
         lo = None if prefix_lo is None else np.ascontiguousarray(prefix_lo, np.float32)
         i = np.zeros(1, np.uint32)
         j = np.zeros(1, np.uint32)
         s = np.zeros(1, np.float32)
-        self.lib.wrso_split(_ptr(prefix), _ptr(lo), prefix.size, heavy_count, np.float32(mean), n,
-                            flags, _ptr(i), _ptr(j), _ptr(s))
+        self.lib.wrso_split(_ptr(prefix), _ptr(lo), prefix.size, heavy_count, np.float32(mean),
+                            float(mean64), n, flags, _ptr(i), _ptr(j), _ptr(s))
         return int(i[0]), int(j[0]), np.float32(s[0])
 
     def split_pack(self, w, idx, prefix, heavy_count, mean, split_size, flags=0, elems=None,
-                   return_splits=False, prefix_lo=None):
+                   return_splits=False, prefix_lo=None, mean64=0.0):
+        """prefix_lo / mean64: the float-float mode's low words and FP64 mean."""
         w = np.ascontiguousarray(w, np.float32)
         idx = np.ascontiguousarray(idx, np.uint32)
         prefix = np.ascontiguousarray(prefix, np.float32)
@@ -169,8 +171,8 @@ class Oracle:
         self.lib.wrso_split_pack(_ptr(w), _ptr(idx),
                                  _ptr(np.ascontiguousarray(elems, np.float32))
                                  if elems is not None else None,
-                                 _ptr(prefix), _ptr(lo), heavy_count, np.float32(mean), N,
-                                 split_size, flags, _ptr(table), _ptr(splits))
+                                 _ptr(prefix), _ptr(lo), heavy_count, np.float32(mean),
+                                 float(mean64), N, split_size, flags, _ptr(table), _ptr(splits))
         if return_splits:
             sp = splits.reshape(K + 1, 3)
             return table, (sp[:, 0].copy(), sp[:, 1].copy(), sp[:, 2].view(np.float32).copy())

@@ -238,13 +238,15 @@ static inline double wrso_prefix64(const float* prefix_lo, float hi, uint32_t po
 }
 
 void wrso_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_t hc, float mean,
-                uint32_t n, int flags, uint32_t* i_out, uint32_t* j_out, float* spill_out) {
+                double mean64, uint32_t n, int flags, uint32_t* i_out, uint32_t* j_out,
+                float* spill_out) {
     const uint32_t lc = N - hc;
     const uint32_t lcap = (flags & WRSO_SPLIT_FULL_LIGHT) ? lc : lc - 1;
     const int residual_f64 = (flags & WRSO_SPLIT_F64) != 0 || prefix_lo != NULL;
     int64_t a = 0, b = (int64_t)hc - 1;
     const float target = mean * (float)n;
-    const double target64 = (double)mean * (double)n;
+    /* float-float mode: targets against the FP64 mean total / N */
+    const double target64 = prefix_lo ? mean64 * (double)n : (double)mean * (double)n;
     while (a <= b) {
         uint32_t j = (uint32_t)((a + b) / 2);
         uint32_t i = (j > n) ? lcap : ((n - j) < lcap ? (n - j) : lcap);
@@ -363,7 +365,7 @@ static void wrso_pack(const wrso_pack_ctx* c, uint32_t i0, uint32_t i1, uint32_t
  * Guards beyond the shader (which is undefined there): heavyCount == 0 or N gives
  * table[i] = (1, i); K == 0 (N < splitSize) is treated as K = 1. */
 void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, const float* prefix,
-                     const float* prefix_lo, uint32_t hc, float mean, uint32_t N,
+                     const float* prefix_lo, uint32_t hc, float mean, double mean64, uint32_t N,
                      uint32_t split_size, int flags, wrso_entry* table, uint32_t* splits) {
     if (N == 0) return;
     if (hc == 0 || hc == N) {
@@ -391,7 +393,8 @@ void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, co
             nj = hc;
             nspill = 0.0f;
         } else {
-            wrso_split(prefix, prefix_lo, N, hc, mean, k * split_size, flags, &ni, &nj, &nspill);
+            wrso_split(prefix, prefix_lo, N, hc, mean, mean64, k * split_size, flags, &ni, &nj,
+                       &nspill);
         }
         if (splits) {
             splits[3 * k + 0] = ni;
@@ -415,6 +418,7 @@ typedef struct {
     uint32_t split_size;
     int flags;
     float mean;
+    double mean64;
     double* part_sum;
     uint32_t* part_heavy;
     double* part_hsum;
@@ -505,8 +509,8 @@ static void psa_splitpack_task(void* p, int t, int nt) {
         pj = 0;
         pspill = 0.0f;
     } else {
-        wrso_split(c->prefix, c->prefix_lo, c->N, c->hc, c->mean, (uint32_t)lo * c->split_size,
-                   c->flags, &pi, &pj, &pspill);
+        wrso_split(c->prefix, c->prefix_lo, c->N, c->hc, c->mean, c->mean64,
+                   (uint32_t)lo * c->split_size, c->flags, &pi, &pj, &pspill);
     }
     for (uint64_t k = lo + 1; k <= hi; ++k) {
         uint32_t ni, nj;
@@ -516,7 +520,7 @@ static void psa_splitpack_task(void* p, int t, int nt) {
             nj = c->hc;
             nspill = 0.0f;
         } else {
-            wrso_split(c->prefix, c->prefix_lo, c->N, c->hc, c->mean,
+            wrso_split(c->prefix, c->prefix_lo, c->N, c->hc, c->mean, c->mean64,
                        (uint32_t)k * c->split_size, c->flags, &ni, &nj, &nspill);
         }
         uint32_t i1 = ni > pi ? ni : pi;
@@ -545,7 +549,8 @@ void wrso_psa_build(const float* w, uint32_t N, uint32_t split_size, int flags, 
     wrso_parallel(psa_sum_task, &c, nthreads);
     double total = 0.0;
     for (int t = 0; t < nthreads; ++t) total += c.part_sum[t];
-    c.mean = N ? (float)(total / (double)N) : 0.0f;
+    c.mean64 = N ? total / (double)N : 0.0;
+    c.mean = (float)c.mean64;
     c.idx = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)N);
     c.elems = (float*)malloc(sizeof(float) * (size_t)N);
     c.prefix = (float*)malloc(sizeof(float) * (size_t)N);

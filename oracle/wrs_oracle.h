@@ -48,13 +48,14 @@ void wrso_prefix_seq_f32(const float* w, uint64_t N, float* out);
 #define WRSO_SPLIT_FULL_LIGHT 2   /* light count capped at lightCount, not lightCount - 1 */
 #define WRSO_SPLIT_FLOAT_FLOAT 4  /* wrso_psa_build: float-float prefix for the split search */
 
-/* prefix_lo: low words of a float-float prefix (prefix = high words), or NULL */
+/* prefix_lo: low words of a float-float prefix (prefix = high words), or NULL.
+ * mean64: total / N in FP64, the float-float mode's split targets (unused otherwise). */
 void wrso_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_t heavy_count,
-                float mean, uint32_t n, int flags, uint32_t* i_out, uint32_t* j_out,
-                float* spill_out);
+                float mean, double mean64, uint32_t n, int flags, uint32_t* i_out,
+                uint32_t* j_out, float* spill_out);
 void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, const float* prefix,
-                     const float* prefix_lo, uint32_t heavy_count, float mean, uint32_t N,
-                     uint32_t split_size, int flags, wrso_entry* table,
+                     const float* prefix_lo, uint32_t heavy_count, float mean, double mean64,
+                     uint32_t N, uint32_t split_size, int flags, wrso_entry* table,
                      uint32_t* splits /* 3*(K+1) or NULL */);
 /* Full PSA build on the CPU (mean -> partition -> prefix -> split+pack) with nthreads
  * worker threads.  Used as the timed CPU port of the reference path. */

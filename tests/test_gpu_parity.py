@@ -38,6 +38,7 @@ class Built:
         if cfg.method == W.METHOD_ALIAS_TABLE:
             self.mean = float(d2h(v["mean"], 1, np.float32)[0])
             self.total = float(d2h(v["total"], 1, np.float64)[0])
+            self.mean64 = float(d2h(v["mean64"], 1, np.float64)[0])
             self.hc = int(d2h(v["heavy_count"], 1, np.uint32)[0])
             self.idx = d2h(v["partition_indices"], self.N, np.uint32)
             self.prefix = d2h(v["partition_prefix"], self.N, np.float32)
@@ -146,11 +147,13 @@ def test_float_float_prefix_mode(pkg, cuda, oracle, N, gen, split_size):
     ref64 = oracle.partition_prefix_f64(w, b.mean)
     got64 = b.prefix.astype(np.float64) + b.prefix_lo.astype(np.float64)
     assert np.abs(got64 - ref64).max() <= 4096 * float(w.max()) * 2.0 ** -20
+    assert b.mean64 == b.total / N
     ref = oracle.split_pack(w, b.idx, b.prefix, b.hc, b.mean, split_size, flags=2,
-                            elems=b.elems, prefix_lo=b.prefix_lo)
+                            elems=b.elems, prefix_lo=b.prefix_lo, mean64=b.mean64)
     assert same_table(b.table, ref)
     implied = oracle.alias_to_weights(b.table)
-    assert np.abs(implied - w / w.astype(np.float64).mean()).max() < 1e-3
+    target = w / w.astype(np.float64).mean()
+    assert np.all(np.abs(implied - target) <= 1e-3 + 1e-7 * target)
 
 
 @pytest.mark.parametrize("gen", list(GENS))
@@ -189,7 +192,8 @@ def test_split_pack_primitive_on_oracle_inputs(pkg, cuda, oracle):
     prefix = oracle.partition_prefix_f64(w, mean).astype(np.float32)
     wrs = W.WRS(pkg.AliasTableConfig(split_size=4))
     internals = W.Internals(wrs.handle, w.size)
-    W.check(W.lib().wrs_buffers_set_partition_info(internals.ptr, None, float(mean), hc))
+    W.check(W.lib().wrs_buffers_set_partition_info(internals.ptr, None, float(mean),
+                                                   oracle.total_mass(w) / w.size, hc))
     table = empty(2 * w.size, "i32")
     wrs.split_pack(None, h2d(w), h2d(idx), h2d(prefix), h2d(elems), w.size, table, internals)
     got = t2h(table, np.uint32).view(ENTRY_DTYPE)
