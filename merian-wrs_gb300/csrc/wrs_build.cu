@@ -265,6 +265,7 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
     float* __restrict__ prefix_lo_out, uint32_t spin_limit) {
     __shared__ float s_wh[kTileWarps], s_wl[kTileWarps];
     __shared__ uint32_t s_wc[kTileWarps];
+    __shared__ ff s_fh[kTileWarps], s_fl[kTileWarps];  // FFOUT: exact warp totals
     __shared__ PartCarry s_ex;
     __shared__ PartCarry s_agg;
 
@@ -302,6 +303,9 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
     uint32_t lex_c[4], voff_c[4];
     float run_h = 0.f, run_l = 0.f;
     uint32_t run_c = 0;
+    // FFOUT: the tile aggregate is also summed exactly (float-float), so that its FP32
+    // rounding does not accumulate along the lookback carry
+    ff fh{0.f, 0.f}, fl{0.f, 0.f};
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
         float th = 0.f, tl = 0.f;
@@ -310,9 +314,11 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
         for (int c = 0; c < 4; ++c) {
             if (x[v][c] > pivot) {
                 th = __fadd_rn(th, x[v][c]);
+                if constexpr (FFOUT) fh = ff_add_f(fh, x[v][c]);
                 ++tc;
             } else {
                 tl = __fadd_rn(tl, x[v][c]);
+                if constexpr (FFOUT) fl = ff_add_f(fl, x[v][c]);
             }
         }
         float ih = warp_incl_f(th, lane), il = warp_incl_f(tl, lane);
@@ -329,10 +335,18 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
         run_l = __fadd_rn(run_l, __shfl_sync(0xffffffffu, il, 31));
         run_c += __shfl_sync(0xffffffffu, ic, 31);
     }
+    if constexpr (FFOUT) {
+        fh = ff_warp_total(fh);
+        fl = ff_warp_total(fl);
+    }
     if (lane == 0) {
         s_wh[warp] = run_h;
         s_wl[warp] = run_l;
         s_wc[warp] = run_c;
+        if constexpr (FFOUT) {
+            s_fh[warp] = fh;
+            s_fl[warp] = fl;
+        }
     }
     __syncthreads();
     if (warp == 0) {
@@ -346,6 +360,10 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
         PartCarry agg{{__shfl_sync(0xffffffffu, ih, kTileWarps - 1), 0.f},
                       {__shfl_sync(0xffffffffu, il, kTileWarps - 1), 0.f},
                       __shfl_sync(0xffffffffu, ic, kTileWarps - 1)};
+        if constexpr (FFOUT) {
+            agg.h = ff_warp_total(lane < kTileWarps ? s_fh[lane] : ff{0.f, 0.f});
+            agg.l = ff_warp_total(lane < kTileWarps ? s_fl[lane] : ff{0.f, 0.f});
+        }
         __syncwarp();
         if (lane < kTileWarps) {
             s_wh[lane] = lane ? eh : 0.f;
@@ -618,13 +636,15 @@ __device__ __forceinline__ double prefix64(const PackIn& c, float hi, uint32_t p
         return static_cast<double>(hi);
 }
 
-// The float-float mode's exact decision for a probe near the crossing.  Kept out of line so
-// that the compiler cannot if-convert it into every probe (it runs on the slow FP64 pipe).
-__device__ __noinline__ bool ff_le(const PackIn& c, uint32_t j, uint32_t i, float heavy,
-                                   float light, double target64) {
-    const double h64 = j == 0 ? 0.0 : prefix64<true>(c, heavy, j - 1);
-    const double l64 = i == 0 ? 0.0 : prefix64<true>(c, light, c.n - i);
-    return __dadd_rn(h64, l64) <= target64;
+// The float-float mode's comparison sigma <= target, all in FP32: sigma = (h + hl) + (l + ll)
+// as two_sum(h, l) plus the low words, target = (t, tl) = the float-float split of
+// (total / N) * n.  The high parts are subtracted first (exact when they are within a factor
+// of two of each other, decisive otherwise), then the low parts are added.
+__device__ __forceinline__ bool ff_le(float h, float hl, float l, float ll, float t, float tl) {
+    const ff s = two_sum(h, l);
+    const float lo = __fadd_rn(__fadd_rn(s.lo, hl), ll);
+    const float d = __fsub_rn(s.hi, t);
+    return __fadd_rn(d, __fsub_rn(lo, tl)) <= 0.0f;
 }
 
 __device__ __forceinline__ float elem_at(const PackIn& c, uint32_t pos) {
@@ -640,13 +660,11 @@ __device__ __forceinline__ float elem_at(const PackIn& c, uint32_t pos) {
 // lightCount - 1 as in the shader, or lightCount (which keeps i + j = n at the end of the
 // table).  If every probe exceeds the target (the shader's b would wrap), j = 0.
 //
-// FF (float-float prefix): the comparison sigma <= target is decided on the exact values --
-// sigma = (hi + lo of the heavy prefix) + (hi + lo of the light prefix) and target =
-// (total / N) * n, evaluated in FP64 -- instead of on FP32 high words and the FP32 mean.  An
-// FP32 pre-test settles every probe whose high words differ by more than a few ulps (bound
-// m = (s + t) * 2^-21), so FP64 runs only near the crossing; the spill is then computed from
-// the float-float prefix in FP64 as well.  Measuring targets against the FP64 mean keeps the
-// FP32 rounding of the mean from piling up in the last heavy bucket.
+// FF (float-float prefix): the comparison sigma <= target is decided on float-float values
+// (ff_le) -- sigma from the high and low words of the heavy and light prefixes, target the
+// float-float form of (total / N) * n -- instead of on FP32 high words and the FP32 mean; the
+// spill is then computed from the float-float prefix in FP64.  Measuring targets against the
+// FP64 mean keeps the FP32 rounding of the mean from piling up in the last heavy bucket.
 template <bool R64, bool FF>
 __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, uint32_t& io,
                                               uint32_t& jo, float& spill) {
@@ -654,25 +672,24 @@ __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, 
     const float target = __fmul_rn(c.mean, __uint2float_rn(nsplit));
     const double target64 = FF ? __dmul_rn(c.mean64, static_cast<double>(nsplit))
                                : __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit));
+    float t_hi = 0.f, t_lo = 0.f;
+    if constexpr (FF) {
+        t_hi = __double2float_rn(target64);
+        t_lo = __double2float_rn(__dsub_rn(target64, static_cast<double>(t_hi)));
+    }
     const uint32_t lcm1 = c.lcap;
     while (a <= b) {
         const uint32_t j = static_cast<uint32_t>((a + b) >> 1);
         const uint32_t i = j > nsplit ? lcm1 : min(nsplit - j, lcm1);
         const float heavy = j == 0 ? 0.f : __ldg(c.prefix + j - 1);
         const float light = i == 0 ? 0.f : __ldg(c.prefix + c.n - i);
-        const float s32 = __fadd_rn(light, heavy);
         bool le;
         if constexpr (FF) {
-            const float d = __fsub_rn(s32, target);
-            const float m = __fmul_rn(__fadd_rn(s32, target), 4.76837158203125e-07f);
-            if (d > m)
-                le = false;
-            else if (d < -m)
-                le = true;
-            else
-                le = ff_le(c, j, i, heavy, light, target64);
+            const float hl = j == 0 ? 0.f : __ldg(c.prefix_lo + j - 1);
+            const float ll = i == 0 ? 0.f : __ldg(c.prefix_lo + c.n - i);
+            le = ff_le(heavy, hl, light, ll, t_hi, t_lo);
         } else {
-            le = s32 <= target;
+            le = __fadd_rn(light, heavy) <= target;
         }
         if (le)
             a = static_cast<int64_t>(j) + 1;

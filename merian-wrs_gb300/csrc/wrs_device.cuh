@@ -73,6 +73,19 @@ __device__ __forceinline__ ff shfl_xor_ff(ff v, int m) {
     return {__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
 }
 
+// float-float accumulation of one FP32 value
+__device__ __forceinline__ ff ff_add_f(ff a, float x) {
+    ff s = two_sum(a.hi, x);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+
+// float-float sum over the warp (butterfly; every lane gets the same value)
+__device__ __forceinline__ ff ff_warp_total(ff v) {
+#pragma unroll
+    for (int m = 1; m < 32; m <<= 1) v = carry_add<true>(v, shfl_xor_ff(v, m));
+    return v;
+}
+
 // ---------------------------------------------------------------------------
 // lookback words.  An ff word is {hi bits, lo bits | 1}: the LSB of lo's
 // mantissa is the ready bit (the value loses at most one ulp of lo).  A count

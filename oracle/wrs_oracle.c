@@ -227,10 +227,10 @@ void wrso_prefix_seq_f32(const float* w, uint64_t N, float* out) {
  * end of the table can have i + j < n, after which the last heavy bucket aliases a light
  * item that then gains mass; the full range keeps i + j = n.
  * prefix_lo != NULL (float-float prefix, prefix[] holding the high words): each comparison
- * sigma <= target is decided on sigma = (hi + lo of the heavy prefix) + (hi + lo of the
- * light prefix) and target = mean * n in FP64, after an FP32 pre-test on the high words
- * that settles probes differing by more than m = (s + t) * 2^-21; the spill is computed from
- * the float-float values in FP64.  This is the kernel's decision procedure step for step.
+ * sigma <= target is decided in FP32 float-float arithmetic -- two_sum of the heavy and light
+ * high words plus their low words, against the float-float split of target = mean64 * n
+ * (mean64 = total / N in FP64) -- and the spill is computed from the float-float values in
+ * FP64.  This is the kernel's decision procedure operation for operation.
  * Guard beyond the shader: if every probe exceeds the target (b would wrap to
  * 0xFFFFFFFF in the shader), j = 0 is used. */
 static inline double wrso_prefix64(const float* prefix_lo, float hi, uint32_t pos) {
@@ -247,6 +247,8 @@ void wrso_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_
     const float target = mean * (float)n;
     /* float-float mode: targets against the FP64 mean total / N */
     const double target64 = prefix_lo ? mean64 * (double)n : (double)mean * (double)n;
+    const float t_hi = (float)target64;
+    const float t_lo = (float)(target64 - (double)t_hi);
     while (a <= b) {
         uint32_t j = (uint32_t)((a + b) / 2);
         uint32_t i = (j > n) ? lcap : ((n - j) < lcap ? (n - j) : lcap);
@@ -255,18 +257,21 @@ void wrso_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_
         volatile float sigma = light + heavy;
         int le;
         if (prefix_lo) {
-            volatile float d = sigma - target;
-            volatile float st = sigma + target;
-            volatile float m = st * 4.76837158203125e-07f;
-            if (d > m) {
-                le = 0;
-            } else if (d < -m) {
-                le = 1;
-            } else {
-                double h64 = j == 0 ? 0.0 : wrso_prefix64(prefix_lo, heavy, j - 1);
-                double l64 = i == 0 ? 0.0 : wrso_prefix64(prefix_lo, light, N - i);
-                le = (h64 + l64) <= target64;
-            }
+            /* float-float comparison in FP32: two_sum(heavy, light) plus the low words
+             * against (t_hi, t_lo) = the float-float split of target64 */
+            const float hl = j == 0 ? 0.0f : prefix_lo[j - 1];
+            const float ll = i == 0 ? 0.0f : prefix_lo[N - i];
+            volatile float s = heavy + light;
+            volatile float bp = s - heavy;
+            volatile float ap = s - bp;
+            volatile float e1 = heavy - ap, e2 = light - bp;
+            volatile float e = e1 + e2;
+            volatile float lo1 = e + hl;
+            volatile float lo = lo1 + ll;
+            volatile float d = s - t_hi;
+            volatile float dl = lo - t_lo;
+            volatile float r = d + dl;
+            le = r <= 0.0f;
         } else {
             le = sigma <= target;
         }
