@@ -181,6 +181,21 @@ wrs_status wrs_alias_sample(const wrs_handle* h, void* stream, const wrs_alias_e
                             uint32_t* samples);
 wrs_status wrs_its_sample(const wrs_handle* h, void* stream, const float* cmf, uint32_t n,
                           uint64_t s, uint64_t seed, uint64_t offset, uint32_t* samples);
+/* Inclusive prefix sum (the scan of wrs_prefix_sum) that allocates no device memory, for
+ * callers that cannot call cudaMalloc -- e.g. code running under a host application whose
+ * pool already holds all device memory, code that must not take the device-wide
+ * synchronisation of cudaMalloc/cudaFree, or code called from inside another allocator.  No
+ * counterpart in the reference.  Instead of a wrs_buffers object it uses one fixed array
+ * of about 512 KiB in this library's own device memory, so n must be <= 2^26 (67,108,864;
+ * larger n returns WRS_ERR_CAPACITY).  The first call on a device looks up that array's
+ * address and caches it; make that first call before capturing the stream into a CUDA
+ * graph.  All calls share the array: each call clears it on `stream` before use, and calls
+ * whose work overlaps on the GPU (different streams, or concurrent host threads) race and
+ * give wrong results.  scan_precision is WRS_SCAN_FP32 or WRS_SCAN_COMPENSATED.  If
+ * device_status is not NULL, the WRS_DEVICE_* bits of this call are copied to that
+ * caller-owned device word on `stream`. */
+wrs_status wrs_prefix_sum_noalloc(void* stream, const float* in, uint32_t n, float* out,
+                                  uint32_t scan_precision, uint32_t* device_status);
 /* Test hook for the bounded-wait path: runs the scan of wrs_prefix_sum with its first
  * tile never scheduled (the tile ticket starts at 1) and a wait budget of `spin_limit`
  * polls, so every other tile's lookback runs out of budget.  The kernel still ends;

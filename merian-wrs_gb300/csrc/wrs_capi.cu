@@ -130,6 +130,11 @@ constexpr uint32_t kMaxN = 0x7fffffffu;  // indices are handled as int where the
 
 }  // namespace
 
+int wrs::set_last_error(int status, const char* msg) {
+    g_last_error = msg;
+    return status;
+}
+
 extern "C" {
 
 int wrs_version(void) { return WRS_VERSION; }

@@ -81,6 +81,10 @@ cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool
                               const float* cmf, uint32_t n, uint64_t s, uint64_t seed,
                               uint64_t offset, uint32_t* out);
 
+// Records `msg` as the calling thread's wrs_last_error() and returns `status`
+// (defined in wrs_capi.cu).
+int set_last_error(int status, const char* msg);
+
 inline uint32_t tiles_for(uint32_t n) {
     return static_cast<uint32_t>((static_cast<uint64_t>(n) + kTileItems - 1) / kTileItems);
 }
