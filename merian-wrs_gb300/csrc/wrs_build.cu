@@ -90,8 +90,11 @@ __global__ __launch_bounds__(kMassThreads) void k_total_mass(const float* __rest
         double total = 0.0;
         for (int k = 0; k < kMassThreads / 32; ++k) total = __dadd_rn(total, s_red[k]);
         ctrl->total = total;
-        ctrl->mean64 = n ? __ddiv_rn(total, static_cast<double>(n)) : 0.0;
-        ctrl->mean = __double2float_rn(ctrl->mean64);
+        const double m64 = n ? __ddiv_rn(total, static_cast<double>(n)) : 0.0;
+        const float m = __double2float_rn(m64);
+        ctrl->mean64 = m64;
+        ctrl->mean = m;
+        ctrl->mean_lo = __double2float_rn(__dsub_rn(m64, static_cast<double>(m)));
         ctrl->mass_done = 0u;
     }
 }
@@ -313,27 +316,34 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             if (x[v][c] > pivot) {
-                th = __fadd_rn(th, x[v][c]);
-                if constexpr (FFOUT) fh = ff_add_f(fh, x[v][c]);
+                if constexpr (FFOUT)
+                    fh = ff_add_f(fh, x[v][c]);
+                else
+                    th = __fadd_rn(th, x[v][c]);
                 ++tc;
             } else {
-                tl = __fadd_rn(tl, x[v][c]);
-                if constexpr (FFOUT) fl = ff_add_f(fl, x[v][c]);
+                if constexpr (FFOUT)
+                    fl = ff_add_f(fl, x[v][c]);
+                else
+                    tl = __fadd_rn(tl, x[v][c]);
             }
         }
-        float ih = warp_incl_f(th, lane), il = warp_incl_f(tl, lane);
         uint32_t ic = warp_incl_u(tc, lane);
-        float eh = __shfl_up_sync(0xffffffffu, ih, 1), el = __shfl_up_sync(0xffffffffu, il, 1);
         uint32_t ec = __shfl_up_sync(0xffffffffu, ic, 1);
-        lex_h[v] = lane ? eh : 0.f;
-        lex_l[v] = lane ? el : 0.f;
         lex_c[v] = lane ? ec : 0u;
-        voff_h[v] = run_h;
-        voff_l[v] = run_l;
         voff_c[v] = run_c;
-        run_h = __fadd_rn(run_h, __shfl_sync(0xffffffffu, ih, 31));
-        run_l = __fadd_rn(run_l, __shfl_sync(0xffffffffu, il, 31));
         run_c += __shfl_sync(0xffffffffu, ic, 31);
+        if constexpr (!FFOUT) {
+            // FP32 local scans (the float-float mode redoes them exactly after the lookback)
+            float ih = warp_incl_f(th, lane), il = warp_incl_f(tl, lane);
+            float eh = __shfl_up_sync(0xffffffffu, ih, 1), el = __shfl_up_sync(0xffffffffu, il, 1);
+            lex_h[v] = lane ? eh : 0.f;
+            lex_l[v] = lane ? el : 0.f;
+            voff_h[v] = run_h;
+            voff_l[v] = run_l;
+            run_h = __fadd_rn(run_h, __shfl_sync(0xffffffffu, ih, 31));
+            run_l = __fadd_rn(run_l, __shfl_sync(0xffffffffu, il, 31));
+        }
     }
     if constexpr (FFOUT) {
         fh = ff_warp_total(fh);
@@ -360,15 +370,24 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
         PartCarry agg{{__shfl_sync(0xffffffffu, ih, kTileWarps - 1), 0.f},
                       {__shfl_sync(0xffffffffu, il, kTileWarps - 1), 0.f},
                       __shfl_sync(0xffffffffu, ic, kTileWarps - 1)};
+        ff fxh{0.f, 0.f}, fxl{0.f, 0.f};  // FFOUT: exact warp-exclusive offsets
         if constexpr (FFOUT) {
-            agg.h = ff_warp_total(lane < kTileWarps ? s_fh[lane] : ff{0.f, 0.f});
-            agg.l = ff_warp_total(lane < kTileWarps ? s_fl[lane] : ff{0.f, 0.f});
+            const ff ith = ff_warp_incl(lane < kTileWarps ? s_fh[lane] : ff{0.f, 0.f}, lane);
+            const ff itl = ff_warp_incl(lane < kTileWarps ? s_fl[lane] : ff{0.f, 0.f}, lane);
+            agg.h = ff_shfl(ith, kTileWarps - 1);
+            agg.l = ff_shfl(itl, kTileWarps - 1);
+            fxh = ff_shfl_up_excl(ith, lane);
+            fxl = ff_shfl_up_excl(itl, lane);
         }
         __syncwarp();
         if (lane < kTileWarps) {
             s_wh[lane] = lane ? eh : 0.f;
             s_wl[lane] = lane ? el : 0.f;
             s_wc[lane] = lane ? ec : 0u;
+            if constexpr (FFOUT) {
+                s_fh[lane] = fxh;
+                s_fl[lane] = fxl;
+            }
         }
         PartCarry ex{{0.f, 0.f}, {0.f, 0.f}, 0u};
         if (tile == 0) {
@@ -392,10 +411,35 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
     const uint32_t light_before = tbase - ex.c;  // light items in tiles before this one
     const float wh = s_wh[warp], wl = s_wl[warp];
     const uint32_t wc = s_wc[warp];
+    // FFOUT: float-float running offsets (warp-exclusive, then per-v warp totals)
+    ff oh{0.f, 0.f}, ol{0.f, 0.f};
+    if constexpr (FFOUT) {
+        oh = s_fh[warp];
+        ol = s_fl[warp];
+    }
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-        float rh = __fadd_rn(__fadd_rn(wh, voff_h[v]), lex_h[v]);
-        float rl = __fadd_rn(__fadd_rn(wl, voff_l[v]), lex_l[v]);
+        float rh = 0.f, rl = 0.f;
+        ff fr_h{0.f, 0.f}, fr_l{0.f, 0.f};
+        if constexpr (FFOUT) {
+            // exact local scan: thread totals, float-float warp scan, running offsets
+            ff th{0.f, 0.f}, tl{0.f, 0.f};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                if (x[v][c] > pivot)
+                    th = ff_add_f(th, x[v][c]);
+                else
+                    tl = ff_add_f(tl, x[v][c]);
+            }
+            const ff ih = ff_warp_incl(th, lane), il = ff_warp_incl(tl, lane);
+            fr_h = carry_add<true>(oh, ff_shfl_up_excl(ih, lane));
+            fr_l = carry_add<true>(ol, ff_shfl_up_excl(il, lane));
+            oh = carry_add<true>(oh, ff_shfl(ih, 31));
+            ol = carry_add<true>(ol, ff_shfl(il, 31));
+        } else {
+            rh = __fadd_rn(__fadd_rn(wh, voff_h[v]), lex_h[v]);
+            rl = __fadd_rn(__fadd_rn(wl, voff_l[v]), lex_l[v]);
+        }
         uint32_t rc = wc + voff_c[v] + lex_c[v];  // heavy items before this one in the tile
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -406,20 +450,24 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
                 uint32_t pos;
                 ff val;
                 if (xv > pivot) {
-                    rh = __fadd_rn(rh, xv);
                     pos = ex.c + rc;
-                    if constexpr (FFOUT)
-                        val = carry_apply_ff(ex.h, rh);
-                    else
+                    if constexpr (FFOUT) {
+                        fr_h = ff_add_f(fr_h, xv);
+                        val = carry_add<true>(ex.h, fr_h);
+                    } else {
+                        rh = __fadd_rn(rh, xv);
                         val = {carry_apply<COMP>(ex.h, rh), 0.f};
+                    }
                     ++rc;
                 } else {
-                    rl = __fadd_rn(rl, xv);
                     pos = n - 1u - (light_before + (local - rc));
-                    if constexpr (FFOUT)
-                        val = carry_apply_ff(ex.l, rl);
-                    else
+                    if constexpr (FFOUT) {
+                        fr_l = ff_add_f(fr_l, xv);
+                        val = carry_add<true>(ex.l, fr_l);
+                    } else {
+                        rl = __fadd_rn(rl, xv);
                         val = {carry_apply<COMP>(ex.l, rl), 0.f};
+                    }
                 }
                 if (pos < n) {  // always true unless a lookback wait gave up
                     idx_out[pos] = e;
@@ -624,27 +672,32 @@ struct PackIn {
     uint32_t n, hc, lc;
     uint32_t lcap;  // largest light count a split may take: lc - 1 (shader) or lc
     float mean;
-    double mean64;  // total / N in FP64 (float-float mode)
+    float mean_lo;  // (mean, mean_lo) = total / N as a float-float pair
 };
 
-// prefix value at position pos as a double: hi only, or hi + lo of the float-float prefix
-template <bool FF>
-__device__ __forceinline__ double prefix64(const PackIn& c, float hi, uint32_t pos) {
-    if constexpr (FF)
-        return __dadd_rn(static_cast<double>(hi), static_cast<double>(__ldg(c.prefix_lo + pos)));
-    else
-        return static_cast<double>(hi);
-}
-
-// The float-float mode's comparison sigma <= target, all in FP32: sigma = (h + hl) + (l + ll)
-// as two_sum(h, l) plus the low words, target = (t, tl) = the float-float split of
-// (total / N) * n.  The high parts are subtracted first (exact when they are within a factor
-// of two of each other, decisive otherwise), then the low parts are added.
-__device__ __forceinline__ bool ff_le(float h, float hl, float l, float ll, float t, float tl) {
+// Float-float (FP32) evaluation of sigma - target with sigma = (h + hl) + (l + ll) and
+// target = (t + tl): two_sum of the high words plus the low words, then the high parts of
+// sigma and target are subtracted first (exact when within a factor of two of each other,
+// decisive otherwise) and the low parts added.  Rounded once to FP32.
+__device__ __forceinline__ float ff_sigma_minus(float h, float hl, float l, float ll, float t,
+                                                float tl) {
     const ff s = two_sum(h, l);
     const float lo = __fadd_rn(__fadd_rn(s.lo, hl), ll);
     const float d = __fsub_rn(s.hi, t);
-    return __fadd_rn(d, __fsub_rn(lo, tl)) <= 0.0f;
+    return __fadd_rn(d, __fsub_rn(lo, tl));
+}
+
+// (mean + mean_lo) * n as a float-float pair in FP32: n = n1 + n2 with n1 = n & ~0xff and
+// n2 = n & 0xff (both exact in FP32); the products of the high word are exact through FMA,
+// the low word's product is rounded once.
+__device__ __forceinline__ ff ff_target(float m, float ml, uint32_t n) {
+    const float n1 = __uint2float_rn(n & ~0xffu), n2 = __uint2float_rn(n & 0xffu);
+    const float p1 = __fmul_rn(m, n1), e1 = __fmaf_rn(m, n1, -p1);
+    const float p2 = __fmul_rn(m, n2), e2 = __fmaf_rn(m, n2, -p2);
+    const float p3 = __fmul_rn(ml, __uint2float_rn(n));
+    const ff s = two_sum(p1, p2);
+    const float lo = __fadd_rn(s.lo, __fadd_rn(__fadd_rn(e1, e2), p3));
+    return fast_two_sum(s.hi, lo);
 }
 
 __device__ __forceinline__ float elem_at(const PackIn& c, uint32_t pos) {
@@ -660,26 +713,23 @@ __device__ __forceinline__ float elem_at(const PackIn& c, uint32_t pos) {
 // lightCount - 1 as in the shader, or lightCount (which keeps i + j = n at the end of the
 // table).  If every probe exceeds the target (the shader's b would wrap), j = 0.
 //
-// FF (float-float prefix): the comparison sigma <= target is decided on float-float values
-// (ff_le) -- sigma from the high and low words of the heavy and light prefixes, target the
-// float-float form of (total / N) * n -- instead of on FP32 high words and the FP32 mean; the
-// spill is then computed from the float-float prefix in FP64.  Measuring targets against the
-// FP64 mean keeps the FP32 rounding of the mean from piling up in the last heavy bucket.
+// FF (float-float prefix): each comparison sigma <= target and the final spill are
+// evaluated on float-float values (ff_sigma_minus) -- sigma from the high and low words of
+// the heavy and light prefixes, target = (total / N) * n as a float-float pair (ff_target) --
+// instead of on FP32 high words and the FP32 mean, all in FP32 arithmetic (GB300 runs FP64
+// at a small fraction of the FP32 rate).  Measuring targets against the exact mean keeps the
+// FP32 rounding of the mean from piling up in the last heavy bucket.
 template <bool R64, bool FF>
 __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, uint32_t& io,
                                               uint32_t& jo, float& spill) {
-    int64_t a = 0, b = static_cast<int64_t>(c.hc) - 1;
+    // indices fit in int32 (n < 2^31); b becomes -1 when every probe exceeds the target
+    int a = 0, b = static_cast<int>(c.hc) - 1;
     const float target = __fmul_rn(c.mean, __uint2float_rn(nsplit));
-    const double target64 = FF ? __dmul_rn(c.mean64, static_cast<double>(nsplit))
-                               : __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit));
-    float t_hi = 0.f, t_lo = 0.f;
-    if constexpr (FF) {
-        t_hi = __double2float_rn(target64);
-        t_lo = __double2float_rn(__dsub_rn(target64, static_cast<double>(t_hi)));
-    }
+    ff tff{0.f, 0.f};
+    if constexpr (FF) tff = ff_target(c.mean, c.mean_lo, nsplit);
     const uint32_t lcm1 = c.lcap;
     while (a <= b) {
-        const uint32_t j = static_cast<uint32_t>((a + b) >> 1);
+        const uint32_t j = static_cast<uint32_t>(a + ((b - a) >> 1));
         const uint32_t i = j > nsplit ? lcm1 : min(nsplit - j, lcm1);
         const float heavy = j == 0 ? 0.f : __ldg(c.prefix + j - 1);
         const float light = i == 0 ? 0.f : __ldg(c.prefix + c.n - i);
@@ -687,23 +737,28 @@ __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, 
         if constexpr (FF) {
             const float hl = j == 0 ? 0.f : __ldg(c.prefix_lo + j - 1);
             const float ll = i == 0 ? 0.f : __ldg(c.prefix_lo + c.n - i);
-            le = ff_le(heavy, hl, light, ll, t_hi, t_lo);
+            le = ff_sigma_minus(heavy, hl, light, ll, tff.hi, tff.lo) <= 0.0f;
         } else {
             le = __fadd_rn(light, heavy) <= target;
         }
         if (le)
-            a = static_cast<int64_t>(j) + 1;
+            a = static_cast<int>(j) + 1;
         else
-            b = static_cast<int64_t>(j) - 1;
+            b = static_cast<int>(j) - 1;
     }
     const uint32_t j = b < 0 ? 0u : static_cast<uint32_t>(b);
     const uint32_t i = j > nsplit ? lcm1 : min(nsplit - j, lcm1);
     const float light = i == 0 ? 0.f : __ldg(c.prefix + c.n - i);
     const float heavy2 = __ldg(c.prefix + j);
-    if constexpr (R64 || FF) {
-        const double h64 = prefix64<FF>(c, heavy2, j);
-        const double l64 = i == 0 ? 0.0 : prefix64<FF>(c, light, c.n - i);
-        spill = __double2float_rn(__dsub_rn(__dadd_rn(h64, l64), target64));
+    if constexpr (FF) {
+        const float hl2 = __ldg(c.prefix_lo + j);
+        const float ll = i == 0 ? 0.f : __ldg(c.prefix_lo + c.n - i);
+        spill = ff_sigma_minus(heavy2, hl2, light, ll, tff.hi, tff.lo);
+    } else if constexpr (R64) {
+        const double target64 =
+            __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit));
+        spill = __double2float_rn(
+            __dsub_rn(__dadd_rn(static_cast<double>(heavy2), static_cast<double>(light)), target64));
     } else {
         spill = __fsub_rn(__fadd_rn(heavy2, light), target);
     }
@@ -802,7 +857,7 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(
         return;
     }
     PackIn c{w,      idx,    elems,  prefix, prefix_lo, n, hc,
-             n - hc, full_light ? n - hc : n - hc - 1u, ctrl->mean, ctrl->mean64};
+             n - hc, full_light ? n - hc : n - hc - 1u, ctrl->mean, ctrl->mean_lo};
     const uint32_t k = blockIdx.x * kSplitPack + threadIdx.x;
     uint32_t si = c.lc, sj = hc;  // past split K: the final split
     float sp = 0.f;

@@ -79,6 +79,26 @@ __device__ __forceinline__ ff ff_add_f(ff a, float x) {
     return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
 }
 
+__device__ __forceinline__ ff ff_shfl(ff v, int src) {
+    return {__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
+// inclusive float-float scan over the lanes of a warp
+__device__ __forceinline__ ff ff_warp_incl(ff v, int lane) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const ff o{__shfl_up_sync(0xffffffffu, v.hi, d), __shfl_up_sync(0xffffffffu, v.lo, d)};
+        if (lane >= d) v = carry_add<true>(o, v);
+    }
+    return v;
+}
+
+// exclusive value from an inclusive scan (lane 0 gets zero)
+__device__ __forceinline__ ff ff_shfl_up_excl(ff incl, int lane) {
+    const ff o{__shfl_up_sync(0xffffffffu, incl.hi, 1), __shfl_up_sync(0xffffffffu, incl.lo, 1)};
+    return lane ? o : ff{0.f, 0.f};
+}
+
 // float-float sum over the warp (butterfly; every lane gets the same value)
 __device__ __forceinline__ ff ff_warp_total(ff v) {
 #pragma unroll

@@ -44,9 +44,11 @@ struct alignas(64) BuildCtrl {
     double total;        // FP64 total mass
     LbCtrl part;         // prefix-partition launches
     LbCtrl scan;         // scan launches
-    double mean64;       // total / N in FP64 (split targets of the float-float mode)
+    double mean64;       // total / N in FP64
+    float mean_lo;       // (float)(mean64 - mean): mean64 as the float-float pair (mean, mean_lo)
+    uint32_t pad[15];
 };
-static_assert(sizeof(BuildCtrl) == 64, "BuildCtrl layout");
+static_assert(sizeof(BuildCtrl) == 128, "BuildCtrl layout");
 
 // Lookback state of one tile of the prefix-partition (64 B):
 //   q0 = {aggregate heavy sum, aggregate light sum}   (ff words)

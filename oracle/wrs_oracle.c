@@ -227,14 +227,44 @@ void wrso_prefix_seq_f32(const float* w, uint64_t N, float* out) {
  * end of the table can have i + j < n, after which the last heavy bucket aliases a light
  * item that then gains mass; the full range keeps i + j = n.
  * prefix_lo != NULL (float-float prefix, prefix[] holding the high words): each comparison
- * sigma <= target is decided in FP32 float-float arithmetic -- two_sum of the heavy and light
- * high words plus their low words, against the float-float split of target = mean64 * n
- * (mean64 = total / N in FP64) -- and the spill is computed from the float-float values in
- * FP64.  This is the kernel's decision procedure operation for operation.
+ * sigma <= target and the final spill are evaluated in FP32 float-float arithmetic
+ * (wrso_ff_sigma_minus) against target = (mean + mean_lo) * n as a float-float pair
+ * (wrso_ff_target), where mean_lo = (float)(mean64 - mean) and mean64 = total / N in FP64.
+ * This is the kernel's arithmetic operation for operation.
  * Guard beyond the shader: if every probe exceeds the target (b would wrap to
  * 0xFFFFFFFF in the shader), j = 0 is used. */
-static inline double wrso_prefix64(const float* prefix_lo, float hi, uint32_t pos) {
-    return prefix_lo ? (double)hi + (double)prefix_lo[pos] : (double)hi;
+static inline float wrso_ff_sigma_minus(float h, float hl, float l, float ll, float t, float tl) {
+    volatile float s = h + l;
+    volatile float bp = s - h;
+    volatile float ap = s - bp;
+    volatile float e1 = h - ap, e2 = l - bp;
+    volatile float e = e1 + e2;
+    volatile float lo1 = e + hl;
+    volatile float lo = lo1 + ll;
+    volatile float d = s - t;
+    volatile float dl = lo - tl;
+    return d + dl;
+}
+
+static inline void wrso_ff_target(float m, float ml, uint32_t n, float* t, float* tl) {
+    const float n1 = (float)(n & ~0xffu), n2 = (float)(n & 0xffu);
+    volatile float p1 = m * n1;
+    volatile float e1 = fmaf(m, n1, -p1);
+    volatile float p2 = m * n2;
+    volatile float e2 = fmaf(m, n2, -p2);
+    volatile float p3 = ml * (float)n;
+    volatile float s = p1 + p2;
+    volatile float bp = s - p1;
+    volatile float ap = s - bp;
+    volatile float x1 = p1 - ap, x2 = p2 - bp;
+    volatile float sl = x1 + x2;
+    volatile float e12 = e1 + e2;
+    volatile float e123 = e12 + p3;
+    volatile float lo = sl + e123;
+    volatile float hi = s + lo; /* fast two-sum */
+    volatile float hs = hi - s;
+    *t = hi;
+    *tl = lo - hs;
 }
 
 void wrso_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_t hc, float mean,
@@ -242,37 +272,23 @@ void wrso_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_
                 float* spill_out) {
     const uint32_t lc = N - hc;
     const uint32_t lcap = (flags & WRSO_SPLIT_FULL_LIGHT) ? lc : lc - 1;
-    const int residual_f64 = (flags & WRSO_SPLIT_F64) != 0 || prefix_lo != NULL;
+    const int residual_f64 = (flags & WRSO_SPLIT_F64) != 0;
     int64_t a = 0, b = (int64_t)hc - 1;
     const float target = mean * (float)n;
-    /* float-float mode: targets against the FP64 mean total / N */
-    const double target64 = prefix_lo ? mean64 * (double)n : (double)mean * (double)n;
-    const float t_hi = (float)target64;
-    const float t_lo = (float)(target64 - (double)t_hi);
+    float t_hi = 0.0f, t_lo = 0.0f;
+    if (prefix_lo) wrso_ff_target(mean, (float)(mean64 - (double)mean), n, &t_hi, &t_lo);
     while (a <= b) {
         uint32_t j = (uint32_t)((a + b) / 2);
         uint32_t i = (j > n) ? lcap : ((n - j) < lcap ? (n - j) : lcap);
         float heavy = j == 0 ? 0.0f : prefix[j - 1];
         float light = i == 0 ? 0.0f : prefix[N - i];
-        volatile float sigma = light + heavy;
         int le;
         if (prefix_lo) {
-            /* float-float comparison in FP32: two_sum(heavy, light) plus the low words
-             * against (t_hi, t_lo) = the float-float split of target64 */
             const float hl = j == 0 ? 0.0f : prefix_lo[j - 1];
             const float ll = i == 0 ? 0.0f : prefix_lo[N - i];
-            volatile float s = heavy + light;
-            volatile float bp = s - heavy;
-            volatile float ap = s - bp;
-            volatile float e1 = heavy - ap, e2 = light - bp;
-            volatile float e = e1 + e2;
-            volatile float lo1 = e + hl;
-            volatile float lo = lo1 + ll;
-            volatile float d = s - t_hi;
-            volatile float dl = lo - t_lo;
-            volatile float r = d + dl;
-            le = r <= 0.0f;
+            le = wrso_ff_sigma_minus(heavy, hl, light, ll, t_hi, t_lo) <= 0.0f;
         } else {
+            volatile float sigma = light + heavy;
             le = sigma <= target;
         }
         if (le)
@@ -285,10 +301,11 @@ void wrso_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_
     float light = i == 0 ? 0.0f : prefix[N - i];
     float heavy2 = prefix[j];
     float spill;
-    if (residual_f64) {
-        double h64 = wrso_prefix64(prefix_lo, heavy2, j);
-        double l64 = i == 0 ? 0.0 : wrso_prefix64(prefix_lo, light, N - i);
-        spill = (float)((h64 + l64) - target64);
+    if (prefix_lo) {
+        const float ll = i == 0 ? 0.0f : prefix_lo[N - i];
+        spill = wrso_ff_sigma_minus(heavy2, prefix_lo[j], light, ll, t_hi, t_lo);
+    } else if (residual_f64) {
+        spill = (float)(((double)heavy2 + (double)light) - (double)mean * (double)n);
     } else {
         volatile float sigma2 = heavy2 + light;
         spill = sigma2 - target;
