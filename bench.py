@@ -47,6 +47,9 @@ WORKLOAD = ("single large distribution: N=2^26 FP32 weights x 3 seeded distribut
             "(uniform(0,1], Zipf s=1.1 permuted, log-normal(0,2)); step = PSA alias build + "
             "S=2^28 alias samples (Philox4x32-10, uint32 indices)")
 METRIC = "samples/s"
+# PSA split size: 8 minimises split+pack time on GB300 at N = 2^26 (2.12 ms at 2, 0.80 ms at 8,
+# 1.16 ms at 32; float-float table accuracy does not depend on it)
+SPLIT_SIZE = 8
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "alias_sample_n26_s28.md")
 
 
@@ -161,10 +164,11 @@ def cpu_threads() -> int:
 def cpu_step(w_host, n: int, s: int, nthreads: int, s_sample: int) -> tuple[float, dict]:
     """One step of the CPU path: full PSA build of n weights + s_sample alias samples,
     extrapolated to s samples.  Returns (seconds per step, description)."""
-    from oracle.oracle import RNG_PHILOX4X32_10, SPLIT_F64, SPLIT_FULL_LIGHT, Oracle
+    from oracle.oracle import RNG_PHILOX4X32_10, SPLIT_FLOAT_FLOAT, SPLIT_FULL_LIGHT, Oracle
     orc = Oracle()
     t0 = time.perf_counter()
-    table, _, _ = orc.psa_build(w_host, 2, nthreads=nthreads, flags=SPLIT_F64 | SPLIT_FULL_LIGHT)
+    table, _, _ = orc.psa_build(w_host, SPLIT_SIZE, nthreads=nthreads,
+                                flags=SPLIT_FLOAT_FLOAT | SPLIT_FULL_LIGHT)
     t1 = time.perf_counter()
     orc.alias_sample(table, s_sample, 7, rng=RNG_PHILOX4X32_10, nthreads=nthreads)
     t2 = time.perf_counter()
@@ -204,7 +208,7 @@ def run_reference(args) -> None:
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "N": n, "S": s, "split_size": 2,
+        "config": {"workload": WORKLOAD, "N": n, "S": s, "split_size": SPLIT_SIZE,
                    "l2": "inputs larger than L2"},
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": nthreads, "kind": kind,
                          "sample": f"per step: full PSA build of N=2^{args.log2n} + "
@@ -240,7 +244,7 @@ def main() -> None:
     pkg.build()
     W = pkg.wrs
     n, s = 1 << args.log2n, 1 << args.log2s
-    cfg = W.AliasTableConfig(split_size=2, rng=W.RNG_PHILOX4X32_10,
+    cfg = W.AliasTableConfig(split_size=SPLIT_SIZE, rng=W.RNG_PHILOX4X32_10,
                              scan_precision=W.SCAN_FLOAT_FLOAT, split_residual_f64=True,
                              split_full_light=True)
     wrs = W.WRS(cfg)
@@ -342,9 +346,9 @@ def main() -> None:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "N": n, "S": s, "split_size": 2,
-                   "rng": "philox4x32-10", "scan": "fp32 + two-sum carry",
-                   "split": "fp64 residual, light cap fixed",
+        "config": {"workload": WORKLOAD, "N": n, "S": s, "split_size": SPLIT_SIZE,
+                   "rng": "philox4x32-10", "precision": "float-float partition prefix",
+                   "split": "float-float residual, light cap fixed",
                    "l2": "inputs larger than L2 (256 MB weights, 512 MB table, 1 GB samples)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 4 * n,
