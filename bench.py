@@ -17,7 +17,11 @@ needed between steps.
   cpu_baseline  the CPU port of the same path (oracle/, single thread) on a bounded sample
 
 Extra keys measure the rest of the configuration with the same events: per-kernel times
-and bandwidths, the decoupled scan (weights scanned/s) and ITS sampling (samples/s).
+and bandwidths, the decoupled scan (weights scanned/s) and ITS sampling (samples/s); and
+"batched", the mixed-size configuration (4096 distributions, N log-uniform in [64, 2^20],
+2^30 samples in total) as one CUDA graph against 4096 per-call build + sample pairs; and
+"served", a Poisson stream of 200k build+sample requests through the continuous-batching
+server (p50/p99 latency, samples/s, alone-vs-mix equality).
 
 `--impl reference` times the reference path's CPU implementation (the oracle port of
 the reference's CPU code; its own compiled CPU code when that loads here) on all host
@@ -63,6 +67,10 @@ def parse_args():
     p.add_argument("--log2s", type=int, default=LOG2_S)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the per-kernel breakdown")
+    p.add_argument("--no-batched", action="store_true",
+                   help="skip the batched mixed-size configuration (4096 distributions)")
+    p.add_argument("--no-served", action="store_true",
+                   help="skip the served request-stream configuration (200k requests)")
     return p.parse_args()
 
 
@@ -366,6 +374,11 @@ def main() -> None:
     if not args.no_extras:
         line["kernels"] = kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s,
                                            stream, pk["hbm_gbs"], args)
+    if not args.no_batched:
+        line["batched"] = batched_leg(W, cfg, dev, stream, max(3, args.steps // 2),
+                                      max(3, args.warmup))
+    if not args.no_served:
+        line["served"] = served_leg(W, cfg, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         w0 = weights[0].cpu().numpy()
         s_sample = 1 << min(args.log2s, 25)
@@ -379,6 +392,175 @@ def main() -> None:
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+BATCH_DISTS = 4096
+BATCH_LOG2_S = 30
+BATCH_SEED = 6
+
+
+def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
+    """The batched configuration: all 4096 distributions built and sampled by one CUDA graph
+    (wrs_batch_build + wrs_batch_sample: 4 launches), against 4096 per-call wrs_build +
+    wrs_sample pairs on the same stream, same inputs and seeds.  Both arms' samples are
+    compared bit for bit and their per-distribution RMSE reported."""
+    import numpy as np
+    import torch
+    wl = importlib.import_module("merian-wrs_gb300.workloads").batched(
+        dev, BATCH_DISTS, BATCH_LOG2_S, BATCH_SEED)
+    sizes, counts, w_off, s_off, w = wl["sizes"], wl["counts"], wl["w_off"], wl["s_off"], wl["w"]
+    D = len(sizes)
+    tables = torch.empty(2 * int(w_off[-1]), dtype=torch.int32, device=dev)
+    out_b = torch.empty(int(s_off[-1]), dtype=torch.int32, device=dev)
+    out_p = torch.empty_like(out_b)
+    seeds = [77 + d for d in range(D)]
+    h = W.Handle(cfg)
+    batch = W.Batch(h, D, int(sizes.sum()), int(counts.sum()))
+    wp, tp, bp, pp = w.data_ptr(), tables.data_ptr(), out_b.data_ptr(), out_p.data_ptr()
+    batch.set(stream, [(wp + 4 * int(w_off[d]), tp + 8 * int(w_off[d]), bp + 4 * int(s_off[d]),
+                        int(sizes[d]), int(counts[d]), seeds[d]) for d in range(D)])
+    batch.build(stream)
+    batch.sample(stream)
+    torch.cuda.synchronize()
+    assert batch.status() == 0
+    graph = torch.cuda.CUDAGraph()
+    gs = torch.cuda.Stream()
+    with torch.cuda.graph(graph, stream=gs):
+        batch.build(torch.cuda.current_stream())
+        batch.sample(torch.cuda.current_stream())
+    for _ in range(warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        graph.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1) / steps
+    assert batch.status() == 0
+
+    # per call: one buffers object sized for the largest distribution, reused
+    L = W.lib()
+    wrs = W.WRS(cfg)
+    internals = W.Internals(wrs.handle, int(sizes.max()))
+    hp, ip, sp = wrs.handle.ptr, internals.ptr, stream.cuda_stream
+    calls = [(wp + 4 * int(w_off[d]), int(sizes[d]), int(counts[d]), seeds[d],
+              pp + 4 * int(s_off[d])) for d in range(D)]
+    build, sample = L.wrs_build, L.wrs_sample_at
+
+    def per_call_pass():
+        for (wa, n, s, seed, oa) in calls:
+            build(hp, sp, wa, n, ip)
+            sample(hp, sp, ip, n, s, seed, 0, oa)
+
+    for _ in range(warmup):
+        per_call_pass()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        per_call_pass()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    per_call_ms = e0.elapsed_time(e1) / steps
+    assert internals.status() == 0
+
+    # accuracy: both arms bit for bit, and the RMSE of each distribution's histogram
+    identical = bool(torch.equal(out_b, out_p))
+    rmse = []
+    for d in range(D):
+        n, s = int(sizes[d]), int(counts[d])
+        if s == 0:
+            continue
+        smp = out_b[int(s_off[d]):int(s_off[d]) + s].long()
+        hist = torch.bincount(smp, minlength=n).double() / s
+        wd = w[int(w_off[d]):int(w_off[d]) + n].double()
+        rmse.append(float(torch.sqrt(torch.mean((hist - wd / wd.sum()) ** 2))))
+    total_s = int(counts.sum())
+    return {
+        "workload": f"batched mixed sizes: {D} distributions, N log-uniform in [64, 2^20] "
+                    f"(sum {int(sizes.sum())}), uniform(0,1] or Zipf s=1.1 per distribution "
+                    f"by seed; S_d proportional to N_d, sum 2^{BATCH_LOG2_S}; Philox4x32-10",
+        "distributions": D, "weights": int(sizes.sum()), "samples": total_s,
+        "graph_ms": batched_ms, "per_call_ms": per_call_ms,
+        "samples_per_s": total_s / (batched_ms / 1e3),
+        "per_call_samples_per_s": total_s / (per_call_ms / 1e3),
+        "builds_per_s": D / (batched_ms / 1e3),
+        "speedup_vs_per_call": per_call_ms / batched_ms,
+        "graph_launches": 4, "per_call_launches": 4 * D,
+        "samples_bitwise_equal": identical,
+        "rmse_mean": statistics.mean(rmse), "rmse_max": max(rmse),
+        "per_call_driver": "Python loop over the C ABI (wrs_build + wrs_sample_at per "
+                           "distribution), one reused buffers object",
+    }
+
+
+SERVED_REQUESTS = 200_000
+SERVED_RATE = 50_000.0
+SERVED_BUDGET = 16 << 30
+
+
+def served_leg(W, cfg, dev, n_requests: int = SERVED_REQUESTS) -> dict:
+    """The served configuration: a seeded Poisson stream of build+sample requests replayed in
+    real time through wrs_server_run_trace (continuous batching over 3 stream slots, alias
+    tables resident by id, 16 GiB device budget for tables and batch scratch).  Latency =
+    completion seen by the host loop - arrival.  A seeded subset of requests is recomputed
+    alone afterwards (a batch of one) and compared bit for bit with the served result."""
+    import numpy as np
+    import torch
+    wl = importlib.import_module("merian-wrs_gb300.workloads").served(
+        dev, n_requests, SERVED_RATE, seed=7)
+    w, s_off = wl["w"], wl["s_off"]
+    out = torch.zeros(int(s_off[-1]), dtype=torch.int32, device=dev)
+    h = W.Handle(cfg)
+    server = W.Server(h, memory_budget=SERVED_BUDGET)
+    wp, op = w.data_ptr(), out.data_ptr()
+    rows = [(int(wl["table_id"][i]), wp + 4 * int(wl["w_off"][i]), op + 4 * int(s_off[i]),
+             int(wl["n"][i]), int(wl["s"][i]), int(wl["seeds"][i])) for i in range(n_requests)]
+    reqs = W.Server.requests(rows)
+    # warm-up: a short prefix of the stream, then a fresh server for the measured run
+    server.run_trace(reqs, [0.0] * 64)
+    torch.cuda.synchronize()
+    del server
+    server = W.Server(h, memory_budget=SERVED_BUDGET)
+    comps = server.run_trace(reqs, [float(a) for a in wl["arrivals"]])
+    torch.cuda.synchronize()
+    st = server.stats()
+    lat = np.array([comps[i].done_s - comps[i].submit_s for i in range(n_requests)])
+    ok = all(comps[i].status == 0 for i in range(n_requests))
+    t_first = min(comps[i].submit_s for i in range(n_requests))
+    t_last = max(comps[i].done_s for i in range(n_requests))
+    makespan = t_last - t_first
+    total_s = int(wl["s"].sum())
+    # alone vs in the mix
+    rng = np.random.default_rng(70)
+    pick = rng.choice(n_requests, 64, replace=False)
+    batch = W.Batch(h, 1, int(wl["n"].max()), int(wl["s"].max()))
+    tab = torch.empty(2 * int(wl["n"].max()), dtype=torch.int32, device=dev)
+    alone = torch.empty(int(wl["s"].max()), dtype=torch.int32, device=dev)
+    equal = 0
+    for i in pick:
+        n, s_i = int(wl["n"][i]), int(wl["s"][i])
+        batch.set(None, [(wp + 4 * int(wl["w_off"][i]), tab, alone, n, s_i, int(wl["seeds"][i]))])
+        batch.build(None)
+        batch.sample(None)
+        equal += bool(torch.equal(alone[:s_i], out[int(s_off[i]):int(s_off[i]) + s_i]))
+    return {
+        "workload": f"served request stream: {n_requests} build+sample requests, Poisson "
+                    f"arrivals at {SERVED_RATE:.0f} req/s, N log-uniform in [256, 2^22] "
+                    f"log-normal(1.5) weights, S log-uniform in [1, 65536], 30% reuse a "
+                    f"recent table by id; 16 GiB budget; 3 stream slots",
+        "requests": n_requests, "samples": total_s, "all_ok": ok,
+        "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)),
+                       "p99": 1e3 * float(np.percentile(lat, 99)),
+                       "mean": 1e3 * float(lat.mean()), "max": 1e3 * float(lat.max())},
+        "samples_per_s": total_s / makespan, "requests_per_s": n_requests / makespan,
+        "offered_requests_per_s": SERVED_RATE, "makespan_s": makespan,
+        "batches": st["batches"], "builds": st["builds"], "resident_reuses": st["reuses"],
+        "evictions": st["evictions"], "table_bytes_peak": st["table_bytes_peak"],
+        "scratch_bytes": st["scratch_bytes"], "device_status": st["device_status"],
+        "alone_vs_mix_equal": f"{equal}/{len(pick)}",
+    }
 
 
 def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, peak, args):

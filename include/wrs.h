@@ -212,6 +212,119 @@ wrs_status wrs_buffers_set_partition_info(wrs_buffers* b, void* stream, float me
 /* device view of the FP64 mean (1 double) */
 const double* wrs_buffers_mean64(const wrs_buffers* b);
 
+/* ---- batches ------------------------------------------------------------------------
+ * Many independent distributions of any sizes, built and sampled with one launch per
+ * stage for the whole batch (3 build launches, 1 sampling launch), e.g. captured once into
+ * a CUDA graph and replayed.  No counterpart in the reference, whose WRS::build and
+ * WRS::sample (src/device/wrs/WRS.hpp:121-168) handle one distribution per call.  Each
+ * distribution's table and samples are bit-for-bit those of wrs_build + wrs_sample on the
+ * same weights, seed and handle configuration (total mass, partition and carries are
+ * deterministic in the compensated precisions), whatever else the batch holds.  Alias
+ * method only. */
+typedef struct wrs_batch wrs_batch;
+
+typedef struct wrs_dist_desc {
+    const float* weights;   /* device, n FP32 weights >= 0; NULL: the table is already built
+                               (sample only) */
+    wrs_alias_entry* table; /* device, n entries: written by wrs_batch_build (if weights),
+                               read by wrs_batch_sample (if samples) */
+    uint32_t* samples;      /* device, s indices for sample indices [0, s); NULL: build only */
+    uint64_t s;
+    uint64_t seed;
+    uint32_t n;             /* >= 1 */
+    uint32_t reserved;      /* 0 */
+} wrs_dist_desc;
+
+/* Capacity: at most max_dists distributions, max_weights weights summed over the
+ * distributions with weights, max_samples samples summed over all. */
+size_t wrs_batch_bytes(const wrs_handle* h, uint32_t max_dists, uint64_t max_weights,
+                       uint64_t max_samples);
+wrs_status wrs_batch_create(const wrs_handle* h, uint32_t max_dists, uint64_t max_weights,
+                            uint64_t max_samples, wrs_batch** out);
+void wrs_batch_destroy(wrs_batch* b);
+/* Sets the batch's distributions: copies the descriptors to the device and lays out the
+ * batch's tile, split and sampling grids (one small kernel) on `stream`.  The pointers the
+ * descriptors hold must stay valid while the batch is built or sampled.  Waits on the host
+ * until the previous wrs_batch_set of this batch has finished its upload; not for use
+ * inside a stream capture. */
+wrs_status wrs_batch_set(wrs_batch* b, void* stream, const wrs_dist_desc* descs,
+                         uint32_t count);
+uint32_t wrs_batch_count(const wrs_batch* b);
+/* Builds the table of every distribution with weights: 3 launches.  No host
+ * synchronisation and no allocation, so the call can be captured into a CUDA graph. */
+wrs_status wrs_batch_build(const wrs_handle* h, void* stream, wrs_batch* b);
+/* Samples every distribution with samples: 1 launch; capturable like wrs_batch_build. */
+wrs_status wrs_batch_sample(const wrs_handle* h, void* stream, wrs_batch* b);
+/* As wrs_buffers_status, for the batch's device status word. */
+wrs_status wrs_batch_status(wrs_batch* b, void* stream, uint32_t* device_status);
+
+/* ---- served request loop --------------------------------------------------------------
+ * Continuous batching of build+sample requests on top of the batches above.  No
+ * counterpart in the reference.  Requests queue on the host (wrs_server_submit); each
+ * wrs_server_progress call reaps finished batches, then admits queued requests in arrival
+ * order into a batch for a free slot (one CUDA stream and one wrs_batch per slot) while
+ * the device memory budget allows, and launches it, so that requests arriving while others
+ * run on the GPU join the next batch and their work overlaps with the batches in flight.
+ * Alias tables stay resident by table_id: a request naming a resident table only samples;
+ * otherwise its table is built into the server's table arena, evicting the least recently
+ * used tables that no batch in flight uses.  The budget covers the table arena and every
+ * slot's batch scratch; weights and sample buffers are the caller's.  Each request's
+ * samples equal those of a per-call wrs_build + wrs_sample of its weights and seed, in the
+ * compensated precisions (see the batches above).  A server is not thread-safe. */
+typedef struct wrs_server wrs_server;
+
+typedef struct wrs_server_config {
+    uint64_t memory_budget;     /* device bytes: table arena + batch scratch (default 16 GiB) */
+    uint32_t slots;             /* batches in flight, one stream each (default 3) */
+    uint32_t max_batch_dists;   /* requests per batch (default 1024) */
+    uint64_t max_batch_weights; /* weights built per batch; bounds a request's n
+                                   (default 2^25) */
+    uint64_t max_batch_samples; /* samples per batch; bounds a request's s (default 2^24) */
+} wrs_server_config;
+
+typedef struct wrs_request {
+    uint64_t table_id;     /* requests naming the same id share one table (same weights) */
+    const float* weights;  /* device, n weights >= 0; read only when the table is built */
+    uint32_t* samples;     /* device, s indices (sample indices [0, s) of the stream) */
+    uint64_t s;
+    uint64_t seed;
+    uint32_t n;            /* 1 <= n <= max_batch_weights */
+    uint32_t reserved;     /* 0 */
+} wrs_request;
+
+typedef struct wrs_completion {
+    uint64_t ticket;   /* from wrs_server_submit */
+    double submit_s;   /* host steady clock, seconds: submission (or trace arrival) */
+    double done_s;     /* host steady clock, seconds: the batch was seen complete */
+    uint32_t built;    /* 1: the table was built for this request; 0: a resident one */
+    uint32_t status;   /* wrs_status of the request */
+} wrs_completion;
+
+typedef struct wrs_server_stats {
+    uint64_t submitted, completed, batches, builds, reuses, evictions;
+    uint64_t table_arena_bytes, table_bytes_peak, scratch_bytes;
+    uint64_t device_status; /* OR of the batches' WRS_DEVICE_* bits */
+} wrs_server_stats;
+
+wrs_status wrs_server_config_init(wrs_server_config* c);
+wrs_status wrs_server_create(const wrs_handle* h, const wrs_server_config* c,
+                             wrs_server** out);
+void wrs_server_destroy(wrs_server* s);
+/* Queues a request (host only, no GPU work). */
+wrs_status wrs_server_submit(wrs_server* s, const wrs_request* r, uint64_t* ticket);
+/* One non-blocking scheduling step (reap, admit, launch); writes up to max_out completions. */
+wrs_status wrs_server_progress(wrs_server* s, wrs_completion* out, uint32_t max_out,
+                               uint32_t* count);
+/* Number of submitted requests not yet reported complete. */
+uint64_t wrs_server_pending(const wrs_server* s);
+wrs_status wrs_server_get_stats(const wrs_server* s, wrs_server_stats* st);
+/* Replays a trace in real time: request i is submitted arrival_s[i] seconds after the call
+ * starts (arrival_s ascending), progress runs until every request completed, and out[i]
+ * receives request i's completion with submit_s = the call's start + arrival_s[i]. */
+wrs_status wrs_server_run_trace(wrs_server* s, const wrs_request* reqs,
+                                const double* arrival_s, uint32_t count,
+                                wrs_completion* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -8,60 +8,94 @@
 //   k_split_pack        PSA split search + pack, one thread per split
 //                                                          (src/device/wrs/alias/psa/splitpack/inline/shader.comp)
 //
+// The total-mass, partition and split+pack kernels come in two forms from one body: a
+// single distribution (BATCH = false; CTA b works on tile / split block b), and a batch
+// of distributions of any sizes in one launch (BATCH = true; a per-CTA map names the
+// distribution, whose tiles and split blocks are numbered from its first one).  A
+// distribution's results do not depend on the form or on the other distributions.
+//
 // All lookback kernels take their tile index from an atomic ticket (a tile only ever
-// waits for tiles whose CTAs already run), bound every spin (kSpinLimit polls, then
-// raise kStatusTimeout and continue), and clean up after themselves: the state buffer
-// is double-buffered by an epoch; each launch clears the half the next launch will use,
-// and its last CTA resets the ticket and advances the epoch.
+// waits for tiles whose CTAs already run; a batch's distributions occupy consecutive
+// ticket ranges), bound every spin (kSpinLimit polls, then raise kStatusTimeout and
+// continue), and clean up after themselves: the state buffer is double-buffered by an
+// epoch; each launch clears the half the next launch will use, and its last CTA resets
+// the ticket and advances the epoch.
 #include "wrs_device.cuh"
 #include "wrs_internal.cuh"
 
 namespace wrs {
 
 // ---------------------------------------------------------------------------------
+// tile loads
+// ---------------------------------------------------------------------------------
+
+// Items of local tile `lt` held by this thread: x[v][c] = item lt*4096 + warp*512 + v*128 +
+// lane*4 + c (16-byte loads, fully coalesced, where the tile is whole and aligned); items
+// past n read as 0.
+__device__ __forceinline__ void load_tile(const float* __restrict__ w, uint32_t n, uint32_t lt,
+                                          float (&x)[4][4]) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t tbase = lt * kTileItems;
+    const uint32_t wbase = tbase + warp * kWarpItems;
+    const bool full = (static_cast<uint64_t>(tbase) + kTileItems <= n) &&
+                      ((reinterpret_cast<uintptr_t>(w) & 15u) == 0);
+    if (full) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            float4 q = __ldcs(reinterpret_cast<const float4*>(w + wbase + v * 128 + lane * 4));
+            x[v][0] = q.x;
+            x[v][1] = q.y;
+            x[v][2] = q.z;
+            x[v][3] = q.w;
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                uint32_t e = wbase + v * 128 + lane * 4 + c;
+                x[v][c] = e < n ? __ldg(w + e) : 0.0f;
+            }
+    }
+}
+
+// ---------------------------------------------------------------------------------
 // total mass
 // ---------------------------------------------------------------------------------
 
-// Per-thread compensated FP32 accumulation (two-sum) over 16-byte vector loads, FP64
-// across threads and CTAs.  The last CTA sums the per-CTA partials in a fixed order, so
-// the result depends only on N and the data (deterministic).
-__global__ __launch_bounds__(kMassThreads) void k_total_mass(const float* __restrict__ w,
-                                                             uint32_t n,
+// One CTA per 4096-item tile.  Each thread sums its 16 items in a fixed order with a
+// compensated FP32 accumulator (two-sum), the CTA combines its threads in FP64 in a fixed
+// tree, and the last tile of the distribution to finish sums the tile partials in a fixed
+// order.  The total is therefore a function of the weights alone (not of the launch
+// geometry, of the buffer's alignment or of other distributions in a batch).
+template <bool BATCH>
+__global__ __launch_bounds__(kTileThreads) void k_total_mass(const float* __restrict__ w_in,
+                                                             uint32_t n_in,
                                                              double* __restrict__ partials,
-                                                             BuildCtrl* __restrict__ ctrl) {
-    __shared__ double s_red[kMassThreads / 32];
+                                                             BuildCtrl* __restrict__ ctrl_in,
+                                                             BatchView bv) {
+    __shared__ double s_red[kTileWarps];
     __shared__ bool s_last;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nth = gridDim.x * blockDim.x;
-
+    const uint32_t tile = blockIdx.x;
+    const float* w = w_in;
+    uint32_t n = n_in, first = 0;
+    BuildCtrl* ctrl = ctrl_in;
+    if constexpr (BATCH) {
+        const uint32_t d = __ldg(bv.tile_map + tile);
+        const DistDesc* D = bv.dist + d;
+        w = D->w;
+        n = D->n;
+        first = D->tile0;
+        ctrl = bv.dctrl + d;
+    }
+    const uint32_t lt = tile - first, ntiles = tiles_for(n);
+    float x[4][4];
+    load_tile(w, n, lt, x);
     ff acc = {0.0f, 0.0f};
-    uint32_t head = static_cast<uint32_t>(((16u - (reinterpret_cast<uintptr_t>(w) & 15u)) & 15u) / 4u);
-    if (head > n) head = n;
-    if (tid < head) acc = carry_add<true>(acc, ff{__ldg(w + tid), 0.0f});
-    const float4* w4 = reinterpret_cast<const float4*>(w + head);
-    const uint32_t n4 = (n - head) / 4u;
-    uint32_t i = tid;
-    for (; i + 3u * nth < n4; i += 4u * nth) {
-        float4 v[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = __ldcs(w4 + i + u * nth);
+    for (int v = 0; v < 4; ++v)
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            acc = carry_add<true>(acc, ff{v[u].x, 0.0f});
-            acc = carry_add<true>(acc, ff{v[u].y, 0.0f});
-            acc = carry_add<true>(acc, ff{v[u].z, 0.0f});
-            acc = carry_add<true>(acc, ff{v[u].w, 0.0f});
-        }
-    }
-    for (; i < n4; i += nth) {
-        float4 v = __ldcs(w4 + i);
-        acc = carry_add<true>(acc, ff{v.x, 0.0f});
-        acc = carry_add<true>(acc, ff{v.y, 0.0f});
-        acc = carry_add<true>(acc, ff{v.z, 0.0f});
-        acc = carry_add<true>(acc, ff{v.w, 0.0f});
-    }
-    for (uint32_t t = head + 4u * n4 + tid; t < n; t += nth)
-        acc = carry_add<true>(acc, ff{__ldg(w + t), 0.0f});
+        for (int c = 0; c < 4; ++c) acc = carry_add<true>(acc, ff{x[v][c], 0.0f});
 
     double d = __dadd_rn(static_cast<double>(acc.hi), static_cast<double>(acc.lo));
 #pragma unroll
@@ -71,24 +105,26 @@ __global__ __launch_bounds__(kMassThreads) void k_total_mass(const float* __rest
     __syncthreads();
     if (threadIdx.x == 0) {
         double b = 0.0;
-        for (int k = 0; k < kMassThreads / 32; ++k) b = __dadd_rn(b, s_red[k]);
-        partials[blockIdx.x] = b;
+        for (int k = 0; k < kTileWarps; ++k) b = __dadd_rn(b, s_red[k]);
+        partials[tile] = b;
         __threadfence();
-        uint32_t prev = atomicAdd(&ctrl->mass_done, 1u);
-        s_last = (prev == gridDim.x - 1);
+        const uint32_t prev = atomicAdd(&ctrl->mass_done, 1u);
+        s_last = (prev == ntiles - 1u);
     }
     __syncthreads();
     if (!s_last) return;
     __threadfence();
     double t = 0.0;
-    for (uint32_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) t = __dadd_rn(t, __ldcg(partials + k));
+    for (uint32_t k = threadIdx.x; k < ntiles; k += blockDim.x)
+        t = __dadd_rn(t, __ldcg(partials + first + k));
 #pragma unroll
     for (int m = 16; m > 0; m >>= 1) t = __dadd_rn(t, __shfl_xor_sync(0xffffffffu, t, m));
+    __syncthreads();
     if (lane == 0) s_red[warp] = t;
     __syncthreads();
     if (threadIdx.x == 0) {
         double total = 0.0;
-        for (int k = 0; k < kMassThreads / 32; ++k) total = __dadd_rn(total, s_red[k]);
+        for (int k = 0; k < kTileWarps; ++k) total = __dadd_rn(total, s_red[k]);
         ctrl->total = total;
         const double m64 = n ? __ddiv_rn(total, static_cast<double>(n)) : 0.0;
         const float m = __double2float_rn(m64);
@@ -101,11 +137,7 @@ __global__ __launch_bounds__(kMassThreads) void k_total_mass(const float* __rest
 
 cudaError_t launch_total_mass(cudaStream_t st, const float* w, uint32_t n, double* partials,
                               BuildCtrl* ctrl) {
-    uint32_t blocks = static_cast<uint32_t>((static_cast<uint64_t>(n) + kMassThreads * 16 - 1) /
-                                            (kMassThreads * 16));
-    if (blocks < 1) blocks = 1;
-    if (blocks > static_cast<uint32_t>(kMassMaxBlocks)) blocks = kMassMaxBlocks;
-    k_total_mass<<<blocks, kMassThreads, 0, st>>>(w, n, partials, ctrl);
+    k_total_mass<false><<<tiles_for(n), kTileThreads, 0, st>>>(w, n, partials, ctrl, BatchView{});
     return cudaGetLastError();
 }
 
@@ -167,58 +199,24 @@ __device__ __forceinline__ void lookback_end(LbCtrl* ctrl) {
     }
 }
 
-// ---------------------------------------------------------------------------------
-// fused prefix-partition
-// ---------------------------------------------------------------------------------
-
-struct PartCarry {
-    ff h, l;
-    uint32_t c;
-};
-
-template <bool COMP>
-__device__ __forceinline__ PartCarry part_add(PartCarry a, PartCarry b) {
-    return {carry_add<COMP>(a.h, b.h), carry_add<COMP>(a.l, b.l), a.c + b.c};
-}
-
-template <bool COMP>
-__device__ __forceinline__ PartCarry part_warp_sum(PartCarry v) {
-#pragma unroll
-    for (int m = 1; m < 32; m <<= 1) {
-        PartCarry o{shfl_xor_ff(v.h, m), shfl_xor_ff(v.l, m), __shfl_xor_sync(0xffffffffu, v.c, m)};
-        v = part_add<COMP>(v, o);
-    }
-    return v;
-}
-
-// Runs on warp 0 only; returns the exclusive prefix of `tile` in every lane.
-template <bool COMP>
-__device__ PartCarry part_lookback(const PartState* st, uint32_t tile, uint32_t* status,
-                                   uint32_t spin_limit) {
+// Decoupled-lookback window walk shared by the partition and scan lookbacks.  `probe(pos,
+// v)` reads tile pos's state into v and returns 2 (inclusive prefix), 1 (aggregate only) or
+// 0 (not yet published); `sum(v, take)` returns the warp total of v over lanes < take;
+// `acc(ex, v)` adds.  Tiles before `first` count as published zeros.  Runs on one warp; the
+// result is valid in every lane.
+template <class V, class Probe, class Sum, class Acc>
+__device__ __forceinline__ V lookback_walk(uint32_t tile, uint32_t first, uint32_t* status,
+                                           uint32_t spin_limit, V zero, Probe probe, Sum sum,
+                                           Acc acc) {
     const int lane = threadIdx.x & 31;
-    PartCarry ex{{0.f, 0.f}, {0.f, 0.f}, 0u};
+    V ex = zero;
     int64_t base = static_cast<int64_t>(tile) - 1;
     uint32_t spins = 0;
     for (;;) {
         const int64_t pos = base - lane;
         int s = 2;
-        PartCarry v{{0.f, 0.f}, {0.f, 0.f}, 0u};
-        if (pos >= 0) {
-            const unsigned long long* q = reinterpret_cast<const unsigned long long*>(st + pos);
-            unsigned long long ah, al, ac, pc, ph, pl;
-            ld_relaxed_v2(q + 0, ah, al);
-            ld_relaxed_v2(q + 2, ac, pc);
-            ld_relaxed_v2(q + 4, ph, pl);
-            if (ff_ready(ph) && ff_ready(pl) && cnt_ready(pc)) {
-                s = 2;
-                v = {unpack_ff(ph), unpack_ff(pl), static_cast<uint32_t>(pc)};
-            } else if (ff_ready(ah) && ff_ready(al) && cnt_ready(ac)) {
-                s = 1;
-                v = {unpack_ff(ah), unpack_ff(al), static_cast<uint32_t>(ac)};
-            } else {
-                s = 0;
-            }
-        }
+        V v = zero;
+        if (pos >= static_cast<int64_t>(first)) s = probe(static_cast<uint32_t>(pos), v);
         const unsigned nr = __ballot_sync(0xffffffffu, s == 0);
         const unsigned dn = __ballot_sync(0xffffffffu, s == 2);
         const int first_nr = nr ? __ffs(nr) - 1 : 32;
@@ -226,8 +224,7 @@ __device__ PartCarry part_lookback(const PartState* st, uint32_t tile, uint32_t*
         const bool finish = first_dn < first_nr;
         const int take = finish ? first_dn + 1 : first_nr;
         if (take > 0) {
-            PartCarry c = lane < take ? v : PartCarry{{0.f, 0.f}, {0.f, 0.f}, 0u};
-            ex = part_add<COMP>(ex, part_warp_sum<COMP>(c));
+            ex = acc(ex, sum(lane < take ? v : zero));
             base -= take;
             spins = 0;
         }
@@ -243,204 +240,384 @@ __device__ PartCarry part_lookback(const PartState* st, uint32_t tile, uint32_t*
     return ex;
 }
 
-__device__ __forceinline__ void part_publish_agg(PartState* s, const PartCarry& a) {
-    unsigned long long* q = reinterpret_cast<unsigned long long*>(s);
-    st_relaxed_v2(q + 0, pack_ff(a.h), pack_ff(a.l));
-    st_relaxed(q + 2, pack_cnt(a.c));
+// ---------------------------------------------------------------------------------
+// fused prefix-partition
+// ---------------------------------------------------------------------------------
+
+// FP32-mode carry (reference arithmetic; association depends on lookback timing)
+struct PartCarry {
+    float h, l;
+    uint32_t c;
+};
+// exact carry of the compensated modes
+struct PartX {
+    u128 h, l;
+    uint32_t c;
+};
+
+__device__ __forceinline__ PartCarry part_sum_f(PartCarry v) {
+#pragma unroll
+    for (int m = 1; m < 32; m <<= 1) {
+        v.h = __fadd_rn(v.h, __shfl_xor_sync(0xffffffffu, v.h, m));
+        v.l = __fadd_rn(v.l, __shfl_xor_sync(0xffffffffu, v.l, m));
+        v.c += __shfl_xor_sync(0xffffffffu, v.c, m);
+    }
+    return v;
 }
-__device__ __forceinline__ void part_publish_pre(PartState* s, const PartCarry& p) {
-    unsigned long long* q = reinterpret_cast<unsigned long long*>(s);
-    st_relaxed_v2(q + 4, pack_ff(p.h), pack_ff(p.l));
-    st_relaxed(q + 3, pack_cnt(p.c));
+__device__ __forceinline__ PartX part_sum_x(PartX v) {
+#pragma unroll
+    for (int m = 1; m < 32; m <<= 1) {
+        v.h += shfl_xor_u128(v.h, m);
+        v.l += shfl_xor_u128(v.l, m);
+        v.c += __shfl_xor_sync(0xffffffffu, v.c, m);
+    }
+    return v;
 }
+
+__device__ PartX part_lookback_x(const PartState* st, uint32_t tile, uint32_t first,
+                                 uint32_t* status, uint32_t spin_limit) {
+    const PartX zero{0, 0, 0u};
+    return lookback_walk(
+        tile, first, status, spin_limit, zero,
+        [st](uint32_t pos, PartX& v) -> int {
+            // inclusive words first; the aggregate only where those are not yet published
+            const unsigned long long* q = st[pos].q;
+            unsigned long long h0, h1, l0, l1, c, pad;
+            ld_relaxed_v2(q + 8, h0, h1);
+            ld_relaxed_v2(q + 10, l0, l1);
+            ld_relaxed_v2(q + 6, c, pad);
+            int s = 2;
+            if (!(fx_ready(h0, h1) && fx_ready(l0, l1) && cnt_ready(c))) {
+                ld_relaxed_v2(q + 0, h0, h1);
+                ld_relaxed_v2(q + 2, l0, l1);
+                ld_relaxed_v2(q + 4, c, pad);
+                s = fx_ready(h0, h1) && fx_ready(l0, l1) && cnt_ready(c) ? 1 : 0;
+            }
+            if (s) v = {fx_unpack(h0, h1), fx_unpack(l0, l1), static_cast<uint32_t>(c)};
+            return s;
+        },
+        [](PartX v) { return part_sum_x(v); },
+        [](PartX a, PartX b) { return PartX{a.h + b.h, a.l + b.l, a.c + b.c}; });
+}
+
+__device__ PartCarry part_lookback_f(const PartState* st, uint32_t tile, uint32_t first,
+                                     uint32_t* status, uint32_t spin_limit) {
+    const PartCarry zero{0.f, 0.f, 0u};
+    return lookback_walk(
+        tile, first, status, spin_limit, zero,
+        [st](uint32_t pos, PartCarry& v) -> int {
+            const unsigned long long* q = st[pos].q;
+            unsigned long long h, l, c, pad;
+            ld_relaxed_v2(q + 8, h, l);
+            ld_relaxed_v2(q + 6, c, pad);
+            int s = 2;
+            if (!(ff_ready(h) && ff_ready(l) && cnt_ready(c))) {
+                ld_relaxed_v2(q + 0, h, l);
+                ld_relaxed_v2(q + 4, c, pad);
+                s = ff_ready(h) && ff_ready(l) && cnt_ready(c) ? 1 : 0;
+            }
+            if (s) v = {unpack_ff(h).hi, unpack_ff(l).hi, static_cast<uint32_t>(c)};
+            return s;
+        },
+        [](PartCarry v) { return part_sum_f(v); },
+        [](PartCarry a, PartCarry b) {
+            return PartCarry{__fadd_rn(a.h, b.h), __fadd_rn(a.l, b.l), a.c + b.c};
+        });
+}
+
+__device__ __forceinline__ void part_publish_x(PartState* s, const PartX& a, bool incl) {
+    unsigned long long* q = s->q + (incl ? 8 : 0);
+    st_relaxed_v2(q + 0, fx_word_lo(a.h), fx_word_hi(a.h));
+    st_relaxed_v2(q + 2, fx_word_lo(a.l), fx_word_hi(a.l));
+    st_relaxed(s->q + (incl ? 6 : 4), pack_cnt(a.c));
+}
+__device__ __forceinline__ void part_publish_f(PartState* s, const PartCarry& a, bool incl) {
+    st_relaxed_v2(s->q + (incl ? 8 : 0), pack_ff(ff{a.h, 0.f}), pack_ff(ff{a.l, 0.f}));
+    st_relaxed(s->q + (incl ? 6 : 4), pack_cnt(a.c));
+}
+
+struct PartArgs {
+    const float* w;  // single distribution: weights, n, control block
+    uint32_t n;
+    BuildCtrl* ctrl;
+    LbCtrl* lb;
+    PartState* states;
+    uint32_t cap_tiles;
+    uint32_t spin_limit;
+    uint32_t* status;
+    uint32_t* idx;  // outputs (a batch adds each distribution's base)
+    float* prefix;
+    float* elems;
+    float* prefix_lo;
+};
 
 // One CTA = one tile of 4096 weights; warp w owns items [w*512, w*512+512) of the tile and
 // lane L holds, for v = 0..3, the 4 consecutive items at v*128 + L*4 (16-byte loads, fully
 // coalesced).  Heavy (w > mean) items go to idx[heavyRank], light items to
 // idx[N-1-lightRank]; prefix[] holds the inclusive heavy resp. light prefix sum, elems[] the
-// weight (shader.comp:329-361).  FFOUT (with the compensated carry) also writes prefix_lo[],
-// the low word of the prefix as a float-float pair (prefix[] is its high word).
-template <bool COMP, bool FFOUT>
-__global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
-    const float* __restrict__ w, uint32_t n, BuildCtrl* __restrict__ ctrl,
-    PartState* __restrict__ states, uint32_t cap_tiles, uint32_t* __restrict__ idx_out,
-    float* __restrict__ prefix_out, float* __restrict__ elems_out,
-    float* __restrict__ prefix_lo_out, uint32_t spin_limit) {
-    __shared__ float s_wh[kTileWarps], s_wl[kTileWarps];
+// weight (shader.comp:329-361).
+//
+// COMP (compensated modes): the tile aggregates and the lookback carry are exact fixed-point
+// sums (fx_*), rounded once to a float-float carry per tile; local sums within the tile run in
+// a fixed order.  Every prefix is then a deterministic function of the weights.  FFOUT also
+// writes prefix_lo[], the low word of the prefix as a float-float pair (prefix[] is its high
+// word), with the local sums in float-float as well.
+template <bool COMP, bool FFOUT, bool BATCH>
+__global__ __launch_bounds__(kTileThreads) void k_prefix_partition(PartArgs a, BatchView bv) {
+    // warp totals (phase A), turned into warp-exclusive offsets by warp 0 (phase B)
     __shared__ uint32_t s_wc[kTileWarps];
-    __shared__ ff s_fh[kTileWarps], s_fl[kTileWarps];  // FFOUT: exact warp totals
-    __shared__ PartCarry s_ex;
-    __shared__ PartCarry s_agg;
+    __shared__ float s_wh[kTileWarps], s_wl[kTileWarps];  // local FP32 sums (!FFOUT)
+    __shared__ ff s_fh[kTileWarps], s_fl[kTileWarps];     // local float-float sums (FFOUT)
+    __shared__ u128 s_xh[kTileWarps], s_xl[kTileWarps];   // exact sums (COMP)
+    __shared__ ff s_exh, s_exl;
+    __shared__ uint32_t s_exc, s_aggc;
+    __shared__ float4 s_x[kTileItems / 4];  // the tile, parked over the lookback
 
     PartState* cur;
-    const uint32_t tile = lookback_begin(&ctrl->part, states, cap_tiles, cur);
+    const uint32_t tile = lookback_begin(a.lb, a.states, a.cap_tiles, cur);
+    const float* w = a.w;
+    uint32_t n = a.n, first = 0;
+    BuildCtrl* ctrl = a.ctrl;
+    uint32_t* idx_out = a.idx;
+    float* prefix_out = a.prefix;
+    float* elems_out = a.elems;
+    float* prefix_lo_out = a.prefix_lo;
+    if constexpr (BATCH) {
+        const uint32_t d = __ldg(bv.tile_map + tile);
+        const DistDesc* D = bv.dist + d;
+        w = D->w;
+        n = D->n;
+        first = D->tile0;
+        ctrl = bv.dctrl + d;
+        const uint64_t base = D->base;
+        idx_out += base;
+        prefix_out += base;
+        if (elems_out) elems_out += base;
+        if (prefix_lo_out) prefix_lo_out += base;
+    }
+    const uint32_t lt = tile - first;
     const float pivot = ctrl->mean;
+    const int grid = COMP ? fx_grid(ctrl->total) : 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t tbase = tile * kTileItems;
-    const uint32_t wbase = tbase + warp * kWarpItems;
+    const uint32_t tbase = lt * kTileItems;
 
     float x[4][4];
-    const bool full = (static_cast<uint64_t>(tbase) + kTileItems <= n) &&
-                      ((reinterpret_cast<uintptr_t>(w) & 15u) == 0);
-    if (full) {
+    load_tile(w, n, lt, x);
+
+    // ---- phase A: thread and warp totals of the heavy / light classes
+    {
+        uint32_t tc = 0;
+        float th = 0.f, tl = 0.f;
+        ff fh{0.f, 0.f}, fl{0.f, 0.f};
+        u128 xh = 0, xl = 0;
 #pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            float4 q = __ldcs(reinterpret_cast<const float4*>(w + wbase + v * 128 + lane * 4));
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float xv = x[v][c];
+                if (xv > pivot) {
+                    ++tc;
+                    if constexpr (COMP) xh += fx_from_float(xv, grid);
+                    if constexpr (FFOUT)
+                        fh = ff_add_f(fh, xv);
+                    else
+                        th = __fadd_rn(th, xv);
+                } else {
+                    if constexpr (COMP) xl += fx_from_float(xv, grid);
+                    if constexpr (FFOUT)
+                        fl = ff_add_f(fl, xv);
+                    else
+                        tl = __fadd_rn(tl, xv);
+                }
+            }
+#pragma unroll
+        for (int m = 1; m < 32; m <<= 1) {
+            tc += __shfl_xor_sync(0xffffffffu, tc, m);
+            if constexpr (!FFOUT) {
+                th = __fadd_rn(th, __shfl_xor_sync(0xffffffffu, th, m));
+                tl = __fadd_rn(tl, __shfl_xor_sync(0xffffffffu, tl, m));
+            }
+            if constexpr (COMP) {
+                xh += shfl_xor_u128(xh, m);
+                xl += shfl_xor_u128(xl, m);
+            }
+        }
+        if constexpr (FFOUT) {
+            fh = ff_warp_total(fh);
+            fl = ff_warp_total(fl);
+        }
+        // park the items in shared memory: registers stay free for the lookback
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+            s_x[(warp * kWarpItems + v * 128 + lane * 4) / 4] =
+                make_float4(x[v][0], x[v][1], x[v][2], x[v][3]);
+        if (lane == 0) {
+            s_wc[warp] = tc;
+            if constexpr (FFOUT) {
+                s_fh[warp] = fh;
+                s_fl[warp] = fl;
+            } else {
+                s_wh[warp] = th;
+                s_wl[warp] = tl;
+            }
+            if constexpr (COMP) {
+                s_xh[warp] = xh;
+                s_xl[warp] = xl;
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- phase B (warp 0): warp-exclusive offsets, tile aggregate, lookback
+    if (warp == 0) {
+        const uint32_t ic = warp_incl_u(lane < kTileWarps ? s_wc[lane] : 0u, lane);
+        const uint32_t ec = __shfl_up_sync(0xffffffffu, ic, 1);
+        const uint32_t agg_c = __shfl_sync(0xffffffffu, ic, kTileWarps - 1);
+        float eh = 0.f, el = 0.f, agg_h = 0.f, agg_l = 0.f;
+        ff fxh{0.f, 0.f}, fxl{0.f, 0.f};
+        if constexpr (FFOUT) {
+            const ff ith = ff_warp_incl(lane < kTileWarps ? s_fh[lane] : ff{0.f, 0.f}, lane);
+            const ff itl = ff_warp_incl(lane < kTileWarps ? s_fl[lane] : ff{0.f, 0.f}, lane);
+            fxh = ff_shfl_up_excl(ith, lane);
+            fxl = ff_shfl_up_excl(itl, lane);
+        } else {
+            const float ih = warp_incl_f(lane < kTileWarps ? s_wh[lane] : 0.f, lane);
+            const float il = warp_incl_f(lane < kTileWarps ? s_wl[lane] : 0.f, lane);
+            eh = __shfl_up_sync(0xffffffffu, ih, 1);
+            el = __shfl_up_sync(0xffffffffu, il, 1);
+            agg_h = __shfl_sync(0xffffffffu, ih, kTileWarps - 1);
+            agg_l = __shfl_sync(0xffffffffu, il, kTileWarps - 1);
+        }
+        __syncwarp();
+        if (lane < kTileWarps) {
+            s_wc[lane] = lane ? ec : 0u;
+            if constexpr (FFOUT) {
+                s_fh[lane] = fxh;
+                s_fl[lane] = fxl;
+            } else {
+                s_wh[lane] = lane ? eh : 0.f;
+                s_wl[lane] = lane ? el : 0.f;
+            }
+        }
+        ff exh{0.f, 0.f}, exl{0.f, 0.f};
+        uint32_t exc = 0;
+        if constexpr (COMP) {
+            PartX agg{0, 0, agg_c};
+#pragma unroll
+            for (int k = 0; k < kTileWarps; ++k) {
+                agg.h += s_xh[k];
+                agg.l += s_xl[k];
+            }
+            PartX ex{0, 0, 0u};
+            if (tile == first) {
+                if (lane == 0) {
+                    part_publish_x(cur + tile, agg, false);
+                    part_publish_x(cur + tile, agg, true);
+                }
+            } else {
+                if (lane == 0) part_publish_x(cur + tile, agg, false);
+                ex = part_lookback_x(cur, tile, first, a.status, a.spin_limit);
+                if (lane == 0)
+                    part_publish_x(cur + tile, PartX{ex.h + agg.h, ex.l + agg.l, ex.c + agg.c}, true);
+            }
+            if (lane == 0) {
+                exh = fx_to_ff(ex.h, grid);
+                exl = fx_to_ff(ex.l, grid);
+            }
+            exc = ex.c;
+        } else {
+            const PartCarry agg{agg_h, agg_l, agg_c};
+            PartCarry ex{0.f, 0.f, 0u};
+            if (tile == first) {
+                if (lane == 0) {
+                    part_publish_f(cur + tile, agg, false);
+                    part_publish_f(cur + tile, agg, true);
+                }
+            } else {
+                if (lane == 0) part_publish_f(cur + tile, agg, false);
+                ex = part_lookback_f(cur, tile, first, a.status, a.spin_limit);
+                if (lane == 0)
+                    part_publish_f(cur + tile,
+                                   PartCarry{__fadd_rn(ex.h, agg.h), __fadd_rn(ex.l, agg.l),
+                                             ex.c + agg.c},
+                                   true);
+            }
+            exh = {ex.h, 0.f};
+            exl = {ex.l, 0.f};
+            exc = ex.c;
+        }
+        if (lane == 0) {
+            s_exh = exh;
+            s_exl = exl;
+            s_exc = exc;
+            s_aggc = agg_c;
+        }
+    }
+    __syncthreads();
+
+    // ---- phase C: local scans in item order, scatter (items back from shared memory)
+    const ff ex_h = s_exh, ex_l = s_exl;
+    const uint32_t ex_c = s_exc;
+    const uint32_t light_before = tbase - ex_c;  // light items in tiles before this one
+    uint32_t oc = s_wc[warp];                    // heavy items of the tile before group v
+    float oh32 = 0.f, ol32 = 0.f;                // running local sums before group v
+    ff oh{0.f, 0.f}, ol{0.f, 0.f};
+    if constexpr (FFOUT) {
+        oh = s_fh[warp];
+        ol = s_fl[warp];
+    } else {
+        oh32 = s_wh[warp];
+        ol32 = s_wl[warp];
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        {
+            const float4 q = s_x[(warp * kWarpItems + v * 128 + lane * 4) / 4];
             x[v][0] = q.x;
             x[v][1] = q.y;
             x[v][2] = q.z;
             x[v][3] = q.w;
         }
-    } else {
-#pragma unroll
-        for (int v = 0; v < 4; ++v)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                uint32_t e = wbase + v * 128 + lane * 4 + c;
-                x[v][c] = e < n ? __ldg(w + e) : 0.0f;  // out of range: light, weight 0
-            }
-    }
-
-    // per-v warp scans of the thread totals
-    float lex_h[4], lex_l[4], voff_h[4], voff_l[4];
-    uint32_t lex_c[4], voff_c[4];
-    float run_h = 0.f, run_l = 0.f;
-    uint32_t run_c = 0;
-    // FFOUT: the tile aggregate is also summed exactly (float-float), so that its FP32
-    // rounding does not accumulate along the lookback carry
-    ff fh{0.f, 0.f}, fl{0.f, 0.f};
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-        float th = 0.f, tl = 0.f;
-        uint32_t tc = 0;
+        uint32_t tcv = 0;
+        float thv = 0.f, tlv = 0.f;
+        ff fth{0.f, 0.f}, ftl{0.f, 0.f};
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-            if (x[v][c] > pivot) {
+            const float xv = x[v][c];
+            if (xv > pivot) {
+                ++tcv;
                 if constexpr (FFOUT)
-                    fh = ff_add_f(fh, x[v][c]);
+                    fth = ff_add_f(fth, xv);
                 else
-                    th = __fadd_rn(th, x[v][c]);
-                ++tc;
+                    thv = __fadd_rn(thv, xv);
             } else {
                 if constexpr (FFOUT)
-                    fl = ff_add_f(fl, x[v][c]);
+                    ftl = ff_add_f(ftl, xv);
                 else
-                    tl = __fadd_rn(tl, x[v][c]);
+                    tlv = __fadd_rn(tlv, xv);
             }
         }
-        uint32_t ic = warp_incl_u(tc, lane);
-        uint32_t ec = __shfl_up_sync(0xffffffffu, ic, 1);
-        lex_c[v] = lane ? ec : 0u;
-        voff_c[v] = run_c;
-        run_c += __shfl_sync(0xffffffffu, ic, 31);
-        if constexpr (!FFOUT) {
-            // FP32 local scans (the float-float mode redoes them exactly after the lookback)
-            float ih = warp_incl_f(th, lane), il = warp_incl_f(tl, lane);
-            float eh = __shfl_up_sync(0xffffffffu, ih, 1), el = __shfl_up_sync(0xffffffffu, il, 1);
-            lex_h[v] = lane ? eh : 0.f;
-            lex_l[v] = lane ? el : 0.f;
-            voff_h[v] = run_h;
-            voff_l[v] = run_l;
-            run_h = __fadd_rn(run_h, __shfl_sync(0xffffffffu, ih, 31));
-            run_l = __fadd_rn(run_l, __shfl_sync(0xffffffffu, il, 31));
-        }
-    }
-    if constexpr (FFOUT) {
-        fh = ff_warp_total(fh);
-        fl = ff_warp_total(fl);
-    }
-    if (lane == 0) {
-        s_wh[warp] = run_h;
-        s_wl[warp] = run_l;
-        s_wc[warp] = run_c;
-        if constexpr (FFOUT) {
-            s_fh[warp] = fh;
-            s_fl[warp] = fl;
-        }
-    }
-    __syncthreads();
-    if (warp == 0) {
-        float th = lane < kTileWarps ? s_wh[lane] : 0.f;
-        float tl = lane < kTileWarps ? s_wl[lane] : 0.f;
-        uint32_t tc = lane < kTileWarps ? s_wc[lane] : 0u;
-        float ih = warp_incl_f(th, lane), il = warp_incl_f(tl, lane);
-        uint32_t ic = warp_incl_u(tc, lane);
-        float eh = __shfl_up_sync(0xffffffffu, ih, 1), el = __shfl_up_sync(0xffffffffu, il, 1);
-        uint32_t ec = __shfl_up_sync(0xffffffffu, ic, 1);
-        PartCarry agg{{__shfl_sync(0xffffffffu, ih, kTileWarps - 1), 0.f},
-                      {__shfl_sync(0xffffffffu, il, kTileWarps - 1), 0.f},
-                      __shfl_sync(0xffffffffu, ic, kTileWarps - 1)};
-        ff fxh{0.f, 0.f}, fxl{0.f, 0.f};  // FFOUT: exact warp-exclusive offsets
-        if constexpr (FFOUT) {
-            const ff ith = ff_warp_incl(lane < kTileWarps ? s_fh[lane] : ff{0.f, 0.f}, lane);
-            const ff itl = ff_warp_incl(lane < kTileWarps ? s_fl[lane] : ff{0.f, 0.f}, lane);
-            agg.h = ff_shfl(ith, kTileWarps - 1);
-            agg.l = ff_shfl(itl, kTileWarps - 1);
-            fxh = ff_shfl_up_excl(ith, lane);
-            fxl = ff_shfl_up_excl(itl, lane);
-        }
-        __syncwarp();
-        if (lane < kTileWarps) {
-            s_wh[lane] = lane ? eh : 0.f;
-            s_wl[lane] = lane ? el : 0.f;
-            s_wc[lane] = lane ? ec : 0u;
-            if constexpr (FFOUT) {
-                s_fh[lane] = fxh;
-                s_fl[lane] = fxl;
-            }
-        }
-        PartCarry ex{{0.f, 0.f}, {0.f, 0.f}, 0u};
-        if (tile == 0) {
-            if (lane == 0) {
-                part_publish_agg(cur, agg);
-                part_publish_pre(cur, agg);
-            }
-        } else {
-            if (lane == 0) part_publish_agg(cur + tile, agg);
-            ex = part_lookback<COMP>(cur, tile, &ctrl->status, spin_limit);
-            if (lane == 0) part_publish_pre(cur + tile, part_add<COMP>(ex, agg));
-        }
-        if (lane == 0) {
-            s_ex = ex;
-            s_agg = agg;
-        }
-    }
-    __syncthreads();
-
-    const PartCarry ex = s_ex;
-    const uint32_t light_before = tbase - ex.c;  // light items in tiles before this one
-    const float wh = s_wh[warp], wl = s_wl[warp];
-    const uint32_t wc = s_wc[warp];
-    // FFOUT: float-float running offsets (warp-exclusive, then per-v warp totals)
-    ff oh{0.f, 0.f}, ol{0.f, 0.f};
-    if constexpr (FFOUT) {
-        oh = s_fh[warp];
-        ol = s_fl[warp];
-    }
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
+        const uint32_t icv = warp_incl_u(tcv, lane);
+        const uint32_t ecv = __shfl_up_sync(0xffffffffu, icv, 1);
+        uint32_t rc = oc + (lane ? ecv : 0u);  // heavy items of the tile before this thread's
+        oc += __shfl_sync(0xffffffffu, icv, 31);
         float rh = 0.f, rl = 0.f;
         ff fr_h{0.f, 0.f}, fr_l{0.f, 0.f};
         if constexpr (FFOUT) {
-            // exact local scan: thread totals, float-float warp scan, running offsets
-            ff th{0.f, 0.f}, tl{0.f, 0.f};
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                if (x[v][c] > pivot)
-                    th = ff_add_f(th, x[v][c]);
-                else
-                    tl = ff_add_f(tl, x[v][c]);
-            }
-            const ff ih = ff_warp_incl(th, lane), il = ff_warp_incl(tl, lane);
+            const ff ih = ff_warp_incl(fth, lane), il = ff_warp_incl(ftl, lane);
             fr_h = carry_add<true>(oh, ff_shfl_up_excl(ih, lane));
             fr_l = carry_add<true>(ol, ff_shfl_up_excl(il, lane));
             oh = carry_add<true>(oh, ff_shfl(ih, 31));
             ol = carry_add<true>(ol, ff_shfl(il, 31));
         } else {
-            rh = __fadd_rn(__fadd_rn(wh, voff_h[v]), lex_h[v]);
-            rl = __fadd_rn(__fadd_rn(wl, voff_l[v]), lex_l[v]);
+            const float ih = warp_incl_f(thv, lane), il = warp_incl_f(tlv, lane);
+            const float eh = __shfl_up_sync(0xffffffffu, ih, 1);
+            const float el = __shfl_up_sync(0xffffffffu, il, 1);
+            rh = lane ? __fadd_rn(oh32, eh) : oh32;
+            rl = lane ? __fadd_rn(ol32, el) : ol32;
+            oh32 = __fadd_rn(oh32, __shfl_sync(0xffffffffu, ih, 31));
+            ol32 = __fadd_rn(ol32, __shfl_sync(0xffffffffu, il, 31));
         }
-        uint32_t rc = wc + voff_c[v] + lex_c[v];  // heavy items before this one in the tile
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             const uint32_t local = warp * kWarpItems + v * 128 + lane * 4 + c;
@@ -450,23 +627,23 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
                 uint32_t pos;
                 ff val;
                 if (xv > pivot) {
-                    pos = ex.c + rc;
+                    pos = ex_c + rc;
                     if constexpr (FFOUT) {
                         fr_h = ff_add_f(fr_h, xv);
-                        val = carry_add<true>(ex.h, fr_h);
+                        val = carry_add<true>(ex_h, fr_h);
                     } else {
                         rh = __fadd_rn(rh, xv);
-                        val = {carry_apply<COMP>(ex.h, rh), 0.f};
+                        val = {carry_apply<COMP>(ex_h, rh), 0.f};
                     }
                     ++rc;
                 } else {
                     pos = n - 1u - (light_before + (local - rc));
                     if constexpr (FFOUT) {
                         fr_l = ff_add_f(fr_l, xv);
-                        val = carry_add<true>(ex.l, fr_l);
+                        val = carry_add<true>(ex_l, fr_l);
                     } else {
                         rl = __fadd_rn(rl, xv);
-                        val = {carry_apply<COMP>(ex.l, rl), 0.f};
+                        val = {carry_apply<COMP>(ex_l, rl), 0.f};
                     }
                 }
                 if (pos < n) {  // always true unless a lookback wait gave up
@@ -478,25 +655,29 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(
             }
         }
     }
-    if (threadIdx.x == 0 && tile == (n - 1u) / kTileItems) ctrl->heavy_count = ex.c + s_agg.c;
-    lookback_end(&ctrl->part);
+    if (threadIdx.x == 0 && lt == tiles_for(n) - 1u) ctrl->heavy_count = ex_c + s_aggc;
+    lookback_end(a.lb);
+}
+
+template <bool BATCH>
+static void part_dispatch(cudaStream_t st, uint32_t precision, uint32_t grid, const PartArgs& a,
+                          const BatchView& bv) {
+    if (precision == 2)
+        k_prefix_partition<true, true, BATCH><<<grid, kTileThreads, 0, st>>>(a, bv);
+    else if (precision == 1)
+        k_prefix_partition<true, false, BATCH><<<grid, kTileThreads, 0, st>>>(a, bv);
+    else
+        k_prefix_partition<false, false, BATCH><<<grid, kTileThreads, 0, st>>>(a, bv);
 }
 
 cudaError_t launch_prefix_partition(cudaStream_t st, bool comp, const float* w, uint32_t n,
                                     BuildCtrl* ctrl, PartState* states, uint32_t cap_tiles,
                                     uint32_t* idx_out, float* prefix_out, float* elems_out,
                                     float* prefix_lo_out) {
-    const uint32_t tiles = tiles_for(n);
-    if (prefix_lo_out)
-        k_prefix_partition<true, true><<<tiles, kTileThreads, 0, st>>>(
-            w, n, ctrl, states, cap_tiles, idx_out, prefix_out, elems_out, prefix_lo_out,
-            kSpinLimit);
-    else if (comp)
-        k_prefix_partition<true, false><<<tiles, kTileThreads, 0, st>>>(
-            w, n, ctrl, states, cap_tiles, idx_out, prefix_out, elems_out, nullptr, kSpinLimit);
-    else
-        k_prefix_partition<false, false><<<tiles, kTileThreads, 0, st>>>(
-            w, n, ctrl, states, cap_tiles, idx_out, prefix_out, elems_out, nullptr, kSpinLimit);
+    const PartArgs a{w,         n,           ctrl,          &ctrl->part, states,   cap_tiles,
+                     kSpinLimit, &ctrl->status, idx_out,  prefix_out, elems_out, prefix_lo_out};
+    const uint32_t precision = prefix_lo_out ? 2u : (comp ? 1u : 0u);
+    part_dispatch<false>(st, precision, tiles_for(n), a, BatchView{});
     return cudaGetLastError();
 }
 
@@ -513,50 +694,24 @@ __device__ __forceinline__ ff ff_warp_sum(ff v) {
 
 template <bool COMP>
 __device__ ff scan_lookback(const ScanState* st, uint32_t tile, uint32_t* status,
-                             uint32_t spin_limit) {
-    const int lane = threadIdx.x & 31;
-    ff ex{0.f, 0.f};
-    int64_t base = static_cast<int64_t>(tile) - 1;
-    uint32_t spins = 0;
-    for (;;) {
-        const int64_t pos = base - lane;
-        int s = 2;
-        ff v{0.f, 0.f};
-        if (pos >= 0) {
+                            uint32_t spin_limit) {
+    return lookback_walk(
+        tile, 0u, status, spin_limit, ff{0.f, 0.f},
+        [st](uint32_t pos, ff& v) -> int {
             unsigned long long a, p;
             ld_relaxed_v2(reinterpret_cast<const unsigned long long*>(st + pos), a, p);
             if (ff_ready(p)) {
-                s = 2;
                 v = unpack_ff(p);
-            } else if (ff_ready(a)) {
-                s = 1;
+                return 2;
+            }
+            if (ff_ready(a)) {
                 v = unpack_ff(a);
-            } else {
-                s = 0;
+                return 1;
             }
-        }
-        const unsigned nr = __ballot_sync(0xffffffffu, s == 0);
-        const unsigned dn = __ballot_sync(0xffffffffu, s == 2);
-        const int first_nr = nr ? __ffs(nr) - 1 : 32;
-        const int first_dn = dn ? __ffs(dn) - 1 : 32;
-        const bool finish = first_dn < first_nr;
-        const int take = finish ? first_dn + 1 : first_nr;
-        if (take > 0) {
-            ff c = lane < take ? v : ff{0.f, 0.f};
-            ex = carry_add<COMP>(ex, ff_warp_sum<COMP>(c));
-            base -= take;
-            spins = 0;
-        }
-        if (finish) break;
-        if (take == 0) {
-            if (++spins >= spin_limit) {
-                if (lane == 0) atomicOr(status, kStatusTimeout);
-                break;
-            }
-            backoff(spins);
-        }
-    }
-    return ex;
+            return 0;
+        },
+        [](ff v) { return ff_warp_sum<COMP>(v); },
+        [](ff a, ff b) { return carry_add<COMP>(a, b); });
 }
 
 template <bool COMP>
@@ -576,24 +731,7 @@ __global__ __launch_bounds__(kTileThreads) void k_scan(const float* __restrict__
                       ((reinterpret_cast<uintptr_t>(in) & 15u) == 0) &&
                       ((reinterpret_cast<uintptr_t>(out) & 15u) == 0);
     float x[4][4];
-    if (full) {
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            float4 q = __ldcs(reinterpret_cast<const float4*>(in + wbase + v * 128 + lane * 4));
-            x[v][0] = q.x;
-            x[v][1] = q.y;
-            x[v][2] = q.z;
-            x[v][3] = q.w;
-        }
-    } else {
-#pragma unroll
-        for (int v = 0; v < 4; ++v)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                uint32_t e = wbase + v * 128 + lane * 4 + c;
-                x[v][c] = e < n ? __ldg(in + e) : 0.0f;
-            }
-    }
+    load_tile(in, n, tile, x);
     float lex[4], voff[4], run = 0.f;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
@@ -833,39 +971,71 @@ __device__ void pack(const PackIn& c, uint2* __restrict__ table, uint32_t i0, ui
     }
 }
 
+struct SplitArgs {
+    const float* w;  // single distribution: weights, n, control block, table
+    uint32_t n;
+    const BuildCtrl* ctrl;
+    uint2* table;
+    const uint32_t* idx;  // partition arrays (a batch adds each distribution's base)
+    const float* elems;
+    const float* prefix;
+    const float* prefix_lo;
+    uint32_t* status;
+    uint32_t split_size;
+    uint32_t full_light;
+};
+
 // Thread t of CTA b computes split k = b*kSplitPack + t (k in [0, K]) and packs subproblem
 // k = [split_k, split_{k+1}) for t < kSplitPack, k < K; split_{k+1} comes from the
 // neighbouring thread through shared memory (shader.comp:225-270).  The last
 // kSplitLook + 1 threads only compute look-ahead splits for the ownership window.
-constexpr int kSplitPack = kSplitThreads - kSplitLook - 1;
-
-template <bool R64, bool FF>
-__global__ __launch_bounds__(kSplitThreads) void k_split_pack(
-    const float* __restrict__ w, const uint32_t* __restrict__ idx,
-    const float* __restrict__ elems, const float* __restrict__ prefix,
-    const float* __restrict__ prefix_lo, const BuildCtrl* __restrict__ ctrl, uint32_t* status,
-    uint32_t n, uint32_t K, uint32_t split_size, uint32_t full_light,
-    uint2* __restrict__ table) {
+template <bool R64, bool FF, bool BATCH>
+__global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, BatchView bv) {
     __shared__ uint32_t s_i[kSplitThreads], s_j[kSplitThreads];
     __shared__ float s_spill[kSplitThreads];
+    const float* w = a.w;
+    uint32_t n = a.n;
+    const BuildCtrl* ctrl = a.ctrl;
+    uint2* table = a.table;
+    const uint32_t* idx = a.idx;
+    const float* elems = a.elems;
+    const float* prefix = a.prefix;
+    const float* prefix_lo = a.prefix_lo;
+    uint32_t blk = blockIdx.x, nblk = gridDim.x;
+    if constexpr (BATCH) {
+        const uint32_t d = __ldg(bv.split_map + blockIdx.x);
+        const DistDesc* D = bv.dist + d;
+        w = D->w;
+        n = D->n;
+        ctrl = bv.dctrl + d;
+        table = D->table;
+        const uint64_t base = D->base;
+        idx += base;
+        if (elems) elems += base;
+        prefix += base;
+        if (prefix_lo) prefix_lo += base;
+        blk -= D->split0;
+        nblk = split_blocks_for(n, a.split_size);
+    }
+    const uint32_t K = splits_for(n, a.split_size);
     const uint32_t hc = ctrl->heavy_count;
     if (hc == 0u || hc >= n) {
         // degenerate (all items light or all heavy): every bucket keeps itself
-        const uint32_t nth = gridDim.x * blockDim.x;
-        for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += nth)
+        const uint32_t nth = nblk * blockDim.x;
+        for (uint32_t e = blk * blockDim.x + threadIdx.x; e < n; e += nth)
             table[e] = make_uint2(__float_as_uint(1.0f), e);
         return;
     }
     PackIn c{w,      idx,    elems,  prefix, prefix_lo, n, hc,
-             n - hc, full_light ? n - hc : n - hc - 1u, ctrl->mean, ctrl->mean_lo};
-    const uint32_t k = blockIdx.x * kSplitPack + threadIdx.x;
+             n - hc, a.full_light ? n - hc : n - hc - 1u, ctrl->mean, ctrl->mean_lo};
+    const uint32_t k = blk * kSplitPack + threadIdx.x;
     uint32_t si = c.lc, sj = hc;  // past split K: the final split
     float sp = 0.f;
     if (k == 0u) {
         si = 0;
         sj = 0;
     } else if (k < K) {
-        compute_split<R64, FF>(c, k * split_size, si, sj, sp);
+        compute_split<R64, FF>(c, k * a.split_size, si, sj, sp);
     }
     s_i[threadIdx.x] = si;
     s_j[threadIdx.x] = sj;
@@ -880,27 +1050,77 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(
         clean = clean && s_i[t + d] >= i1 && s_j[t + d] >= j1;
     // a step back reaching past the window cannot be resolved here: report it
     if (k + kSplitLook + 1u < K && (s_i[t + kSplitLook + 1] < i1 || s_j[t + kSplitLook + 1] < j1))
-        atomicOr(status, kStatusNonMonotone);
+        atomicOr(a.status, kStatusNonMonotone);
     const LaterSplits later{s_i, s_j, t, count};
     pack(c, table, si, i1, sj, j1, sp, clean ? nullptr : &later);
+}
+
+template <bool BATCH>
+static void split_dispatch(cudaStream_t st, bool r64, bool ff, uint32_t grid, const SplitArgs& a,
+                           const BatchView& bv) {
+    if (ff)
+        k_split_pack<true, true, BATCH><<<grid, kSplitThreads, 0, st>>>(a, bv);
+    else if (r64)
+        k_split_pack<true, false, BATCH><<<grid, kSplitThreads, 0, st>>>(a, bv);
+    else
+        k_split_pack<false, false, BATCH><<<grid, kSplitThreads, 0, st>>>(a, bv);
 }
 
 cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const float* w,
                               const uint32_t* idx, const float* elems, const float* prefix,
                               const float* prefix_lo, const BuildCtrl* ctrl, uint32_t* status,
                               uint32_t n, uint32_t split_size, uint2* table) {
-    uint32_t K = n / split_size;
-    if (K == 0) K = 1;
-    const uint32_t blocks = (K + kSplitPack - 1) / kSplitPack;
-    if (prefix_lo)
-        k_split_pack<true, true><<<blocks, kSplitThreads, 0, st>>>(
-            w, idx, elems, prefix, prefix_lo, ctrl, status, n, K, split_size, full_light, table);
-    else if (r64)
-        k_split_pack<true, false><<<blocks, kSplitThreads, 0, st>>>(
-            w, idx, elems, prefix, nullptr, ctrl, status, n, K, split_size, full_light, table);
-    else
-        k_split_pack<false, false><<<blocks, kSplitThreads, 0, st>>>(
-            w, idx, elems, prefix, nullptr, ctrl, status, n, K, split_size, full_light, table);
+    const SplitArgs a{w,      n,         ctrl,   table,      idx,
+                      elems,  prefix,    prefix_lo, status,  split_size,
+                      full_light ? 1u : 0u};
+    split_dispatch<false>(st, r64, prefix_lo != nullptr, split_blocks_for(n, split_size), a,
+                          BatchView{});
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------
+// batches
+// ---------------------------------------------------------------------------------
+
+// One CTA per distribution fills its ranges of the tile, split-block and sampling-block maps.
+__global__ __launch_bounds__(256) void k_batch_maps(const DistDesc* __restrict__ dist,
+                                                    uint32_t* __restrict__ tile_map,
+                                                    uint32_t* __restrict__ split_map,
+                                                    uint32_t* __restrict__ sample_map,
+                                                    uint32_t split_size) {
+    const uint32_t d = blockIdx.x;
+    const DistDesc D = dist[d];
+    if (D.w) {
+        const uint32_t nt = tiles_for(D.n);
+        for (uint32_t i = threadIdx.x; i < nt; i += blockDim.x) tile_map[D.tile0 + i] = d;
+        const uint32_t ns = split_blocks_for(D.n, split_size);
+        for (uint32_t i = threadIdx.x; i < ns; i += blockDim.x) split_map[D.split0 + i] = d;
+    }
+    if (D.out) {
+        const uint64_t nb = alias_blocks_for(D.s);
+        for (uint64_t i = threadIdx.x; i < nb; i += blockDim.x) sample_map[D.sample0 + i] = d;
+    }
+}
+
+cudaError_t launch_batch_maps(cudaStream_t st, const DistDesc* dist, uint32_t count,
+                              uint32_t* tile_map, uint32_t* split_map, uint32_t* sample_map,
+                              uint32_t split_size) {
+    if (count == 0) return cudaSuccess;
+    k_batch_maps<<<count, 256, 0, st>>>(dist, tile_map, split_map, sample_map, split_size);
+    return cudaGetLastError();
+}
+
+// total mass -> prefix-partition -> split+pack over every distribution of the batch that
+// has weights: three launches, whatever the number and sizes of the distributions.
+cudaError_t launch_batch_build(cudaStream_t st, uint32_t precision, bool r64, const BatchView& b) {
+    if (b.tiles == 0) return cudaSuccess;
+    k_total_mass<true><<<b.tiles, kTileThreads, 0, st>>>(nullptr, 0u, b.partials, nullptr, b);
+    const PartArgs pa{nullptr,    0u,       nullptr,  b.lb,   b.states,  b.cap_tiles,
+                      kSpinLimit, b.status, b.idx,    b.prefix, b.elems, b.prefix_lo};
+    part_dispatch<true>(st, precision, b.tiles, pa, b);
+    const SplitArgs sa{nullptr, 0u,       nullptr,     nullptr,  b.idx,        b.elems,
+                       b.prefix, b.prefix_lo, b.status, b.split_size, b.full_light};
+    split_dispatch<true>(st, r64, precision == 2, b.split_blocks, sa, b);
     return cudaGetLastError();
 }
 

@@ -7,6 +7,8 @@
 //                 (PSA::run, src/device/wrs/alias/psa/PSA.hpp:170-237)
 //   ITS build   : k_scan (ITS::build, src/device/wrs/its/ITS.hpp:90-108)
 //   sample      : k_alias_sample | k_its_sample (WRS::sample, src/device/wrs/WRS.hpp:145-168)
+//   batch       : k_batch_maps (wrs_batch_set), then the same three build kernels and the
+//                 alias sampler over all distributions of a batch, one launch each
 // Stream order replaces the reference's pipeline barriers.
 #include <cstdio>
 #include <cstring>
@@ -80,7 +82,7 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
         return at;
     };
     L.ctrl = take(sizeof(BuildCtrl));
-    L.partials = take(sizeof(double) * kMassMaxBlocks);
+    L.partials = take(sizeof(double) * static_cast<size_t>(cap_tiles));
     const bool alias = cfg.method == WRS_METHOD_ALIAS_TABLE;
     L.part_states = alias ? take(sizeof(PartState) * 2 * static_cast<size_t>(cap_tiles)) : 0;
     L.scan_states = take(sizeof(ScanState) * 2 * static_cast<size_t>(cap_tiles));
@@ -451,3 +453,275 @@ const uint32_t* wrs_buffers_heavy_count(const wrs_buffers* b) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// batches
+// ---------------------------------------------------------------------------------
+
+struct wrs_batch {
+    wrs_config cfg;
+    uint32_t max_dists = 0;
+    uint64_t max_weights = 0, max_samples = 0;
+    uint32_t cap_tiles = 0, cap_split = 0, cap_sample = 0;
+    void* base = nullptr;
+    size_t bytes = 0;
+    BuildCtrl* bctrl = nullptr;  // batch tickets (part) and status
+    DistDesc* staging = nullptr; // pinned host copy of the descriptors
+    cudaEvent_t staged = nullptr;
+    bool staged_pending = false;
+    BatchView view{};
+    uint32_t count = 0;
+};
+
+namespace {
+
+struct BatchCaps {
+    uint32_t tiles, split, sample;
+};
+
+bool batch_caps(const wrs_config& cfg, uint32_t max_dists, uint64_t max_weights,
+                uint64_t max_samples, BatchCaps& c) {
+    const uint64_t tiles = max_weights / kTileItems + max_dists + 1;
+    const uint64_t split = max_weights / (static_cast<uint64_t>(cfg.split_size) * kSplitPack) +
+                           max_dists + 1;
+    const uint64_t sample = max_samples / kAliasPerBlock + max_dists + 1;
+    if (tiles > 0x7fffffffull || split > 0x7fffffffull || sample > 0x7fffffffull) return false;
+    c = {static_cast<uint32_t>(tiles), static_cast<uint32_t>(split),
+         static_cast<uint32_t>(sample)};
+    return true;
+}
+
+struct BatchLayout {
+    size_t bctrl, dctrl, states, dist, partials, tile_map, split_map, sample_map, idx, prefix,
+        elems, prefix_lo, zero_end, total;
+};
+
+BatchLayout batch_layout(const wrs_config& cfg, uint32_t max_dists, uint64_t max_weights,
+                         const BatchCaps& c) {
+    BatchLayout L{};
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = off;
+        off = align_up(off + bytes, 256);
+        return at;
+    };
+    L.bctrl = take(sizeof(BuildCtrl));
+    L.dctrl = take(sizeof(BuildCtrl) * static_cast<size_t>(max_dists));
+    L.states = take(sizeof(PartState) * 2 * static_cast<size_t>(c.tiles));
+    L.zero_end = off;
+    L.dist = take(sizeof(DistDesc) * static_cast<size_t>(max_dists));
+    L.partials = take(sizeof(double) * static_cast<size_t>(c.tiles));
+    L.tile_map = take(sizeof(uint32_t) * static_cast<size_t>(c.tiles));
+    L.split_map = take(sizeof(uint32_t) * static_cast<size_t>(c.split));
+    L.sample_map = take(sizeof(uint32_t) * static_cast<size_t>(c.sample));
+    L.idx = take(sizeof(uint32_t) * max_weights);
+    L.prefix = take(sizeof(float) * max_weights);
+    L.elems = cfg.use_partition_elements ? take(sizeof(float) * max_weights) : 0;
+    L.prefix_lo = cfg.scan_precision == WRS_SCAN_FLOAT_FLOAT ? take(sizeof(float) * max_weights) : 0;
+    L.total = off;
+    return L;
+}
+
+wrs_status check_batch_handle(const wrs_handle* h, const wrs_batch* b) {
+    if (!h || !b) return fail(WRS_ERR_INVALID_ARG, "handle or batch is NULL");
+    if (h->cfg.method != WRS_METHOD_ALIAS_TABLE)
+        return fail(WRS_ERR_NOT_IMPLEMENTED, "batches exist for the alias method only");
+    if (h->cfg.split_size != b->cfg.split_size ||
+        h->cfg.use_partition_elements != b->cfg.use_partition_elements ||
+        h->cfg.scan_precision != b->cfg.scan_precision)
+        return fail(WRS_ERR_INVALID_ARG,
+                    "the batch was created for another split size, element or precision setting");
+    return WRS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t wrs_batch_bytes(const wrs_handle* h, uint32_t max_dists, uint64_t max_weights,
+                       uint64_t max_samples) {
+    BatchCaps c;
+    if (!h || h->cfg.method != WRS_METHOD_ALIAS_TABLE ||
+        !batch_caps(h->cfg, max_dists, max_weights, max_samples, c))
+        return 0;
+    return batch_layout(h->cfg, max_dists, max_weights, c).total;
+}
+
+wrs_status wrs_batch_create(const wrs_handle* h, uint32_t max_dists, uint64_t max_weights,
+                            uint64_t max_samples, wrs_batch** out) {
+    if (!h || !out) return fail(WRS_ERR_INVALID_ARG, "handle or out is NULL");
+    *out = nullptr;
+    if (h->cfg.method != WRS_METHOD_ALIAS_TABLE)
+        return fail(WRS_ERR_NOT_IMPLEMENTED, "batches exist for the alias method only");
+    if (max_dists == 0 || max_dists > (1u << 24))
+        return fail(WRS_ERR_INVALID_ARG, "max_dists out of range");
+    BatchCaps c;
+    if (!batch_caps(h->cfg, max_dists, max_weights, max_samples, c))
+        return fail(WRS_ERR_INVALID_ARG, "batch capacity out of range");
+    const BatchLayout L = batch_layout(h->cfg, max_dists, max_weights, c);
+    wrs_batch* b = new (std::nothrow) wrs_batch;
+    if (!b) return fail(WRS_ERR_OOM, "host allocation failed");
+    b->cfg = h->cfg;
+    b->max_dists = max_dists;
+    b->max_weights = max_weights;
+    b->max_samples = max_samples;
+    b->cap_tiles = c.tiles;
+    b->cap_split = c.split;
+    b->cap_sample = c.sample;
+    cudaError_t e = cudaMalloc(&b->base, L.total);
+    if (e != cudaSuccess) {
+        delete b;
+        (void)cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? fail(WRS_ERR_OOM, "cudaMalloc failed")
+                                              : cuda_fail(e, "cudaMalloc");
+    }
+    b->bytes = L.total;
+    e = cudaHostAlloc(reinterpret_cast<void**>(&b->staging), sizeof(DistDesc) * max_dists,
+                      cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMemset(b->base, 0, L.zero_end);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        wrs_batch_destroy(b);
+        return cuda_fail(e, "batch setup");
+    }
+    char* p = static_cast<char*>(b->base);
+    b->bctrl = reinterpret_cast<BuildCtrl*>(p + L.bctrl);
+    BatchView& v = b->view;
+    v.dist = reinterpret_cast<const DistDesc*>(p + L.dist);
+    v.tile_map = reinterpret_cast<const uint32_t*>(p + L.tile_map);
+    v.split_map = reinterpret_cast<const uint32_t*>(p + L.split_map);
+    v.sample_map = reinterpret_cast<const uint32_t*>(p + L.sample_map);
+    v.dctrl = reinterpret_cast<BuildCtrl*>(p + L.dctrl);
+    v.lb = &b->bctrl->part;
+    v.status = &b->bctrl->status;
+    v.states = reinterpret_cast<PartState*>(p + L.states);
+    v.partials = reinterpret_cast<double*>(p + L.partials);
+    v.idx = reinterpret_cast<uint32_t*>(p + L.idx);
+    v.prefix = reinterpret_cast<float*>(p + L.prefix);
+    v.elems = h->cfg.use_partition_elements ? reinterpret_cast<float*>(p + L.elems) : nullptr;
+    v.prefix_lo = h->cfg.scan_precision == WRS_SCAN_FLOAT_FLOAT
+                      ? reinterpret_cast<float*>(p + L.prefix_lo)
+                      : nullptr;
+    v.cap_tiles = c.tiles;
+    v.split_size = h->cfg.split_size;
+    v.full_light = h->cfg.split_full_light ? 1u : 0u;
+    *out = b;
+    return WRS_OK;
+}
+
+void wrs_batch_destroy(wrs_batch* b) {
+    if (!b) return;
+    if (b->staged) {
+        cudaEventSynchronize(b->staged);
+        cudaEventDestroy(b->staged);
+    }
+    if (b->staging) cudaFreeHost(b->staging);
+    if (b->base) cudaFree(b->base);
+    delete b;
+}
+
+wrs_status wrs_batch_set(wrs_batch* b, void* stream, const wrs_dist_desc* descs, uint32_t count) {
+    if (!b) return fail(WRS_ERR_INVALID_ARG, "batch is NULL");
+    if (count && !descs) return fail(WRS_ERR_INVALID_ARG, "descs is NULL");
+    if (count > b->max_dists) return fail(WRS_ERR_CAPACITY, "more distributions than max_dists");
+    uint64_t weights = 0, tiles = 0, split = 0, sample = 0, samples = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const wrs_dist_desc& d = descs[i];
+        if (d.n == 0 || d.n > kMaxN) return fail(WRS_ERR_INVALID_ARG, "a distribution's n is out of range");
+        if (!d.table) return fail(WRS_ERR_INVALID_ARG, "a distribution has no table");
+        if (d.s && !d.samples) return fail(WRS_ERR_INVALID_ARG, "s > 0 with samples NULL");
+        if (d.weights) {
+            weights += d.n;
+            tiles += tiles_for(d.n);
+            split += split_blocks_for(d.n, b->cfg.split_size);
+        }
+        if (d.samples) {
+            sample += alias_blocks_for(d.s);
+            samples += d.s;
+        }
+    }
+    if (weights > b->max_weights || tiles > b->cap_tiles || split > b->cap_split)
+        return fail(WRS_ERR_CAPACITY, "the distributions' weights exceed max_weights");
+    if (samples > b->max_samples || sample > b->cap_sample)
+        return fail(WRS_ERR_CAPACITY, "the distributions' samples exceed max_samples");
+    if (b->staged_pending) {
+        WRS_CUDA(cudaEventSynchronize(b->staged), "staging wait");
+        b->staged_pending = false;
+    }
+    uint64_t base = 0;
+    uint32_t t0 = 0, s0 = 0, m0 = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const wrs_dist_desc& d = descs[i];
+        DistDesc& o = b->staging[i];
+        o.w = d.weights;
+        o.table = reinterpret_cast<uint2*>(d.table);
+        o.out = d.samples;
+        o.s = d.samples ? d.s : 0;
+        o.seed = d.seed;
+        o.base = base;
+        o.n = d.n;
+        o.tile0 = t0;
+        o.split0 = s0;
+        o.sample0 = m0;
+        if (d.weights) {
+            base += d.n;
+            t0 += tiles_for(d.n);
+            s0 += split_blocks_for(d.n, b->cfg.split_size);
+        }
+        if (d.samples) m0 += static_cast<uint32_t>(alias_blocks_for(d.s));
+    }
+    const cudaStream_t st = as_stream(stream);
+    BatchView& v = b->view;
+    if (count) {
+        WRS_CUDA(cudaMemcpyAsync(const_cast<DistDesc*>(v.dist), b->staging, sizeof(DistDesc) * count,
+                                 cudaMemcpyHostToDevice, st),
+                 "descriptor upload");
+        WRS_CUDA(cudaEventRecord(b->staged, st), "staging event");
+        b->staged_pending = true;
+        WRS_CUDA(launch_batch_maps(st, v.dist, count, const_cast<uint32_t*>(v.tile_map),
+                                   const_cast<uint32_t*>(v.split_map),
+                                   const_cast<uint32_t*>(v.sample_map), b->cfg.split_size),
+                 "batch maps");
+    }
+    v.tiles = t0;
+    v.split_blocks = s0;
+    v.sample_blocks = m0;
+    b->count = count;
+    return WRS_OK;
+}
+
+wrs_status wrs_batch_build(const wrs_handle* h, void* stream, wrs_batch* b) {
+    wrs_status s = check_batch_handle(h, b);
+    if (s != WRS_OK) return s;
+    WRS_CUDA(launch_batch_build(as_stream(stream), h->cfg.scan_precision,
+                                h->cfg.split_residual_f64 != 0, b->view),
+             "batch build");
+    return WRS_OK;
+}
+
+wrs_status wrs_batch_sample(const wrs_handle* h, void* stream, wrs_batch* b) {
+    wrs_status s = check_batch_handle(h, b);
+    if (s != WRS_OK) return s;
+    WRS_CUDA(launch_batch_alias_sample(as_stream(stream), h->cfg.rng, h->cfg.coop_size, b->view),
+             "batch sample");
+    return WRS_OK;
+}
+
+wrs_status wrs_batch_status(wrs_batch* b, void* stream, uint32_t* device_status) {
+    if (!b) return fail(WRS_ERR_INVALID_ARG, "batch is NULL");
+    const cudaStream_t st = as_stream(stream);
+    WRS_CUDA(cudaStreamSynchronize(st), "stream synchronize");
+    uint32_t v = 0;
+    WRS_CUDA(cudaMemcpy(&v, &b->bctrl->status, sizeof(v), cudaMemcpyDeviceToHost), "status read");
+    if (v) WRS_CUDA(cudaMemset(&b->bctrl->status, 0, sizeof(v)), "status clear");
+    if (device_status) *device_status = v;
+    if (v & kStatusTimeout) return fail(WRS_ERR_TIMEOUT, "a lookback wait gave up");
+    return WRS_OK;
+}
+
+uint32_t wrs_batch_count(const wrs_batch* b) { return b ? b->count : 0u; }
+
+}  // extern "C"
+
+uint32_t* wrs::batch_status_word(wrs_batch* b) { return &b->bctrl->status; }

@@ -107,6 +107,104 @@ __device__ __forceinline__ ff ff_warp_total(ff v) {
 }
 
 // ---------------------------------------------------------------------------
+// Exact fixed-point carries.  A distribution's heavy/light sums are carried through
+// the lookback as unsigned integers k on the grid 2^g, g = E - 123 where the FP64
+// total mass lies in [2^(E-1), 2^E): every weight is at most 2^123 grid units and
+// every sum stays below 2^125.  Integer addition is associative, so a tile's carry
+// does not depend on which predecessors the lookback happened to see (the FP32 and
+// float-float carries do): builds are bit-for-bit reproducible, alone or batched.
+// A weight converts to the grid by truncation (exact for weights above 2^(E-100)).
+// ---------------------------------------------------------------------------
+typedef unsigned __int128 u128;
+
+__device__ __forceinline__ int fx_grid(double total) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(total));
+    const int e = static_cast<int>((b >> 52) & 0x7ffu);
+    if (e == 0) return -149 - 24;    // zero total: every weight is zero
+    if (e == 0x7ff) return 0;        // not finite: results are meaningless, stay defined
+    return (e - 1022) - 123;
+}
+
+__device__ __forceinline__ u128 fx_from_float(float x, int g) {
+    const uint32_t b = __float_as_uint(x);
+    const int e = static_cast<int>((b >> 23) & 0xffu);
+    uint32_t m = b & 0x7fffffu;
+    int ex = -149;
+    if (e) {
+        m |= 0x800000u;
+        ex = e - 150;
+    }
+    int sh = ex - g;
+    if (sh >= 0) return static_cast<u128>(m) << (sh < 103 ? sh : 103);
+    sh = -sh;
+    return sh >= 24 ? static_cast<u128>(0) : static_cast<u128>(m >> sh);
+}
+
+__device__ __forceinline__ u128 shfl_xor_u128(u128 v, int m) {
+    const unsigned long long lo = __shfl_xor_sync(0xffffffffu, static_cast<unsigned long long>(v), m);
+    const unsigned long long hi =
+        __shfl_xor_sync(0xffffffffu, static_cast<unsigned long long>(v >> 64), m);
+    return (static_cast<u128>(hi) << 64) | lo;
+}
+
+// k > 0 rounded to nearest FP32, as the float f = RN(top) with top the leading 64 bits of
+// k (a sticky bit folded into bit 0) and the bit length nb of k: value = f * 2^(nb - 64).
+__device__ __forceinline__ float fx_lead(u128 k, int& nb) {
+    const unsigned long long hi = static_cast<unsigned long long>(k >> 64);
+    const unsigned long long lo = static_cast<unsigned long long>(k);
+    const int lz = hi ? __clzll(static_cast<long long>(hi)) : 64 + __clzll(static_cast<long long>(lo));
+    nb = 128 - lz;
+    const u128 norm = k << lz;
+    const unsigned long long top = static_cast<unsigned long long>(norm >> 64) |
+                                   (static_cast<unsigned long long>(norm) != 0ull ? 1ull : 0ull);
+    return __ull2float_rn(top);
+}
+
+// The grid value f * 2^(nb - 64) of fx_lead as an integer (f has at most 24 significant
+// bits, and is a multiple of 2^40 when nb > 24, so the shifts below are exact).
+__device__ __forceinline__ u128 fx_lead_int(float f, int nb) {
+    if (f >= 18446744073709551616.0f) return static_cast<u128>(1) << nb;  // rounded up to 2^64
+    const unsigned long long fi = __float2ull_rn(f);
+    return nb >= 64 ? static_cast<u128>(fi) << (nb - 64) : static_cast<u128>(fi >> (64 - nb));
+}
+
+// k * 2^g as a float-float pair: hi = RN(k * 2^g), lo = RN((k - hi) * 2^g).  Deterministic
+// (a function of k and g only).
+__device__ __forceinline__ ff fx_to_ff(u128 k, int g) {
+    if (k == 0) return {0.0f, 0.0f};
+    int nb;
+    const float f = fx_lead(k, nb);
+    const u128 kh = fx_lead_int(f, nb);
+    const float hi = ldexpf(f, nb - 64 + g);
+    float lo = 0.0f;
+    if (kh != k) {
+        const bool neg = kh > k;
+        const u128 r = neg ? kh - k : k - kh;
+        int nr;
+        const float fr = fx_lead(r, nr);
+        lo = ldexpf(neg ? -fr : fr, nr - 64 + g);
+    }
+    return {hi, lo};
+}
+
+// Lookback words of a fixed-point value (k < 2^126): two 63-bit limbs, bit 63 of each word
+// is its ready bit.
+constexpr unsigned long long kLimbMask = 0x7fffffffffffffffull;
+constexpr unsigned long long kLimbReady = 0x8000000000000000ull;
+__device__ __forceinline__ unsigned long long fx_word_lo(u128 k) {
+    return (static_cast<unsigned long long>(k) & kLimbMask) | kLimbReady;
+}
+__device__ __forceinline__ unsigned long long fx_word_hi(u128 k) {
+    return (static_cast<unsigned long long>(k >> 63) & kLimbMask) | kLimbReady;
+}
+__device__ __forceinline__ bool fx_ready(unsigned long long lo, unsigned long long hi) {
+    return (lo & hi & kLimbReady) != 0ull;
+}
+__device__ __forceinline__ u128 fx_unpack(unsigned long long lo, unsigned long long hi) {
+    return (static_cast<u128>(hi & kLimbMask) << 63) | (lo & kLimbMask);
+}
+
+// ---------------------------------------------------------------------------
 // lookback words.  An ff word is {hi bits, lo bits | 1}: the LSB of lo's
 // mantissa is the ready bit (the value loses at most one ulp of lo).  A count
 // word is {count, 1}.  State buffers are zero when a build starts.

@@ -7,6 +7,8 @@
 
 #include "wrs_device.cuh"
 
+struct wrs_batch;
+
 namespace wrs {
 
 // Tile geometry of the decoupled-lookback kernels: 256 threads x 16 items.
@@ -15,14 +17,16 @@ constexpr int kTileWarps = kTileThreads / 32;
 constexpr int kTileItems = 4096;
 constexpr int kWarpItems = kTileItems / kTileWarps;  // 512 contiguous items per warp
 
-// Total-mass reduction grid cap (152 SMs x 8); also the size of the partials array.
-constexpr int kMassThreads = 256;
-constexpr int kMassMaxBlocks = 152 * 8;
-
 // Split+pack: one thread per split; kSplitThreads - kSplitLook - 1 subproblems packed per CTA,
 // the remaining threads compute look-ahead splits (see k_split_pack).
 constexpr int kSplitThreads = 512;
 constexpr int kSplitLook = 32;
+constexpr int kSplitPack = kSplitThreads - kSplitLook - 1;
+
+// Alias sampling: 256 threads x 4 samples per CTA.
+constexpr int kSampleThreads = 256;
+constexpr int kAliasPerThread = 4;
+constexpr int kAliasPerBlock = kSampleThreads * kAliasPerThread;
 
 // Ticket / completion / epoch of one lookback kernel kind.  The epoch selects which half
 // of that kernel's double-buffered state array is live in the current launch.
@@ -33,11 +37,11 @@ struct LbCtrl {
     uint32_t pad;
 };
 
-// Per-build control block (device memory, zero-initialised once at allocation).
+// Per-distribution control block (device memory, zero-initialised once at allocation).
 // Every counter below is returned to zero by the last CTA of the kernel that used it,
 // so successive builds (and CUDA-graph replays) need no memset.
 struct alignas(64) BuildCtrl {
-    uint32_t mass_done;  // CTAs finished in the total-mass reduction
+    uint32_t mass_done;  // tiles finished in the total-mass reduction
     uint32_t status;     // kStatus* bits raised by the device
     uint32_t heavy_count;
     float mean;          // (float)(total / N)
@@ -50,16 +54,55 @@ struct alignas(64) BuildCtrl {
 };
 static_assert(sizeof(BuildCtrl) == 128, "BuildCtrl layout");
 
-// Lookback state of one tile of the prefix-partition (64 B):
-//   q0 = {aggregate heavy sum, aggregate light sum}   (ff words)
-//   q1 = {aggregate heavy count, inclusive heavy count} (count words)
-//   q2 = {inclusive heavy sum, inclusive light sum}   (ff words)
-struct alignas(64) PartState {
-    unsigned long long agg_h, agg_l, agg_c, pre_c, pre_h, pre_l, pad0, pad1;
+// Lookback state of one tile of the prefix-partition (128 B, 16 words).
+//  compensated modes (exact fixed-point carries, two 63-bit limbs per sum):
+//    agg heavy {0,1}, agg light {2,3}, agg count 4, incl count 6, incl heavy {8,9},
+//    incl light {10,11}
+//  FP32 mode (ff words): agg {0: heavy, 1: light}, agg count 4, incl count 6,
+//    incl {8: heavy, 9: light}
+struct alignas(128) PartState {
+    unsigned long long q[16];
 };
 // Lookback state of one tile of the scan (16 B): {aggregate, inclusive prefix}.
 struct alignas(16) ScanState {
     unsigned long long agg, pre;
+};
+
+// One distribution of a batch (device copy of wrs_dist_desc plus its place in the
+// batch's tile, split and sampling grids).
+struct alignas(64) DistDesc {
+    const float* w;     // weights, nullptr: the table is already built
+    uint2* table;       // alias table (n entries)
+    uint32_t* out;      // samples, nullptr: build only
+    uint64_t s;         // samples to draw
+    uint64_t seed;
+    uint64_t base;      // offset of this distribution in the batch's partition arrays
+    uint32_t n;
+    uint32_t tile0;     // first partition / total-mass tile (batch numbering)
+    uint32_t split0;    // first split-pack CTA
+    uint32_t sample0;   // first sampling CTA
+};
+static_assert(sizeof(DistDesc) == 64, "DistDesc layout");
+
+// Device view of a batch, passed by value to the batched kernels.
+struct BatchView {
+    const DistDesc* dist;
+    const uint32_t* tile_map;    // tile -> distribution
+    const uint32_t* split_map;   // split-pack CTA -> distribution
+    const uint32_t* sample_map;  // sampling CTA -> distribution
+    BuildCtrl* dctrl;            // per distribution
+    LbCtrl* lb;                  // partition tickets of the batch
+    uint32_t* status;            // batch status word
+    PartState* states;
+    double* partials;            // per tile
+    uint32_t* idx;               // partition arrays, distribution d at dist[d].base
+    float* prefix;
+    float* elems;                // nullptr: gather w[idx]
+    float* prefix_lo;            // float-float mode only
+    uint32_t cap_tiles;
+    uint32_t tiles, split_blocks, sample_blocks;  // grid sizes of the three launches
+    uint32_t split_size;
+    uint32_t full_light;
 };
 
 // ---- launchers (defined in wrs_build.cu / wrs_sample.cu) -------------------------
@@ -83,12 +126,33 @@ cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool
                               const float* cmf, uint32_t n, uint64_t s, uint64_t seed,
                               uint64_t offset, uint32_t* out);
 
+// batched forms (one launch each for all distributions of the batch)
+cudaError_t launch_batch_maps(cudaStream_t st, const DistDesc* dist, uint32_t count,
+                              uint32_t* tile_map, uint32_t* split_map, uint32_t* sample_map,
+                              uint32_t split_size);
+cudaError_t launch_batch_build(cudaStream_t st, uint32_t precision, bool r64,
+                               const BatchView& b);
+cudaError_t launch_batch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop,
+                                      const BatchView& b);
+
 // Records `msg` as the calling thread's wrs_last_error() and returns `status`
 // (defined in wrs_capi.cu).
 int set_last_error(int status, const char* msg);
 
-inline uint32_t tiles_for(uint32_t n) {
+// Device address of a batch's status word (defined in wrs_capi.cu).
+uint32_t* batch_status_word(::wrs_batch* b);
+
+__host__ __device__ inline uint32_t tiles_for(uint32_t n) {
     return static_cast<uint32_t>((static_cast<uint64_t>(n) + kTileItems - 1) / kTileItems);
 }
+// number of split subproblems of a distribution of n weights
+__host__ __device__ inline uint32_t splits_for(uint32_t n, uint32_t split_size) {
+    const uint32_t k = n / split_size;
+    return k ? k : 1u;
+}
+__host__ __device__ inline uint32_t split_blocks_for(uint32_t n, uint32_t split_size) {
+    return (splits_for(n, split_size) + kSplitPack - 1) / kSplitPack;
+}
+__host__ __device__ inline uint64_t alias_blocks_for(uint64_t s) { return (s + kAliasPerBlock - 1) / kAliasPerBlock; }
 
 }  // namespace wrs

@@ -21,8 +21,6 @@
 
 namespace wrs {
 
-constexpr int kSampleThreads = 256;
-constexpr int kAliasPerThread = 4;
 constexpr uint32_t RNG_REF = 0, RNG_PHILOX = 1;
 
 // mix(x, y, a) evaluated as x*(1-a) + y*a, one rounding per operation
@@ -30,13 +28,13 @@ __device__ __forceinline__ float mix_rn(float x, float y, float a) {
     return __fadd_rn(__fmul_rn(x, __fsub_rn(1.0f, a)), __fmul_rn(y, a));
 }
 
+// Samples [block * 1024 + 4t, +4) of one distribution (thread t of the CTA).
 template <uint32_t RNG, bool COOP>
-__global__ __launch_bounds__(kSampleThreads) void k_alias_sample(const uint2* __restrict__ table,
-                                                                 uint32_t n, uint64_t S,
-                                                                 uint64_t seed, uint64_t offset,
-                                                                 uint32_t coop,
-                                                                 uint32_t* __restrict__ out) {
-    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void alias_block(const uint2* __restrict__ table, uint32_t n,
+                                            uint64_t S, uint64_t seed, uint64_t offset,
+                                            uint32_t coop, uint32_t* __restrict__ out,
+                                            uint64_t block) {
+    const uint64_t t = block * kSampleThreads + threadIdx.x;
     const uint64_t s0 = t * kAliasPerThread;
     if (s0 >= S) return;
     uint32_t r[kAliasPerThread];
@@ -103,6 +101,27 @@ __global__ __launch_bounds__(kSampleThreads) void k_alias_sample(const uint2* __
         for (int v = 0; v < kAliasPerThread; ++v)
             if (s0 + v < S) out[s0 + v] = r[v];
     }
+}
+
+template <uint32_t RNG, bool COOP>
+__global__ __launch_bounds__(kSampleThreads) void k_alias_sample(const uint2* __restrict__ table,
+                                                                 uint32_t n, uint64_t S,
+                                                                 uint64_t seed, uint64_t offset,
+                                                                 uint32_t coop,
+                                                                 uint32_t* __restrict__ out) {
+    alias_block<RNG, COOP>(table, n, S, seed, offset, coop, out, blockIdx.x);
+}
+
+// All distributions of a batch in one launch: CTA b samples block b - sample0 of the
+// distribution the map names, with that distribution's seed and counter = sample index,
+// so each distribution draws exactly the samples a per-call wrs_sample would.
+template <uint32_t RNG, bool COOP>
+__global__ __launch_bounds__(kSampleThreads) void k_alias_sample_batch(BatchView bv,
+                                                                       uint32_t coop) {
+    const uint32_t d = __ldg(bv.sample_map + blockIdx.x);
+    const DistDesc* D = bv.dist + d;
+    alias_block<RNG, COOP>(D->table, D->n, D->s, D->seed, 0ull, coop, D->out,
+                           blockIdx.x - D->sample0);
 }
 
 // its/sampling/shader.comp:80-94
@@ -260,6 +279,20 @@ cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, co
             k_alias_sample<RNG_REF, false><<<grid, kSampleThreads, 0, st>>>(table, n, S, seed, offset, coop, out);
     } else {
         k_alias_sample<RNG_PHILOX, false><<<grid, kSampleThreads, 0, st>>>(table, n, S, seed, offset, coop, out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop,
+                                      const BatchView& b) {
+    if (b.sample_blocks == 0) return cudaSuccess;
+    if (rng == RNG_REF) {
+        if (coop)
+            k_alias_sample_batch<RNG_REF, true><<<b.sample_blocks, kSampleThreads, 0, st>>>(b, coop);
+        else
+            k_alias_sample_batch<RNG_REF, false><<<b.sample_blocks, kSampleThreads, 0, st>>>(b, 0u);
+    } else {
+        k_alias_sample_batch<RNG_PHILOX, false><<<b.sample_blocks, kSampleThreads, 0, st>>>(b, 0u);
     }
     return cudaGetLastError();
 }

@@ -46,6 +46,30 @@ class _Config(C.Structure):
         "scan_precision", "split_residual_f64", "split_full_light")]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("memory_budget", C.c_uint64), ("slots", C.c_uint32),
+                ("max_batch_dists", C.c_uint32), ("max_batch_weights", C.c_uint64),
+                ("max_batch_samples", C.c_uint64)]
+
+
+class Request(C.Structure):
+    """wrs_request: one build+sample request (device pointers)."""
+    _fields_ = [("table_id", C.c_uint64), ("weights", C.c_void_p), ("samples", C.c_void_p),
+                ("s", C.c_uint64), ("seed", C.c_uint64), ("n", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("submit_s", C.c_double), ("done_s", C.c_double),
+                ("built", C.c_uint32), ("status", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "submitted", "completed", "batches", "builds", "reuses", "evictions",
+        "table_arena_bytes", "table_bytes_peak", "scratch_bytes", "device_status")]
+
+
 _lib: C.CDLL | None = None
 
 
@@ -93,6 +117,23 @@ def lib() -> C.CDLL:
             "wrs_buffers_mean64": (vp, [vp]),
             "wrs_test_prefix_sum_stalled": (i32, [vp, vp, vp, u32, vp, vp, u32]),
             "wrs_prefix_sum_noalloc": (i32, [vp, vp, u32, vp, u32, vp]),
+            "wrs_batch_bytes": (sz, [vp, u32, u64, u64]),
+            "wrs_batch_create": (i32, [vp, u32, u64, u64, C.POINTER(vp)]),
+            "wrs_batch_destroy": (None, [vp]),
+            "wrs_batch_set": (i32, [vp, vp, vp, u32]),
+            "wrs_batch_count": (u32, [vp]),
+            "wrs_batch_build": (i32, [vp, vp, vp]),
+            "wrs_batch_sample": (i32, [vp, vp, vp]),
+            "wrs_batch_status": (i32, [vp, vp, C.POINTER(u32)]),
+            "wrs_server_config_init": (i32, [C.POINTER(ServerConfig)]),
+            "wrs_server_create": (i32, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
+            "wrs_server_destroy": (None, [vp]),
+            "wrs_server_submit": (i32, [vp, C.POINTER(Request), C.POINTER(u64)]),
+            "wrs_server_progress": (i32, [vp, C.POINTER(Completion), u32, C.POINTER(u32)]),
+            "wrs_server_pending": (u64, [vp]),
+            "wrs_server_get_stats": (i32, [vp, C.POINTER(ServerStats)]),
+            "wrs_server_run_trace": (i32, [vp, C.POINTER(Request), C.POINTER(C.c_double), u32,
+                                           C.POINTER(Completion)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -283,3 +324,116 @@ class WRS:
     def its_sample(self, stream, cmf, N, S, seed, offset, out) -> None:
         check(lib().wrs_its_sample(self.handle.ptr, _stream_ptr(stream), _dev_ptr(cmf), N, S,
                                    seed, offset, _dev_ptr(out)))
+
+
+class DistDesc(C.Structure):
+    """wrs_dist_desc: one distribution of a batch (device pointers)."""
+    _fields_ = [("weights", C.c_void_p), ("table", C.c_void_p), ("samples", C.c_void_p),
+                ("s", C.c_uint64), ("seed", C.c_uint64), ("n", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class Batch:
+    """Many distributions built and sampled with one launch per stage (wrs_batch_*): the
+    batched form of WRS.build / WRS.sample.  No counterpart in the reference."""
+
+    def __init__(self, handle: Handle, max_dists: int, max_weights: int, max_samples: int):
+        self.handle = handle
+        p = C.c_void_p()
+        check(lib().wrs_batch_create(handle.ptr, max_dists, max_weights, max_samples,
+                                     C.byref(p)))
+        self.ptr = p.value
+        self._descs = None
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib().wrs_batch_destroy(self.ptr)
+            self.ptr = None
+
+    @staticmethod
+    def bytes(handle: Handle, max_dists: int, max_weights: int, max_samples: int) -> int:
+        return lib().wrs_batch_bytes(handle.ptr, max_dists, max_weights, max_samples)
+
+    def set(self, stream, dists) -> None:
+        """dists: iterable of (weights, table, samples, n, s, seed); weights / samples may be
+        None (sample only / build only); tensors or raw device addresses."""
+        dists = list(dists)
+        arr = (DistDesc * max(1, len(dists)))()
+        for i, (w, t, out, n, s, seed) in enumerate(dists):
+            arr[i] = DistDesc(_dev_ptr(w), _dev_ptr(t), _dev_ptr(out), s, seed, n, 0)
+        self._descs = arr
+        check(lib().wrs_batch_set(self.ptr, _stream_ptr(stream), arr, len(dists)))
+
+    def build(self, stream) -> None:
+        check(lib().wrs_batch_build(self.handle.ptr, _stream_ptr(stream), self.ptr))
+
+    def sample(self, stream) -> None:
+        check(lib().wrs_batch_sample(self.handle.ptr, _stream_ptr(stream), self.ptr))
+
+    def count(self) -> int:
+        return lib().wrs_batch_count(self.ptr)
+
+    def status(self, stream=None) -> int:
+        v = C.c_uint32()
+        check(lib().wrs_batch_status(self.ptr, _stream_ptr(stream), C.byref(v)))
+        return v.value
+
+
+class Server:
+    """The served request loop (wrs_server_*): continuous batching of build+sample requests
+    with resident alias tables under a device memory budget.  No counterpart in the
+    reference."""
+
+    def __init__(self, handle: Handle, memory_budget: int = 16 << 30, slots: int = 3,
+                 max_batch_dists: int = 1024, max_batch_weights: int = 1 << 25,
+                 max_batch_samples: int = 1 << 24):
+        self.handle = handle
+        c = ServerConfig()
+        check(lib().wrs_server_config_init(C.byref(c)))
+        c.memory_budget, c.slots, c.max_batch_dists = memory_budget, slots, max_batch_dists
+        c.max_batch_weights, c.max_batch_samples = max_batch_weights, max_batch_samples
+        p = C.c_void_p()
+        check(lib().wrs_server_create(handle.ptr, C.byref(c), C.byref(p)))
+        self.ptr = p.value
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib().wrs_server_destroy(self.ptr)
+            self.ptr = None
+
+    @staticmethod
+    def requests(rows) -> "C.Array":
+        """rows: iterable of (table_id, weights_ptr, samples_ptr, n, s, seed)."""
+        rows = list(rows)
+        arr = (Request * max(1, len(rows)))()
+        for i, (tid, w, out, n, s, seed) in enumerate(rows):
+            arr[i] = Request(tid, _dev_ptr(w), _dev_ptr(out), s, seed, n, 0)
+        return arr
+
+    def submit(self, req: Request) -> int:
+        t = C.c_uint64()
+        check(lib().wrs_server_submit(self.ptr, C.byref(req), C.byref(t)))
+        return t.value
+
+    def progress(self, max_out: int = 1024) -> list:
+        buf = (Completion * max_out)()
+        c = C.c_uint32()
+        check(lib().wrs_server_progress(self.ptr, buf, max_out, C.byref(c)))
+        return [buf[i] for i in range(c.value)]
+
+    def pending(self) -> int:
+        return lib().wrs_server_pending(self.ptr)
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(lib().wrs_server_get_stats(self.ptr, C.byref(st)))
+        return {name: getattr(st, name) for name, _ in ServerStats._fields_}
+
+    def run_trace(self, reqs, arrivals) -> "C.Array":
+        """Replays requests at their arrival times (seconds from the call); returns the
+        completions in request order."""
+        n = len(arrivals)
+        arr = (C.c_double * max(1, n))(*arrivals)
+        out = (Completion * max(1, n))()
+        check(lib().wrs_server_run_trace(self.ptr, reqs, arr, n, out))
+        return out

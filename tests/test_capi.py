@@ -89,3 +89,66 @@ def test_cpp_facade_compiles(pkg, tmp_path):
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"),
                         str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_batch_argument_checks_on_host(pkg):
+    """wrs_batch_* reject bad arguments before touching a GPU."""
+    w = pkg.wrs
+    L = w.lib()
+    out = C.c_void_p()
+    h = w.Handle(w.AliasTableConfig())
+    assert L.wrs_batch_create(None, 1, 1, 1, C.byref(out)) == 1
+    assert L.wrs_batch_create(h.ptr, 0, 1, 1, C.byref(out)) == 1       # max_dists = 0
+    assert L.wrs_batch_create(h.ptr, 1 << 25, 1, 1, C.byref(out)) == 1  # too many
+    its = w.Handle(w.ITSConfig())
+    assert L.wrs_batch_create(its.ptr, 1, 1, 1, C.byref(out)) == 5     # alias method only
+    assert L.wrs_batch_set(None, None, None, 0) == 1
+    assert L.wrs_batch_build(h.ptr, None, None) == 1
+    assert L.wrs_batch_sample(h.ptr, None, None) == 1
+    assert L.wrs_batch_status(None, None, None) == 1
+    assert L.wrs_batch_bytes(its.ptr, 1, 1, 1) == 0
+    assert L.wrs_batch_bytes(h.ptr, 4096, 1 << 28, 1 << 30) > (1 << 28) * 12
+
+
+def test_server_argument_checks_on_host(pkg):
+    """wrs_server_* validate their configuration before touching a GPU."""
+    w = pkg.wrs
+    L = w.lib()
+    c = w.ServerConfig()
+    assert L.wrs_server_config_init(C.byref(c)) == 0
+    assert (c.memory_budget, c.slots, c.max_batch_dists) == (16 << 30, 3, 1024)
+    assert (c.max_batch_weights, c.max_batch_samples) == (1 << 25, 1 << 24)
+    h = w.Handle(w.AliasTableConfig())
+    out = C.c_void_p()
+    assert L.wrs_server_create(None, C.byref(c), C.byref(out)) == 1
+    bad = w.ServerConfig.from_buffer_copy(c)
+    bad.slots = 0
+    assert L.wrs_server_create(h.ptr, C.byref(bad), C.byref(out)) == 1
+    small = w.ServerConfig.from_buffer_copy(c)
+    small.memory_budget = 1 << 20  # below one slot's batch scratch
+    assert L.wrs_server_create(h.ptr, C.byref(small), C.byref(out)) == 1
+    its = w.Handle(w.ITSConfig())
+    assert L.wrs_server_create(its.ptr, C.byref(c), C.byref(out)) == 1
+    assert L.wrs_server_submit(None, None, None) == 1
+    assert L.wrs_server_progress(None, None, 0, None) == 1
+    assert L.wrs_server_pending(None) == 0
+
+
+def test_served_workload_shape(pkg):
+    """The served request stream: Poisson arrivals at the stated rate, N and S in range,
+    about 30% of requests reuse an earlier table id, and a reused id keeps its n and its
+    weights slice."""
+    import importlib
+    import numpy as np
+    wl = importlib.import_module("merian-wrs_gb300.workloads").served(
+        "cpu", 20000, 50000.0, seed=7, n_max=1 << 16, pool_log2=20)
+    a = wl["arrivals"]
+    assert np.all(np.diff(a) >= 0) and abs(len(a) / a[-1] - 50000.0) < 2500.0
+    assert wl["n"].min() >= 256 and wl["n"].max() <= 1 << 16
+    assert wl["s"].min() >= 1 and wl["s"].max() <= 65536
+    reused = wl["table_id"] != np.arange(len(a))
+    assert 0.27 < reused.mean() < 0.33
+    for i in np.nonzero(reused)[0][:200]:
+        j = wl["table_id"][i]
+        assert wl["n"][i] == wl["n"][j] and wl["w_off"][i] == wl["w_off"][j]
+    assert np.all(wl["w_off"] % 32 == 0) and wl["w"].numel() == 1 << 20

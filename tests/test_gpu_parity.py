@@ -321,14 +321,19 @@ def test_precision_weights_never_sample_zero(pkg, cuda, oracle):
 
 # ------------------------------------------------------------ determinism, status ---
 
-def test_build_is_deterministic(pkg, cuda):
-    """Repeated builds of one input give identical tables (compensated carry)."""
-    w = weights_lognormal((1 << 21) + 9, 12)
-    cfg = pkg.AliasTableConfig(scan_precision=1)
+@pytest.mark.parametrize("precision", [1, 2])
+def test_build_is_deterministic(pkg, cuda, precision):
+    """Repeated builds of one input give identical prefixes and tables: in the compensated
+    precisions the lookback carries exact fixed-point sums, so a tile's carry does not
+    depend on which predecessors the lookback saw."""
+    w = weights_lognormal((1 << 22) + 9, 12)
+    cfg = pkg.AliasTableConfig(scan_precision=precision, split_size=8)
     a = Built(pkg, w, cfg)
-    for _ in range(2):
+    for _ in range(3):
         b = Built(pkg, w, cfg)
         assert np.array_equal(a.prefix.view(np.uint32), b.prefix.view(np.uint32))
+        if precision == 2:
+            assert np.array_equal(a.prefix_lo.view(np.uint32), b.prefix_lo.view(np.uint32))
         assert same_table(a.table, b.table)
 
 
