@@ -379,6 +379,9 @@ def main() -> None:
                                       max(3, args.warmup))
     if not args.no_served:
         line["served"] = served_leg(W, cfg, dev)
+    if not args.no_extras:
+        line["small"] = small_leg(W, dev)
+        line["precision"] = precision_leg(W, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         w0 = weights[0].cpu().numpy()
         s_sample = 1 << min(args.log2s, 25)
@@ -561,6 +564,141 @@ def served_leg(W, cfg, dev, n_requests: int = SERVED_REQUESTS) -> dict:
         "scratch_bytes": st["scratch_bytes"], "device_status": st["device_status"],
         "alone_vs_mix_equal": f"{equal}/{len(pick)}",
     }
+
+
+def _dev_copy(dst, src_ptr: int, nbytes: int) -> None:
+    """Device-to-device copy from a raw device address (an internals view) into a tensor."""
+    import ctypes
+    import torch
+    torch.cuda.synchronize()
+    rt = ctypes.CDLL("libcudart.so." + torch.version.cuda.split(".")[0])
+    rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    assert rt.cudaMemcpy(dst.data_ptr(), src_ptr, nbytes, 3) == 0
+
+
+def _implied(table, n: int):
+    """Probability mass (in mean units) an alias table gives each index, on the device:
+    p_i + sum over buckets j aliasing to i of (1 - p_j)."""
+    import torch
+    t = table.view(torch.int32).view(-1, 2)
+    p = t[:, 0].contiguous().view(torch.float32).double()
+    a = t[:, 1].long()
+    return p.index_add(0, a, 1.0 - p)
+
+
+def precision_leg(W, dev, log2n: int = 28, log2s: int = 30) -> dict:
+    """The precision study: N = 2^28 log-normal(0, 3) weights with 1% forced to 0 and 0.01%
+    scaled by 1e6.  Scans (plain FP32 carry, compensated carry) against an FP64 scan of the
+    same weights (torch.cumsum in FP64); alias tables of the three precisions against
+    w / mean (FP64); RMSE of S = 2^30 ITS and alias draws against w / sum(w); zero-weight
+    indices must never be drawn."""
+    import torch
+    n, s = 1 << log2n, 1 << log2s
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    w = torch.exp(3.0 * torch.randn(n, generator=g, device=dev, dtype=torch.float32))
+    w[torch.rand(n, generator=g, device=dev) < 0.01] = 0.0
+    big = torch.rand(n, generator=g, device=dev) < 1e-4
+    w[big] = (w[big].double() * 1e6).float()
+    ref = torch.cumsum(w.double(), 0)
+    pos = ref > 0
+    total = float(ref[-1])
+    target = w.double() / total
+    out = {"workload": f"precision study: N=2^{log2n} log-normal(0,3), 1% zeros, 0.01% x1e6; "
+                       f"S=2^{log2s} draws per sampler", "N": n, "S": s}
+    cmf = torch.empty(n, dtype=torch.float32, device=dev)
+    scans = {}
+    for name, prec in (("fp32", W.SCAN_FP32), ("compensated", W.SCAN_COMPENSATED)):
+        its = W.WRS(W.ITSConfig(rng=W.RNG_PHILOX4X32_10, scan_precision=prec))
+        internals = W.Internals(its.handle, n)
+        its.prefix_sum(None, w, n, cmf, internals)
+        torch.cuda.synchronize()
+        rel = ((cmf.double() - ref).abs() / ref.clamp_min(1e-300))[pos]
+        scans[name] = {"max_rel_prefix_err": float(rel.max()),
+                       "max_rel_err_last": float(abs(float(cmf[-1]) - total) / total)}
+        if prec == W.SCAN_COMPENSATED:
+            samples = torch.empty(s, dtype=torch.int32, device=dev)
+            its.its_sample(None, cmf, n, s, 11, 0, samples)
+            hist = torch.bincount(samples.long(), minlength=n).double() / s
+            scans[name]["its_rmse"] = float(torch.sqrt(torch.mean((hist - target) ** 2)))
+            scans[name]["its_zero_weight_draws"] = int(hist[w == 0].sum() * s)
+            del samples, hist
+        del internals
+    out["scan"] = scans
+    tables = {}
+    mean_units = w.double() / (total / n)
+    for name, prec in (("fp32", W.SCAN_FP32), ("compensated", W.SCAN_COMPENSATED),
+                       ("float-float", W.SCAN_FLOAT_FLOAT)):
+        cfg = W.AliasTableConfig(split_size=SPLIT_SIZE, rng=W.RNG_PHILOX4X32_10,
+                                 scan_precision=prec, split_residual_f64=True,
+                                 split_full_light=True)
+        wrs = W.WRS(cfg)
+        internals = W.Internals(wrs.handle, n)
+        samples = torch.empty(s, dtype=torch.int32, device=dev)
+        wrs.build(None, W.WRSBuffers(w, samples, internals), n)
+        wrs.sample(None, W.WRSBuffers(w, samples, internals), n, s, seed=11)
+        torch.cuda.synchronize()
+        table_t = torch.empty(2 * n, dtype=torch.int32, device=dev)
+        _dev_copy(table_t, internals.views()["alias_table"], 8 * n)
+        imp = _implied(table_t, n)
+        err = (imp - mean_units).abs()
+        hist = torch.bincount(samples.long(), minlength=n).double() / s
+        tables[name] = {"max_abs_err_mean_units": float(err.max()),
+                        "max_rel_err_w_ge_mean": float((err / mean_units)[mean_units >= 1].max()),
+                        "alias_rmse": float(torch.sqrt(torch.mean((hist - target) ** 2))),
+                        "zero_weight_draws": int(hist[w == 0].sum() * s),
+                        "status": internals.status()}
+        del internals, samples, hist, table_t, imp, err
+        torch.cuda.empty_cache()
+    out["alias"] = tables
+    out["rmse_ideal"] = float(torch.sqrt(torch.mean(target * (1 - target) / s)))
+    return out
+
+
+def small_leg(W, dev, steps: int = 20) -> dict:
+    """The plain small configuration: N = 65,536 uniform(0,1] weights (seed 1), PSA build +
+    S = 2^20 Philox4x32-10 samples (seed 1); builds/s and samples/s over `steps` repetitions,
+    chi-square (df = N - 1) p-value and RMSE of the histogram against w / sum(w)."""
+    import numpy as np
+    import torch
+    n, s = 65536, 1 << 20
+    cfg = W.AliasTableConfig(split_size=2, rng=W.RNG_PHILOX4X32_10)
+    wrs = W.WRS(cfg)
+    w = make_weights(0, n, 1, dev)
+    samples = torch.empty(s, dtype=torch.int32, device=dev)
+    bufs = W.WRSBuffers(w, samples, W.Internals(wrs.handle, n))
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        wrs.build(stream, bufs, n)
+        wrs.sample(stream, bufs, n, s, seed=1)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    e[0].record(stream)
+    for _ in range(steps):
+        wrs.build(stream, bufs, n)
+    e[1].record(stream)
+    for _ in range(steps):
+        wrs.sample(stream, bufs, n, s, seed=1)
+    e[2].record(stream)
+    torch.cuda.synchronize()
+    build_s = e[0].elapsed_time(e[1]) / steps / 1e3
+    sample_s = e[1].elapsed_time(e[2]) / steps / 1e3
+    hist = torch.bincount(samples.long(), minlength=n).double().cpu().numpy()
+    p = w.double().cpu().numpy()
+    p /= p.sum()
+    exp = p * s
+    chi2 = float(((hist - exp) ** 2 / exp).sum())
+    try:
+        from scipy.stats import chi2 as chi2_dist
+        pval = float(chi2_dist.sf(chi2, n - 1))
+    except ImportError:
+        pval = None
+    return {"workload": "plain path, small: N=65,536 uniform(0,1] (seed 1), PSA build (split 2) "
+                        "+ S=2^20 Philox4x32-10 samples (seed 1)",
+            "builds_per_s": 1.0 / build_s, "samples_per_s": s / sample_s,
+            "build_us": build_s * 1e6, "sample_us": sample_s * 1e6,
+            "chi2": chi2, "df": n - 1, "p_value": pval,
+            "rmse": float(np.sqrt(np.mean((hist / s - p) ** 2))),
+            "rmse_ideal": float(np.sqrt(np.mean(p * (1 - p) / s)))}
 
 
 def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, peak, args):

@@ -59,15 +59,28 @@ __device__ __forceinline__ void load_tile(const float* __restrict__ w, uint32_t 
     }
 }
 
+// Resident partition CTAs per SM the register allocation is sized for (5 x 256 threads:
+// at most 51 registers per thread).
+#ifndef WRS_PART_MIN_BLOCKS
+#define WRS_PART_MIN_BLOCKS 5
+#endif
+constexpr int kPartMinBlocks = WRS_PART_MIN_BLOCKS;
+
+// float4 slot of chunk q (items 4q..4q+3) of a tile parked in shared memory: the XOR
+// swizzle spreads both the coalesced order (q = 32v + lane per warp) and the transposed order
+// (q = 4 lane + j) over all eight 16-byte bank groups (4 wavefronts per warp access).
+__device__ __forceinline__ uint32_t park_slot(uint32_t q) { return q ^ ((q >> 3) & 7u); }
+
 // ---------------------------------------------------------------------------------
 // total mass
 // ---------------------------------------------------------------------------------
 
 // One CTA per 4096-item tile.  Each thread sums its 16 items in a fixed order with a
-// compensated FP32 accumulator (two-sum), the CTA combines its threads in FP64 in a fixed
-// tree, and the last tile of the distribution to finish sums the tile partials in a fixed
-// order.  The total is therefore a function of the weights alone (not of the launch
-// geometry, of the buffer's alignment or of other distributions in a batch).
+// compensated FP32 accumulator (two-sum), the CTA combines its threads in float-float in a
+// fixed tree (FP32 arithmetic: GB300's FP64 pipe is narrow), the tile partial hi + lo is
+// stored in FP64, and the last tile of the distribution to finish sums the partials in FP64
+// in a fixed order.  The total is therefore a function of the weights alone (not of the
+// launch geometry, of the buffer's alignment or of other distributions in a batch).
 template <bool BATCH>
 __global__ __launch_bounds__(kTileThreads) void k_total_mass(const float* __restrict__ w_in,
                                                              uint32_t n_in,
@@ -75,6 +88,7 @@ __global__ __launch_bounds__(kTileThreads) void k_total_mass(const float* __rest
                                                              BuildCtrl* __restrict__ ctrl_in,
                                                              BatchView bv) {
     __shared__ double s_red[kTileWarps];
+    __shared__ ff s_part[kTileWarps];
     __shared__ bool s_last;
     const uint32_t tile = blockIdx.x;
     const float* w = w_in;
@@ -97,16 +111,14 @@ __global__ __launch_bounds__(kTileThreads) void k_total_mass(const float* __rest
 #pragma unroll
         for (int c = 0; c < 4; ++c) acc = carry_add<true>(acc, ff{x[v][c], 0.0f});
 
-    double d = __dadd_rn(static_cast<double>(acc.hi), static_cast<double>(acc.lo));
-#pragma unroll
-    for (int m = 16; m > 0; m >>= 1) d = __dadd_rn(d, __shfl_xor_sync(0xffffffffu, d, m));
+    acc = ff_warp_total(acc);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) s_red[warp] = d;
+    if (lane == 0) s_part[warp] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double b = 0.0;
-        for (int k = 0; k < kTileWarps; ++k) b = __dadd_rn(b, s_red[k]);
-        partials[tile] = b;
+        ff b = s_part[0];
+        for (int k = 1; k < kTileWarps; ++k) b = carry_add<true>(b, s_part[k]);
+        partials[tile] = __dadd_rn(static_cast<double>(b.hi), static_cast<double>(b.lo));
         __threadfence();
         const uint32_t prev = atomicAdd(&ctrl->mass_done, 1u);
         s_last = (prev == ntiles - 1u);
@@ -351,118 +363,117 @@ struct PartArgs {
     float* prefix_lo;
 };
 
-// One CTA = one tile of 4096 weights; warp w owns items [w*512, w*512+512) of the tile and
-// lane L holds, for v = 0..3, the 4 consecutive items at v*128 + L*4 (16-byte loads, fully
-// coalesced).  Heavy (w > mean) items go to idx[heavyRank], light items to
-// idx[N-1-lightRank]; prefix[] holds the inclusive heavy resp. light prefix sum, elems[] the
-// weight (shader.comp:329-361).
+// One CTA = one tile of 4096 weights.  The tile is loaded with 16-byte coalesced loads and
+// parked in shared memory; thread t of warp w then works on the 16 consecutive items
+// [w*512 + 16t, +16), so a single warp scan per class gives every thread its offsets.
+// Heavy (w > mean) items go to idx[heavyRank], light items to idx[N-1-lightRank]; prefix[]
+// holds the inclusive heavy resp. light prefix sum, elems[] the weight
+// (shader.comp:329-361).
 //
-// COMP (compensated modes): the tile aggregates and the lookback carry are exact fixed-point
-// sums (fx_*), rounded once to a float-float carry per tile; local sums within the tile run in
-// a fixed order.  Every prefix is then a deterministic function of the weights.  FFOUT also
-// writes prefix_lo[], the low word of the prefix as a float-float pair (prefix[] is its high
-// word), with the local sums in float-float as well.
+// COMP (compensated modes): the tile aggregates (FP32, or float-float with FFOUT) are summed
+// along the lookback exactly in fixed point (fx_*) and the carry is rounded once to a
+// float-float pair per tile; sums within a tile run in a fixed order.  Every prefix is then a
+// deterministic function of the weights.  FFOUT also writes prefix_lo[], the low word of the
+// prefix as a float-float pair (prefix[] is its high word), with float-float local sums.
 template <bool COMP, bool FFOUT, bool BATCH>
-__global__ __launch_bounds__(kTileThreads) void k_prefix_partition(PartArgs a, BatchView bv) {
+__global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partition(PartArgs a,
+                                                                                   BatchView bv) {
     // warp totals (phase A), turned into warp-exclusive offsets by warp 0 (phase B)
     __shared__ uint32_t s_wc[kTileWarps];
     __shared__ float s_wh[kTileWarps], s_wl[kTileWarps];  // local FP32 sums (!FFOUT)
     __shared__ ff s_fh[kTileWarps], s_fl[kTileWarps];     // local float-float sums (FFOUT)
-    __shared__ u128 s_xh[kTileWarps], s_xl[kTileWarps];   // exact sums (COMP)
     __shared__ ff s_exh, s_exl;
     __shared__ uint32_t s_exc, s_aggc;
-    __shared__ float4 s_x[kTileItems / 4];  // the tile, parked over the lookback
+    __shared__ float4 s_x[kTileItems / 4];  // the tile, swizzled (park_slot)
+
+    __shared__ uint32_t s_lc[kTileThreads];                  // lane-exclusive heavy counts
+    __shared__ float2 s_lh[kTileThreads], s_ll[kTileThreads];  // lane-exclusive local sums
 
     PartState* cur;
     const uint32_t tile = lookback_begin(a.lb, a.states, a.cap_tiles, cur);
     const float* w = a.w;
     uint32_t n = a.n, first = 0;
     BuildCtrl* ctrl = a.ctrl;
-    uint32_t* idx_out = a.idx;
-    float* prefix_out = a.prefix;
-    float* elems_out = a.elems;
-    float* prefix_lo_out = a.prefix_lo;
+    const DistDesc* D = nullptr;
     if constexpr (BATCH) {
-        const uint32_t d = __ldg(bv.tile_map + tile);
-        const DistDesc* D = bv.dist + d;
+        D = bv.dist + __ldg(bv.tile_map + tile);
         w = D->w;
         n = D->n;
         first = D->tile0;
-        ctrl = bv.dctrl + d;
-        const uint64_t base = D->base;
-        idx_out += base;
-        prefix_out += base;
-        if (elems_out) elems_out += base;
-        if (prefix_lo_out) prefix_lo_out += base;
+        ctrl = bv.dctrl + (D - bv.dist);
     }
     const uint32_t lt = tile - first;
     const float pivot = ctrl->mean;
-    const int grid = COMP ? fx_grid(ctrl->total) : 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t tbase = lt * kTileItems;
 
-    float x[4][4];
-    load_tile(w, n, lt, x);
-
-    // ---- phase A: thread and warp totals of the heavy / light classes
     {
+        float x[4][4];
+        load_tile(w, n, lt, x);
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+            s_x[park_slot(warp * 128 + v * 32 + lane)] = make_float4(x[v][0], x[v][1], x[v][2], x[v][3]);
+    }
+    __syncwarp();
+
+    // ---- phase A: thread totals over 16 consecutive items, warp scans; the lane-exclusive
+    // values wait in shared memory until phase C (registers stay free for the lookback)
+    {
+        float y[16];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float4 q = s_x[park_slot(warp * 128 + lane * 4 + j)];
+            y[4 * j] = q.x;
+            y[4 * j + 1] = q.y;
+            y[4 * j + 2] = q.z;
+            y[4 * j + 3] = q.w;
+        }
         uint32_t tc = 0;
         float th = 0.f, tl = 0.f;
         ff fh{0.f, 0.f}, fl{0.f, 0.f};
-        u128 xh = 0, xl = 0;
 #pragma unroll
-        for (int v = 0; v < 4; ++v)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const float xv = x[v][c];
-                if (xv > pivot) {
-                    ++tc;
-                    if constexpr (COMP) xh += fx_from_float(xv, grid);
-                    if constexpr (FFOUT)
-                        fh = ff_add_f(fh, xv);
-                    else
-                        th = __fadd_rn(th, xv);
-                } else {
-                    if constexpr (COMP) xl += fx_from_float(xv, grid);
-                    if constexpr (FFOUT)
-                        fl = ff_add_f(fl, xv);
-                    else
-                        tl = __fadd_rn(tl, xv);
-                }
-            }
-#pragma unroll
-        for (int m = 1; m < 32; m <<= 1) {
-            tc += __shfl_xor_sync(0xffffffffu, tc, m);
-            if constexpr (!FFOUT) {
-                th = __fadd_rn(th, __shfl_xor_sync(0xffffffffu, th, m));
-                tl = __fadd_rn(tl, __shfl_xor_sync(0xffffffffu, tl, m));
-            }
-            if constexpr (COMP) {
-                xh += shfl_xor_u128(xh, m);
-                xl += shfl_xor_u128(xl, m);
-            }
-        }
-        if constexpr (FFOUT) {
-            fh = ff_warp_total(fh);
-            fl = ff_warp_total(fl);
-        }
-        // park the items in shared memory: registers stay free for the lookback
-#pragma unroll
-        for (int v = 0; v < 4; ++v)
-            s_x[(warp * kWarpItems + v * 128 + lane * 4) / 4] =
-                make_float4(x[v][0], x[v][1], x[v][2], x[v][3]);
-        if (lane == 0) {
-            s_wc[warp] = tc;
-            if constexpr (FFOUT) {
-                s_fh[warp] = fh;
-                s_fl[warp] = fl;
+        for (int i = 0; i < 16; ++i) {
+            if (y[i] > pivot) {
+                ++tc;
+                if constexpr (FFOUT)
+                    fh = ff_add_f(fh, y[i]);
+                else
+                    th = __fadd_rn(th, y[i]);
             } else {
-                s_wh[warp] = th;
-                s_wl[warp] = tl;
+                if constexpr (FFOUT)
+                    fl = ff_add_f(fl, y[i]);
+                else
+                    tl = __fadd_rn(tl, y[i]);
             }
-            if constexpr (COMP) {
-                s_xh[warp] = xh;
-                s_xl[warp] = xl;
+        }
+        const uint32_t ic = warp_incl_u(tc, lane);
+        s_lc[threadIdx.x] = ic - tc;
+        uint32_t wtot_c = __shfl_sync(0xffffffffu, ic, 31);
+        float wtot_h = 0.f, wtot_l = 0.f;
+        ff wf_h{0.f, 0.f}, wf_l{0.f, 0.f};
+        if constexpr (FFOUT) {
+            const ff ih = ff_warp_incl(fh, lane), il = ff_warp_incl(fl, lane);
+            const ff lh = ff_shfl_up_excl(ih, lane), ll = ff_shfl_up_excl(il, lane);
+            s_lh[threadIdx.x] = make_float2(lh.hi, lh.lo);
+            s_ll[threadIdx.x] = make_float2(ll.hi, ll.lo);
+            wf_h = ff_shfl(ih, 31);
+            wf_l = ff_shfl(il, 31);
+        } else {
+            const float ih = warp_incl_f(th, lane), il = warp_incl_f(tl, lane);
+            const float eh = __shfl_up_sync(0xffffffffu, ih, 1);
+            const float el = __shfl_up_sync(0xffffffffu, il, 1);
+            s_lh[threadIdx.x] = make_float2(lane ? eh : 0.f, 0.f);
+            s_ll[threadIdx.x] = make_float2(lane ? el : 0.f, 0.f);
+            wtot_h = __shfl_sync(0xffffffffu, ih, 31);
+            wtot_l = __shfl_sync(0xffffffffu, il, 31);
+        }
+        if (lane == 0) {
+            s_wc[warp] = wtot_c;
+            if constexpr (FFOUT) {
+                s_fh[warp] = wf_h;
+                s_fl[warp] = wf_l;
+            } else {
+                s_wh[warp] = wtot_h;
+                s_wl[warp] = wtot_l;
             }
         }
     }
@@ -473,20 +484,22 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(PartArgs a, B
         const uint32_t ic = warp_incl_u(lane < kTileWarps ? s_wc[lane] : 0u, lane);
         const uint32_t ec = __shfl_up_sync(0xffffffffu, ic, 1);
         const uint32_t agg_c = __shfl_sync(0xffffffffu, ic, kTileWarps - 1);
-        float eh = 0.f, el = 0.f, agg_h = 0.f, agg_l = 0.f;
-        ff fxh{0.f, 0.f}, fxl{0.f, 0.f};
+        float eh = 0.f, el = 0.f;
+        ff agg_h{0.f, 0.f}, agg_l{0.f, 0.f}, fxh{0.f, 0.f}, fxl{0.f, 0.f};
         if constexpr (FFOUT) {
             const ff ith = ff_warp_incl(lane < kTileWarps ? s_fh[lane] : ff{0.f, 0.f}, lane);
             const ff itl = ff_warp_incl(lane < kTileWarps ? s_fl[lane] : ff{0.f, 0.f}, lane);
             fxh = ff_shfl_up_excl(ith, lane);
             fxl = ff_shfl_up_excl(itl, lane);
+            agg_h = ff_shfl(ith, kTileWarps - 1);
+            agg_l = ff_shfl(itl, kTileWarps - 1);
         } else {
             const float ih = warp_incl_f(lane < kTileWarps ? s_wh[lane] : 0.f, lane);
             const float il = warp_incl_f(lane < kTileWarps ? s_wl[lane] : 0.f, lane);
             eh = __shfl_up_sync(0xffffffffu, ih, 1);
             el = __shfl_up_sync(0xffffffffu, il, 1);
-            agg_h = __shfl_sync(0xffffffffu, ih, kTileWarps - 1);
-            agg_l = __shfl_sync(0xffffffffu, il, kTileWarps - 1);
+            agg_h = {__shfl_sync(0xffffffffu, ih, kTileWarps - 1), 0.f};
+            agg_l = {__shfl_sync(0xffffffffu, il, kTileWarps - 1), 0.f};
         }
         __syncwarp();
         if (lane < kTileWarps) {
@@ -502,12 +515,8 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(PartArgs a, B
         ff exh{0.f, 0.f}, exl{0.f, 0.f};
         uint32_t exc = 0;
         if constexpr (COMP) {
-            PartX agg{0, 0, agg_c};
-#pragma unroll
-            for (int k = 0; k < kTileWarps; ++k) {
-                agg.h += s_xh[k];
-                agg.l += s_xl[k];
-            }
+            const int grid = fx_grid(ctrl->total);
+            const PartX agg{fx_from_ff(agg_h, grid), fx_from_ff(agg_l, grid), agg_c};
             PartX ex{0, 0, 0u};
             if (tile == first) {
                 if (lane == 0) {
@@ -526,7 +535,7 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(PartArgs a, B
             }
             exc = ex.c;
         } else {
-            const PartCarry agg{agg_h, agg_l, agg_c};
+            const PartCarry agg{agg_h.hi, agg_l.hi, agg_c};
             PartCarry ex{0.f, 0.f, 0u};
             if (tile == first) {
                 if (lane == 0) {
@@ -555,95 +564,66 @@ __global__ __launch_bounds__(kTileThreads) void k_prefix_partition(PartArgs a, B
     }
     __syncthreads();
 
-    // ---- phase C: local scans in item order, scatter (items back from shared memory)
+    // ---- phase C: running sums over the thread's items, scatter
+    uint32_t* idx_out = a.idx;
+    float* prefix_out = a.prefix;
+    float* elems_out = a.elems;
+    float* prefix_lo_out = a.prefix_lo;
+    if constexpr (BATCH) {
+        const uint64_t base = D->base;
+        idx_out += base;
+        prefix_out += base;
+        if (elems_out) elems_out += base;
+        if (prefix_lo_out) prefix_lo_out += base;
+    }
+    const uint32_t tbase = lt * kTileItems;
+    const uint32_t tloc = warp * kWarpItems + lane * 16;  // this thread's first item in the tile
     const ff ex_h = s_exh, ex_l = s_exl;
     const uint32_t ex_c = s_exc;
-    const uint32_t light_before = tbase - ex_c;  // light items in tiles before this one
-    uint32_t oc = s_wc[warp];                    // heavy items of the tile before group v
-    float oh32 = 0.f, ol32 = 0.f;                // running local sums before group v
-    ff oh{0.f, 0.f}, ol{0.f, 0.f};
-    if constexpr (FFOUT) {
-        oh = s_fh[warp];
-        ol = s_fl[warp];
-    } else {
-        oh32 = s_wh[warp];
-        ol32 = s_wl[warp];
+    const uint32_t light_before = tbase - ex_c;   // light items in tiles before this one
+    uint32_t hc_loc = s_wc[warp] + s_lc[threadIdx.x];  // heavy items of the tile before the item
+    float rh32 = 0.f, rl32 = 0.f;
+    ff rh{0.f, 0.f}, rl{0.f, 0.f};
+    {
+        const float2 lh = s_lh[threadIdx.x], ll = s_ll[threadIdx.x];
+        if constexpr (FFOUT) {
+            rh = carry_add<true>(s_fh[warp], ff{lh.x, lh.y});
+            rl = carry_add<true>(s_fl[warp], ff{ll.x, ll.y});
+        } else {
+            rh32 = __fadd_rn(s_wh[warp], lh.x);
+            rl32 = __fadd_rn(s_wl[warp], ll.x);
+        }
     }
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-        {
-            const float4 q = s_x[(warp * kWarpItems + v * 128 + lane * 4) / 4];
-            x[v][0] = q.x;
-            x[v][1] = q.y;
-            x[v][2] = q.z;
-            x[v][3] = q.w;
-        }
-        uint32_t tcv = 0;
-        float thv = 0.f, tlv = 0.f;
-        ff fth{0.f, 0.f}, ftl{0.f, 0.f};
+    for (int j = 0; j < 4; ++j) {
+        const float4 q = s_x[park_slot(warp * 128 + lane * 4 + j)];
+        const float yv[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-            const float xv = x[v][c];
-            if (xv > pivot) {
-                ++tcv;
-                if constexpr (FFOUT)
-                    fth = ff_add_f(fth, xv);
-                else
-                    thv = __fadd_rn(thv, xv);
-            } else {
-                if constexpr (FFOUT)
-                    ftl = ff_add_f(ftl, xv);
-                else
-                    tlv = __fadd_rn(tlv, xv);
-            }
-        }
-        const uint32_t icv = warp_incl_u(tcv, lane);
-        const uint32_t ecv = __shfl_up_sync(0xffffffffu, icv, 1);
-        uint32_t rc = oc + (lane ? ecv : 0u);  // heavy items of the tile before this thread's
-        oc += __shfl_sync(0xffffffffu, icv, 31);
-        float rh = 0.f, rl = 0.f;
-        ff fr_h{0.f, 0.f}, fr_l{0.f, 0.f};
-        if constexpr (FFOUT) {
-            const ff ih = ff_warp_incl(fth, lane), il = ff_warp_incl(ftl, lane);
-            fr_h = carry_add<true>(oh, ff_shfl_up_excl(ih, lane));
-            fr_l = carry_add<true>(ol, ff_shfl_up_excl(il, lane));
-            oh = carry_add<true>(oh, ff_shfl(ih, 31));
-            ol = carry_add<true>(ol, ff_shfl(il, 31));
-        } else {
-            const float ih = warp_incl_f(thv, lane), il = warp_incl_f(tlv, lane);
-            const float eh = __shfl_up_sync(0xffffffffu, ih, 1);
-            const float el = __shfl_up_sync(0xffffffffu, il, 1);
-            rh = lane ? __fadd_rn(oh32, eh) : oh32;
-            rl = lane ? __fadd_rn(ol32, el) : ol32;
-            oh32 = __fadd_rn(oh32, __shfl_sync(0xffffffffu, ih, 31));
-            ol32 = __fadd_rn(ol32, __shfl_sync(0xffffffffu, il, 31));
-        }
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const uint32_t local = warp * kWarpItems + v * 128 + lane * 4 + c;
+            const uint32_t local = tloc + 4 * j + c;
             const uint32_t e = tbase + local;
             if (e < n) {
-                const float xv = x[v][c];
+                const float xv = yv[c];
                 uint32_t pos;
                 ff val;
                 if (xv > pivot) {
-                    pos = ex_c + rc;
+                    pos = ex_c + hc_loc;
                     if constexpr (FFOUT) {
-                        fr_h = ff_add_f(fr_h, xv);
-                        val = carry_add<true>(ex_h, fr_h);
+                        rh = ff_add_f(rh, xv);
+                        val = carry_add<true>(ex_h, rh);
                     } else {
-                        rh = __fadd_rn(rh, xv);
-                        val = {carry_apply<COMP>(ex_h, rh), 0.f};
+                        rh32 = __fadd_rn(rh32, xv);
+                        val = {carry_apply<COMP>(ex_h, rh32), 0.f};
                     }
-                    ++rc;
+                    ++hc_loc;
                 } else {
-                    pos = n - 1u - (light_before + (local - rc));
+                    pos = n - 1u - (light_before + (local - hc_loc));
                     if constexpr (FFOUT) {
-                        fr_l = ff_add_f(fr_l, xv);
-                        val = carry_add<true>(ex_l, fr_l);
+                        rl = ff_add_f(rl, xv);
+                        val = carry_add<true>(ex_l, rl);
                     } else {
-                        rl = __fadd_rn(rl, xv);
-                        val = {carry_apply<COMP>(ex_l, rl), 0.f};
+                        rl32 = __fadd_rn(rl32, xv);
+                        val = {carry_apply<COMP>(ex_l, rl32), 0.f};
                     }
                 }
                 if (pos < n) {  // always true unless a lookback wait gave up

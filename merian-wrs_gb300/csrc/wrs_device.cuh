@@ -140,6 +140,13 @@ __device__ __forceinline__ u128 fx_from_float(float x, int g) {
     return sh >= 24 ? static_cast<u128>(0) : static_cast<u128>(m >> sh);
 }
 
+// A float-float value hi + lo (hi >= 0, |lo| <= ulp(hi) / 2) on the grid; lo may be negative,
+// so its part enters in two's complement and the sum is again non-negative.
+__device__ __forceinline__ u128 fx_from_ff(ff v, int g) {
+    const u128 lo = fx_from_float(v.lo, g);  // magnitude (the sign bit is ignored)
+    return fx_from_float(v.hi, g) + (v.lo < 0.0f ? static_cast<u128>(0) - lo : lo);
+}
+
 __device__ __forceinline__ u128 shfl_xor_u128(u128 v, int m) {
     const unsigned long long lo = __shfl_xor_sync(0xffffffffu, static_cast<unsigned long long>(v), m);
     const unsigned long long hi =

@@ -264,6 +264,129 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample(const float* __re
     if (s < S) __stcs(out + s, res);
 }
 
+// ---- ITS without cooperative narrowing: the bisection's probe tree, top cached ----------
+//
+// Every non-cooperative search starts with x = 0, y = N - 1 and probes mid = x + (y - x) / 2,
+// so its first probes walk one implicit binary tree: node k (root 1; children 2k for
+// "T <= cmf[mid]" and 2k + 1 for "T > cmf[mid]") holds the range left by the branch
+// decisions spelled by the bits of k below its leading one.  Each CTA copies the probe
+// values of the top kItsTreeLevels levels into shared memory once, then runs the searches
+// -- unchanged probe sequence, so results are bit-identical to the plain bisection -- with
+// kItsPerThread searches interleaved per thread to keep several loads in flight.
+constexpr int kItsTreeLevels = 12;
+constexpr int kItsTreeNodes = 1 << kItsTreeLevels;  // nodes 1 .. 4095 (index 0 unused)
+constexpr int kItsPerThread = 4;
+constexpr int kItsGroup = kSampleThreads * kItsPerThread;
+constexpr int kItsMaxBlocks = 152 * 16;
+
+__device__ __forceinline__ void tree_range(uint32_t k, uint32_t last, uint32_t& x, uint32_t& y) {
+    x = 0;
+    y = last;
+    const int d = 31 - __clz(k);
+    for (int b = d - 1; b >= 0; --b) {
+        if (x >= y) return;
+        const uint32_t mid = x + ((y - x) >> 1);
+        if ((k >> b) & 1u)
+            x = mid + 1;
+        else
+            y = mid;
+    }
+}
+
+template <uint32_t RNG>
+__global__ __launch_bounds__(kSampleThreads) void k_its_sample_tree(const float* __restrict__ cmf,
+                                                                    uint32_t n, uint64_t S,
+                                                                    uint64_t seed, uint64_t offset,
+                                                                    uint32_t* __restrict__ out) {
+    __shared__ float s_tree[kItsTreeNodes];
+    const uint32_t last = n - 1u;
+    for (uint32_t k = threadIdx.x + 1; k < kItsTreeNodes; k += blockDim.x) {
+        uint32_t x, y;
+        tree_range(k, last, x, y);
+        s_tree[k] = x < y ? __ldg(cmf + x + ((y - x) >> 1)) : 0.0f;
+    }
+    __syncthreads();
+    const float total = __ldg(cmf + last);
+    for (uint64_t grp = blockIdx.x; grp * kItsGroup < S; grp += gridDim.x) {
+        const uint64_t s0 = grp * kItsGroup + threadIdx.x;
+        float t_hi[kItsPerThread];
+        int t_sgn[kItsPerThread];
+        uint32_t x[kItsPerThread], y[kItsPerThread], node[kItsPerThread];
+        if constexpr (RNG == RNG_REF) {
+            const uint32_t seed32 = static_cast<uint32_t>(seed);
+#pragma unroll
+            for (int v = 0; v < kItsPerThread; ++v) {
+                const uint32_t g = static_cast<uint32_t>(offset + s0 + v * kSampleThreads);
+                t_hi[v] = search_range_u(cmf, 0, last, unit_ref(wang_hash((seed32 ^ 0xA9EC5C80u) + g)));
+                t_sgn[v] = 0;
+            }
+        } else {
+            uint2 ks[10];
+            philox4x32_10_keys(seed, ks);
+#pragma unroll
+            for (int v = 0; v < kItsPerThread; ++v) {
+                const uint64_t g = offset + s0 + v * kSampleThreads;
+                const uint4 r = philox4x32_10(
+                    make_uint4(static_cast<uint32_t>(g), static_cast<uint32_t>(g >> 32), 0u, 0u), ks);
+                exact_target(r.x, total, t_hi[v], t_sgn[v]);
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < kItsPerThread; ++v) {
+            x[v] = 0;
+            y[v] = s0 + v * kSampleThreads < S ? last : 0u;
+            node[v] = 1;
+        }
+        // levels held in shared memory
+#pragma unroll 1
+        for (int l = 0; l < kItsTreeLevels; ++l) {
+#pragma unroll
+            for (int v = 0; v < kItsPerThread; ++v) {
+                if (x[v] < y[v]) {
+                    const uint32_t mid = x[v] + ((y[v] - x[v]) >> 1);
+                    const float c = s_tree[node[v]];
+                    const bool right = RNG == RNG_REF ? t_hi[v] > c
+                                                      : (t_hi[v] > c || (t_hi[v] == c && t_sgn[v] > 0));
+                    if (right) {
+                        x[v] = mid + 1;
+                        node[v] = 2 * node[v] + 1;
+                    } else {
+                        y[v] = mid;
+                        node[v] = 2 * node[v];
+                    }
+                }
+            }
+        }
+        // remaining levels from global memory, the searches' loads issued together
+        for (;;) {
+            float c[kItsPerThread];
+            bool any = false;
+#pragma unroll
+            for (int v = 0; v < kItsPerThread; ++v) {
+                any = any || x[v] < y[v];
+                c[v] = x[v] < y[v] ? __ldg(cmf + x[v] + ((y[v] - x[v]) >> 1)) : 0.0f;
+            }
+            if (!any) break;
+#pragma unroll
+            for (int v = 0; v < kItsPerThread; ++v) {
+                if (x[v] < y[v]) {
+                    const uint32_t mid = x[v] + ((y[v] - x[v]) >> 1);
+                    const bool right = RNG == RNG_REF
+                                           ? t_hi[v] > c[v]
+                                           : (t_hi[v] > c[v] || (t_hi[v] == c[v] && t_sgn[v] > 0));
+                    if (right)
+                        x[v] = mid + 1;
+                    else
+                        y[v] = mid;
+                }
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < kItsPerThread; ++v)
+            if (s0 + v * kSampleThreads < S) __stcs(out + s0 + v * kSampleThreads, x[v]);
+    }
+}
+
 cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, const uint2* table,
                                 uint32_t n, uint64_t S, uint64_t seed, uint64_t offset,
                                 uint32_t* out) {
@@ -304,15 +427,17 @@ cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool
     if (blocks == 0) return cudaSuccess;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
     const dim3 grid(static_cast<unsigned>(blocks));
-    if (rng == RNG_REF) {
-        if (coop == 0)
-            k_its_sample<RNG_REF, 0><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
-        else if (parray)
-            k_its_sample<RNG_REF, 2><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
+    if (coop == 0) {
+        const uint64_t groups = (S + kItsGroup - 1) / kItsGroup;
+        const unsigned tb = static_cast<unsigned>(groups < kItsMaxBlocks ? groups : kItsMaxBlocks);
+        if (rng == RNG_REF)
+            k_its_sample_tree<RNG_REF><<<tb, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, out);
         else
-            k_its_sample<RNG_REF, 1><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
+            k_its_sample_tree<RNG_PHILOX><<<tb, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, out);
+    } else if (parray) {
+        k_its_sample<RNG_REF, 2><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
     } else {
-        k_its_sample<RNG_PHILOX, 0><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
+        k_its_sample<RNG_REF, 1><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
     }
     return cudaGetLastError();
 }

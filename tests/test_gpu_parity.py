@@ -278,6 +278,21 @@ def test_its_sample_bit_exact(pkg, cuda, oracle, rng, coop, parray):
     assert np.array_equal(got, ref)
 
 
+@pytest.mark.parametrize("N", [1, 2, 3, 7, 4095, 4096, 4097, 8191, 8193, 70001])
+@pytest.mark.parametrize("rng", [RNG_REFERENCE, RNG_PHILOX4X32_10])
+def test_its_sample_edge_sizes(pkg, cuda, oracle, N, rng):
+    """The non-cooperative ITS sampler (probe tree cached in shared memory) at sizes around
+    the cached depth, with runs of zero weights (equal CMF values), equals the oracle."""
+    w = weights_uniform(N, N)
+    w[np.random.default_rng(N).random(N) < 0.2] = 0.0
+    w[0] = max(w[0], np.float32(0.5))
+    b = Built(pkg, w, pkg.ITSConfig(rng=rng))
+    S = 3 * 1024 + 77
+    got = b.sample(S, 7, 5)
+    ref = oracle.its_sample(b.cmf, S, 7, rng=rng, offset=5)
+    assert np.array_equal(got, ref)
+
+
 # ----------------------------------------------------------------- statistics ---
 
 @pytest.mark.parametrize("gen", list(GENS))
