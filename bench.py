@@ -746,6 +746,15 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
     rec("scan", timed(lambda: its.prefix_sum(stream, w, n, cmf, internals)), 8 * n, n, "weights")
     rec("its_sample", timed(lambda: its.its_sample(stream, cmf, n, s, 99, 0, samples)), 4 * s, s,
         "samples")
+    cp = W.WRS(W.CutpointConfig(128))
+    G = (n + 127) // 128
+    guide = torch.empty(G, dtype=torch.int32, device=w.device)
+    # guiding table: one lower-bound search per entry (reads ~1 sector per level, writes 4 B)
+    rec("cutpoint_guide", timed(lambda: cp.cutpoint_guide(stream, cmf, n, guide)), 4 * G, G,
+        "entries")
+    rec("cutpoint_sample",
+        timed(lambda: cp.cutpoint_sample(stream, cmf, n, guide, s, 99, 0, samples)), 4 * s, s,
+        "samples")
     assert not internals.status() & W.DEVICE_TIMEOUT
     return out
 

@@ -31,6 +31,9 @@
  *                                                               src/device/wrs/alias/psa/splitpack/inline/InlineSplitPack.hpp:105-150
  *   wrs_alias_sample              SampleAliasTable::run         src/device/wrs/alias/sampling/AliasTableSampling.hpp:75-84
  *   wrs_its_sample                InverseTransformSampling::run src/device/wrs/its/sampling/InverseTransformSampling.hpp
+ *   wrs_cutpoint_guide            CutpointGuidingTable::run     src/device/wrs/cutpoint/guiding_table/CutpointGuidingTable.hpp
+ *   wrs_cutpoint_sample           CutpointSampling::run         src/device/wrs/cutpoint/sampling/CutpointSampling.hpp
+ *                                 (Cutpoint::build / ::sample,  src/device/wrs/cutpoint/Cutpoint.hpp:108-158)
  *   wrs_batch_*                   no counterpart (the reference builds and samples one
  *                                 distribution per call)
  *
@@ -62,7 +65,7 @@ typedef enum wrs_status {
     WRS_ERR_OOM = 2,
     WRS_ERR_TIMEOUT = 3,         /* a lookback wait gave up (device status bit 1) */
     WRS_ERR_CUDA = 4,
-    WRS_ERR_NOT_IMPLEMENTED = 5, /* e.g. the Cutpoint method */
+    WRS_ERR_NOT_IMPLEMENTED = 5, /* e.g. a batch of a method other than the alias table */
     WRS_ERR_CAPACITY = 6         /* N larger than the buffers were created for */
 } wrs_status;
 
@@ -70,11 +73,12 @@ typedef enum wrs_status {
 typedef enum wrs_method {
     WRS_METHOD_ALIAS_TABLE = 0, /* AliasTable: PSA build + alias sampling */
     WRS_METHOD_ITS = 1,         /* ITS: decoupled scan + inverse transform sampling */
-    WRS_METHOD_CUTPOINT = 2     /* Cutpoint: not implemented */
+    WRS_METHOD_CUTPOINT = 2     /* Cutpoint: decoupled scan + guiding table + guided sampling */
 } wrs_method;
 
 typedef enum wrs_rng {
-    WRS_RNG_REFERENCE = 0,     /* the shaders' streams: Philox2x32-7 (alias), wang_hash (ITS) */
+    WRS_RNG_REFERENCE = 0,     /* the shaders' streams: Philox2x32-7 (alias), wang_hash (ITS,
+                                  Cutpoint) */
     WRS_RNG_PHILOX4X32_10 = 1  /* Philox4x32-10, key = seed, counter = sample index */
 } wrs_rng;
 
@@ -108,6 +112,9 @@ typedef struct wrs_config {
                                         (splitpack/inline/shader.comp:90,104), which at the end
                                         of the table can leave i + j < n and give the last
                                         light bucket extra mass; 0 = reference behaviour */
+    uint32_t guiding_entry_size;     /* Cutpoint: CutpointConfig::guidingEntrySize, weights per
+                                        guiding-table entry (table size ceil(N / this));
+                                        default 32 */
 } wrs_config;
 
 typedef struct wrs_alias_entry {
@@ -123,7 +130,8 @@ const char* wrs_status_string(wrs_status s);
 const char* wrs_last_error(void);
 
 /* Defaults: alias = PSA split size 2, partition elements on, coop 0, reference RNG, FP32
- * scan; ITS = coop 0, reference RNG, FP32 scan. */
+ * scan; ITS = coop 0, reference RNG, FP32 scan; Cutpoint = guiding entry size 32, reference
+ * RNG, FP32 scan. */
 wrs_status wrs_config_init(wrs_config* cfg, uint32_t method);
 
 wrs_status wrs_create(const wrs_config* cfg, wrs_handle** out);
@@ -150,7 +158,8 @@ wrs_status wrs_buffers_status(wrs_buffers* b, void* stream, uint32_t* device_sta
 
 /* Device views of the internals (valid while b lives). */
 const wrs_alias_entry* wrs_buffers_alias_table(const wrs_buffers* b);
-const float* wrs_buffers_cmf(const wrs_buffers* b);
+const float* wrs_buffers_cmf(const wrs_buffers* b);              /* ITS and Cutpoint */
+const uint32_t* wrs_buffers_guide_table(const wrs_buffers* b);   /* Cutpoint: ceil(N / entry) */
 const uint32_t* wrs_buffers_partition_indices(const wrs_buffers* b);
 const float* wrs_buffers_partition_prefix(const wrs_buffers* b);
 const float* wrs_buffers_partition_elements(const wrs_buffers* b);
@@ -181,6 +190,15 @@ wrs_status wrs_alias_sample(const wrs_handle* h, void* stream, const wrs_alias_e
                             uint32_t* samples);
 wrs_status wrs_its_sample(const wrs_handle* h, void* stream, const float* cmf, uint32_t n,
                           uint64_t s, uint64_t seed, uint64_t offset, uint32_t* samples);
+/* Cutpoint guiding table of a CMF: guide[k] = first index with cmf >= (total / G) * k for
+ * k < G = ceil(n / guiding_entry_size) (cutpoint/guiding_table/shader.comp:40-55). */
+wrs_status wrs_cutpoint_guide(const wrs_handle* h, void* stream, const float* cmf, uint32_t n,
+                              uint32_t* guide);
+/* Cutpoint sampling (cutpoint/sampling/shader.comp:100-140): each group of 32 consecutive
+ * samples picks one guiding-table cell, each sample bisects inside it. */
+wrs_status wrs_cutpoint_sample(const wrs_handle* h, void* stream, const float* cmf, uint32_t n,
+                               const uint32_t* guide, uint64_t s, uint64_t seed,
+                               uint64_t offset, uint32_t* samples);
 /* Inclusive prefix sum (the scan of wrs_prefix_sum) that allocates no device memory, for
  * callers that cannot call cudaMalloc -- e.g. code running under a host application whose
  * pool already holds all device memory, code that must not take the device-wide

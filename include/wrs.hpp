@@ -2,8 +2,8 @@
 // (src/device/wrs/WRS.hpp:14-172) on top of the C ABI in wrs.h.
 //
 //   reference                                         here
-//   WRSConfig = variant<ITS::Config, AliasTable::Config, ...>   wrs::WRSConfig (+ AliasTableConfig(),
-//                                                               ITSConfig() factories)
+//   WRSConfig = variant<ITS::Config, AliasTable::Config,        wrs::WRSConfig (+ AliasTableConfig(),
+//                       Cutpoint::Config>                       ITSConfig(), CutpointConfig() factories)
 //   WRSBuffers::allocate(alloc, mapping, N, S, config)          wrs::WRSBuffers::allocate(wrs, N, weights, samples)
 //   WRS(context, shaderCompiler, config)                        wrs::WRS(config)
 //   WRS::build(cmd, buffers, N, profiler)                       wrs::WRS::build(stream, buffers, N)
@@ -52,6 +52,13 @@ inline WRSConfig ITSConfig(uint32_t coop_size = 0, bool parray = false) {
     check(wrs_config_init(&c, WRS_METHOD_ITS));
     c.coop_size = coop_size;
     c.its_parray = parray ? 1u : 0u;
+    return c;
+}
+
+inline WRSConfig CutpointConfig(uint32_t guiding_entry_size = 32) {
+    WRSConfig c;
+    check(wrs_config_init(&c, WRS_METHOD_CUTPOINT));
+    c.guiding_entry_size = guiding_entry_size;
     return c;
 }
 

@@ -6,6 +6,6 @@ The directory name contains a hyphen, so load it with
     importlib.import_module("merian-wrs_gb300")
 """
 from . import wrs  # noqa: F401
-from .wrs import (AliasTableConfig, Batch, ITSConfig, WRS, WRSBuffers, WRSConfig,  # noqa: F401
-                  WRSError)
+from .wrs import (AliasTableConfig, Batch, CutpointConfig, ITSConfig, WRS,  # noqa: F401
+                  WRSBuffers, WRSConfig, WRSError)
 from .build import build  # noqa: F401

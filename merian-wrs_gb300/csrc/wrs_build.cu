@@ -66,6 +66,11 @@ __device__ __forceinline__ void load_tile(const float* __restrict__ w, uint32_t 
 #endif
 constexpr int kPartMinBlocks = WRS_PART_MIN_BLOCKS;
 
+// staged-output array index of output slot q: one padding word per 32 spreads the scattered
+// stores of a warp over the banks; consecutive slots stay conflict-free for the write-out
+constexpr int kStageWords = kTileItems + kTileItems / 32;
+__device__ __forceinline__ uint32_t stage_idx(uint32_t q) { return q + (q >> 5); }
+
 // float4 slot of chunk q (items 4q..4q+3) of a tile parked in shared memory: the XOR
 // swizzle spreads both the coalesced order (q = 32v + lane per warp) and the transposed order
 // (q = 4 lane + j) over all eight 16-byte bank groups (4 wavefronts per warp access).
@@ -384,10 +389,17 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
     __shared__ ff s_fh[kTileWarps], s_fl[kTileWarps];     // local float-float sums (FFOUT)
     __shared__ ff s_exh, s_exl;
     __shared__ uint32_t s_exc, s_aggc;
-    __shared__ float4 s_x[kTileItems / 4];  // the tile, swizzled (park_slot)
-
-    __shared__ uint32_t s_lc[kTileThreads];                  // lane-exclusive heavy counts
-    __shared__ float2 s_lh[kTileThreads], s_ll[kTileThreads];  // lane-exclusive local sums
+    // the parked tile (swizzled, park_slot), then the staged outputs by output slot: the tile's
+    // heavy items take slots [0, heavy) in order, its light items slots 4095, 4094, ... in order,
+    // so both runs are written out as contiguous, coalesced segments (stage_idx pads 1 word per
+    // 32).  Until phase C the staging area holds the lane-exclusive offsets of phase A.
+    __shared__ __align__(16) unsigned char s_raw[kTileItems * 4 + kStageWords * 2 + kStageWords * 4];
+    float4* const s_x = reinterpret_cast<float4*>(s_raw);
+    uint16_t* const s_key = reinterpret_cast<uint16_t*>(s_raw + kTileItems * 4);
+    float* const s_val = reinterpret_cast<float*>(s_raw + kTileItems * 4 + kStageWords * 2);
+    uint32_t* const s_lc = reinterpret_cast<uint32_t*>(s_val);                 // lane-exclusive counts
+    float2* const s_lh = reinterpret_cast<float2*>(s_val + kTileThreads);      // lane-exclusive sums
+    float2* const s_ll = reinterpret_cast<float2*>(s_val + 3 * kTileThreads);
 
     PartState* cur;
     const uint32_t tile = lookback_begin(a.lb, a.states, a.cap_tiles, cur);
@@ -564,7 +576,68 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
     }
     __syncthreads();
 
-    // ---- phase C: running sums over the thread's items, scatter
+    // ---- phase C: running sums over the thread's items, staged by output slot, written out
+    const uint32_t tbase = lt * kTileItems;
+    const uint32_t tloc = warp * kWarpItems + lane * 16;  // this thread's first item in the tile
+    const ff ex_h = s_exh, ex_l = s_exl;
+    const uint32_t ex_c = s_exc, agg_c = s_aggc;
+    const uint32_t m = n - tbase < static_cast<uint32_t>(kTileItems) ? n - tbase : kTileItems;
+    const uint32_t hc0 = s_wc[warp] + s_lc[threadIdx.x];  // heavy items of the tile before ours
+    float rh32 = 0.f, rl32 = 0.f;
+    ff rh0{0.f, 0.f}, rl0{0.f, 0.f};
+    {
+        const float2 lh = s_lh[threadIdx.x], ll = s_ll[threadIdx.x];
+        if constexpr (FFOUT) {
+            rh0 = carry_add<true>(s_fh[warp], ff{lh.x, lh.y});
+            rl0 = carry_add<true>(s_fl[warp], ff{ll.x, ll.y});
+        } else {
+            rh32 = __fadd_rn(s_wh[warp], lh.x);
+            rl32 = __fadd_rn(s_wl[warp], ll.x);
+        }
+    }
+    __syncthreads();  // the lane offsets are read; the staging area is free
+    {
+        uint32_t hc = hc0;
+        ff rh = rh0, rl = rl0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float4 q = s_x[park_slot(warp * 128 + lane * 4 + j)];
+            const float yv[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const uint32_t local = tloc + 4 * j + c;
+                if (local < m) {
+                    const float xv = yv[c];
+                    uint32_t slot;
+                    float hi;
+                    if (xv > pivot) {
+                        slot = hc++;
+                        if constexpr (FFOUT) {
+                            rh = ff_add_f(rh, xv);
+                            hi = carry_add<true>(ex_h, rh).hi;
+                        } else {
+                            rh32 = __fadd_rn(rh32, xv);
+                            hi = carry_apply<COMP>(ex_h, rh32);
+                        }
+                    } else {
+                        slot = kTileItems - 1u - (local - hc);
+                        if constexpr (FFOUT) {
+                            rl = ff_add_f(rl, xv);
+                            hi = carry_add<true>(ex_l, rl).hi;
+                        } else {
+                            rl32 = __fadd_rn(rl32, xv);
+                            hi = carry_apply<COMP>(ex_l, rl32);
+                        }
+                    }
+                    s_key[stage_idx(slot)] = static_cast<uint16_t>(local);
+                    s_val[stage_idx(slot)] = hi;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // write-out: slot q < agg_c -> heavy position ex_c + q; slot q >= 4096 - light -> light
+    // rank 4095 - q at position n - 1 - (light items before the tile) - rank
     uint32_t* idx_out = a.idx;
     float* prefix_out = a.prefix;
     float* elems_out = a.elems;
@@ -576,63 +649,50 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
         if (elems_out) elems_out += base;
         if (prefix_lo_out) prefix_lo_out += base;
     }
-    const uint32_t tbase = lt * kTileItems;
-    const uint32_t tloc = warp * kWarpItems + lane * 16;  // this thread's first item in the tile
-    const ff ex_h = s_exh, ex_l = s_exl;
-    const uint32_t ex_c = s_exc;
-    const uint32_t light_before = tbase - ex_c;   // light items in tiles before this one
-    uint32_t hc_loc = s_wc[warp] + s_lc[threadIdx.x];  // heavy items of the tile before the item
-    float rh32 = 0.f, rl32 = 0.f;
-    ff rh{0.f, 0.f}, rl{0.f, 0.f};
-    {
-        const float2 lh = s_lh[threadIdx.x], ll = s_ll[threadIdx.x];
-        if constexpr (FFOUT) {
-            rh = carry_add<true>(s_fh[warp], ff{lh.x, lh.y});
-            rl = carry_add<true>(s_fl[warp], ff{ll.x, ll.y});
-        } else {
-            rh32 = __fadd_rn(s_wh[warp], lh.x);
-            rl32 = __fadd_rn(s_wl[warp], ll.x);
-        }
+    const uint32_t light_top = kTileItems - (m - agg_c);      // first light slot
+    const uint32_t light_base = n - 1u - (tbase - ex_c) - (kTileItems - 1u);  // position of slot 0
+    const float* s_xf = reinterpret_cast<const float*>(s_x);
+    for (uint32_t q = threadIdx.x; q < static_cast<uint32_t>(kTileItems); q += kTileThreads) {
+        const bool heavy = q < agg_c;
+        if (!heavy && q < light_top) continue;
+        const uint32_t pos = heavy ? ex_c + q : light_base + q;
+        if (pos >= n) continue;  // only after a lookback wait gave up
+        const uint32_t local = s_key[stage_idx(q)];
+        idx_out[pos] = tbase + local;
+        prefix_out[pos] = s_val[stage_idx(q)];
+        if (elems_out) elems_out[pos] = s_xf[park_slot(local >> 2) * 4 + (local & 3)];
     }
+    if constexpr (FFOUT) {
+        // second round for the low words: the same running sums, staged again
+        __syncthreads();
+        uint32_t hc = hc0;
+        ff rh = rh0, rl = rl0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const float4 q = s_x[park_slot(warp * 128 + lane * 4 + j)];
-        const float yv[4] = {q.x, q.y, q.z, q.w};
+        for (int j = 0; j < 4; ++j) {
+            const float4 q = s_x[park_slot(warp * 128 + lane * 4 + j)];
+            const float yv[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const uint32_t local = tloc + 4 * j + c;
-            const uint32_t e = tbase + local;
-            if (e < n) {
-                const float xv = yv[c];
-                uint32_t pos;
-                ff val;
-                if (xv > pivot) {
-                    pos = ex_c + hc_loc;
-                    if constexpr (FFOUT) {
+            for (int c = 0; c < 4; ++c) {
+                const uint32_t local = tloc + 4 * j + c;
+                if (local < m) {
+                    const float xv = yv[c];
+                    if (xv > pivot) {
                         rh = ff_add_f(rh, xv);
-                        val = carry_add<true>(ex_h, rh);
+                        s_val[stage_idx(hc++)] = carry_add<true>(ex_h, rh).lo;
                     } else {
-                        rh32 = __fadd_rn(rh32, xv);
-                        val = {carry_apply<COMP>(ex_h, rh32), 0.f};
-                    }
-                    ++hc_loc;
-                } else {
-                    pos = n - 1u - (light_before + (local - hc_loc));
-                    if constexpr (FFOUT) {
                         rl = ff_add_f(rl, xv);
-                        val = carry_add<true>(ex_l, rl);
-                    } else {
-                        rl32 = __fadd_rn(rl32, xv);
-                        val = {carry_apply<COMP>(ex_l, rl32), 0.f};
+                        s_val[stage_idx(kTileItems - 1u - (local - hc))] = carry_add<true>(ex_l, rl).lo;
                     }
-                }
-                if (pos < n) {  // always true unless a lookback wait gave up
-                    idx_out[pos] = e;
-                    prefix_out[pos] = val.hi;
-                    if constexpr (FFOUT) prefix_lo_out[pos] = val.lo;
-                    if (elems_out) elems_out[pos] = xv;
                 }
             }
+        }
+        __syncthreads();
+        for (uint32_t q = threadIdx.x; q < static_cast<uint32_t>(kTileItems); q += kTileThreads) {
+            const bool heavy = q < agg_c;
+            if (!heavy && q < light_top) continue;
+            const uint32_t pos = heavy ? ex_c + q : light_base + q;
+            if (pos >= n) continue;
+            prefix_lo_out[pos] = s_val[stage_idx(q)];
         }
     }
     if (threadIdx.x == 0 && lt == tiles_for(n) - 1u) ctrl->heavy_count = ex_c + s_aggc;

@@ -6,7 +6,9 @@
 //   alias build : k_total_mass -> k_prefix_partition -> k_split_pack
 //                 (PSA::run, src/device/wrs/alias/psa/PSA.hpp:170-237)
 //   ITS build   : k_scan (ITS::build, src/device/wrs/its/ITS.hpp:90-108)
-//   sample      : k_alias_sample | k_its_sample (WRS::sample, src/device/wrs/WRS.hpp:145-168)
+//   Cutpoint    : k_scan -> k_cutpoint_guide (Cutpoint::build, src/device/wrs/cutpoint/Cutpoint.hpp:108-138)
+//   sample      : k_alias_sample | k_its_sample | k_cutpoint_sample
+//                 (WRS::sample, src/device/wrs/WRS.hpp:145-168)
 //   batch       : k_batch_maps (wrs_batch_set), then the same three build kernels and the
 //                 alias sampler over all distributions of a batch, one launch each
 // Stream order replaces the reference's pipeline barriers.
@@ -41,6 +43,7 @@ struct wrs_buffers {
     float* prefix_lo = nullptr;
     uint2* table = nullptr;
     float* cmf = nullptr;
+    uint32_t* guide = nullptr;
 };
 
 namespace {
@@ -69,7 +72,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct Layout {
     size_t ctrl, partials, part_states, scan_states, idx, prefix, elems, prefix_lo, table, cmf,
-        total;
+        guide, total;
 };
 
 Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
@@ -98,6 +101,8 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
         L.table = take(sizeof(uint2) * static_cast<size_t>(max_n));
     } else {
         L.cmf = take(sizeof(float) * static_cast<size_t>(max_n));
+        if (cfg.method == WRS_METHOD_CUTPOINT)
+            L.guide = take(sizeof(uint32_t) * guide_entries(max_n, cfg.guiding_entry_size));
     }
     L.total = off;
     return L;
@@ -111,10 +116,14 @@ size_t zeroed_bytes(const wrs_config& cfg, uint32_t max_n) {
 
 wrs_status check_config(const wrs_config* c) {
     if (!c) return fail(WRS_ERR_INVALID_ARG, "config is NULL");
-    if (c->method == WRS_METHOD_CUTPOINT)
-        return fail(WRS_ERR_NOT_IMPLEMENTED, "the Cutpoint method is not implemented");
-    if (c->method != WRS_METHOD_ALIAS_TABLE && c->method != WRS_METHOD_ITS)
+    if (c->method != WRS_METHOD_ALIAS_TABLE && c->method != WRS_METHOD_ITS &&
+        c->method != WRS_METHOD_CUTPOINT)
         return fail(WRS_ERR_INVALID_ARG, "unknown method");
+    if (c->method == WRS_METHOD_CUTPOINT && c->guiding_entry_size == 0)
+        return fail(WRS_ERR_INVALID_ARG, "guiding_entry_size must be >= 1");
+    if (c->method == WRS_METHOD_CUTPOINT && c->coop_size != 0)
+        return fail(WRS_ERR_INVALID_ARG,
+                    "the Cutpoint method has no cooperative-size setting (coop_size must be 0)");
     if (c->method == WRS_METHOD_ALIAS_TABLE && c->split_size == 0)
         return fail(WRS_ERR_INVALID_ARG, "split_size must be >= 1");
     if (c->rng > WRS_RNG_PHILOX4X32_10) return fail(WRS_ERR_INVALID_ARG, "unknown rng");
@@ -168,6 +177,7 @@ wrs_status wrs_config_init(wrs_config* cfg, uint32_t method) {
     cfg->scan_precision = WRS_SCAN_FP32;
     cfg->split_residual_f64 = 0;
     cfg->split_full_light = 0;
+    cfg->guiding_entry_size = 32;
     return check_config(cfg);
 }
 
@@ -224,6 +234,7 @@ wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers**
         b->table = reinterpret_cast<uint2*>(p + L.table);
     } else {
         b->cmf = reinterpret_cast<float*>(p + L.cmf);
+        if (h->cfg.method == WRS_METHOD_CUTPOINT) b->guide = reinterpret_cast<uint32_t*>(p + L.guide);
     }
     e = cudaMemset(b->base, 0, zeroed_bytes(h->cfg, max_n));
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -339,6 +350,33 @@ wrs_status wrs_its_sample(const wrs_handle* h, void* stream, const float* cmf, u
     return WRS_OK;
 }
 
+wrs_status wrs_cutpoint_guide(const wrs_handle* h, void* stream, const float* cmf, uint32_t n,
+                              uint32_t* guide) {
+    if (!h || !cmf || !guide) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    if (n == 0 || n > kMaxN) return fail(WRS_ERR_INVALID_ARG, "n out of range");
+    if (h->cfg.method != WRS_METHOD_CUTPOINT)
+        return fail(WRS_ERR_INVALID_ARG, "the handle is not configured for the Cutpoint method");
+    WRS_CUDA(launch_cutpoint_guide(as_stream(stream), cmf, n,
+                                   guide_entries(n, h->cfg.guiding_entry_size), guide),
+             "guiding table");
+    return WRS_OK;
+}
+
+wrs_status wrs_cutpoint_sample(const wrs_handle* h, void* stream, const float* cmf, uint32_t n,
+                               const uint32_t* guide, uint64_t s, uint64_t seed, uint64_t offset,
+                               uint32_t* samples) {
+    if (!h || !cmf || !guide || (!samples && s)) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    if (n == 0 || n > kMaxN) return fail(WRS_ERR_INVALID_ARG, "n out of range");
+    if (h->cfg.method != WRS_METHOD_CUTPOINT)
+        return fail(WRS_ERR_INVALID_ARG, "the handle is not configured for the Cutpoint method");
+    if (s == 0) return WRS_OK;
+    WRS_CUDA(launch_cutpoint_sample(as_stream(stream), h->cfg.rng, cmf, n, guide,
+                                    guide_entries(n, h->cfg.guiding_entry_size), s, seed, offset,
+                                    samples),
+             "cutpoint sample");
+    return WRS_OK;
+}
+
 wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, uint32_t n,
                      wrs_buffers* b) {
     if (!h || !weights) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
@@ -348,9 +386,13 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
         return fail(WRS_ERR_INVALID_ARG, "buffers were created for another method");
     const cudaStream_t st = as_stream(stream);
     const bool comp = compensated(h);
-    if (h->cfg.method == WRS_METHOD_ITS) {
+    if (h->cfg.method != WRS_METHOD_ALIAS_TABLE) {
         WRS_CUDA(launch_scan(st, comp, weights, n, b->cmf, b->ctrl, b->scan_states, b->cap_tiles),
                  "ITS build");
+        if (h->cfg.method == WRS_METHOD_CUTPOINT)
+            WRS_CUDA(launch_cutpoint_guide(st, b->cmf, n, guide_entries(n, h->cfg.guiding_entry_size),
+                                           b->guide),
+                     "guiding table");
         return WRS_OK;
     }
     if (h->cfg.use_partition_elements && !b->elems)
@@ -379,6 +421,8 @@ wrs_status wrs_sample_at(const wrs_handle* h, void* stream, const wrs_buffers* b
         return fail(WRS_ERR_INVALID_ARG, "buffers were created for another method");
     if (h->cfg.method == WRS_METHOD_ITS)
         return wrs_its_sample(h, stream, b->cmf, n, s, seed, offset, samples);
+    if (h->cfg.method == WRS_METHOD_CUTPOINT)
+        return wrs_cutpoint_sample(h, stream, b->cmf, n, b->guide, s, seed, offset, samples);
     return wrs_alias_sample(h, stream, reinterpret_cast<const wrs_alias_entry*>(b->table), n, s,
                             seed, offset, samples);
 }
@@ -440,6 +484,7 @@ const wrs_alias_entry* wrs_buffers_alias_table(const wrs_buffers* b) {
     return b ? reinterpret_cast<const wrs_alias_entry*>(b->table) : nullptr;
 }
 const float* wrs_buffers_cmf(const wrs_buffers* b) { return b ? b->cmf : nullptr; }
+const uint32_t* wrs_buffers_guide_table(const wrs_buffers* b) { return b ? b->guide : nullptr; }
 const uint32_t* wrs_buffers_partition_indices(const wrs_buffers* b) { return b ? b->idx : nullptr; }
 const float* wrs_buffers_partition_prefix(const wrs_buffers* b) { return b ? b->prefix : nullptr; }
 const float* wrs_buffers_partition_elements(const wrs_buffers* b) { return b ? b->elems : nullptr; }

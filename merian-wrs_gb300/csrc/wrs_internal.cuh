@@ -126,6 +126,12 @@ cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool
                               const float* cmf, uint32_t n, uint64_t s, uint64_t seed,
                               uint64_t offset, uint32_t* out);
 
+cudaError_t launch_cutpoint_guide(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
+                                  uint32_t* guide);
+cudaError_t launch_cutpoint_sample(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
+                                   const uint32_t* guide, uint32_t G, uint64_t S, uint64_t seed,
+                                   uint64_t offset, uint32_t* out);
+
 // batched forms (one launch each for all distributions of the batch)
 cudaError_t launch_batch_maps(cudaStream_t st, const DistDesc* dist, uint32_t count,
                               uint32_t* tile_map, uint32_t* split_map, uint32_t* sample_map,
@@ -154,5 +160,9 @@ __host__ __device__ inline uint32_t split_blocks_for(uint32_t n, uint32_t split_
     return (splits_for(n, split_size) + kSplitPack - 1) / kSplitPack;
 }
 __host__ __device__ inline uint64_t alias_blocks_for(uint64_t s) { return (s + kAliasPerBlock - 1) / kAliasPerBlock; }
+// guiding-table entries of the Cutpoint method (cutpoint/Cutpoint.hpp:72-73)
+__host__ __device__ inline uint32_t guide_entries(uint32_t n, uint32_t entry_size) {
+    return static_cast<uint32_t>((static_cast<uint64_t>(n) + entry_size - 1) / entry_size);
+}
 
 }  // namespace wrs

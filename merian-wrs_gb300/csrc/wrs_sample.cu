@@ -387,6 +387,78 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_tree(const float*
     }
 }
 
+// ---- Cutpoint (guiding table) -----------------------------------------------------------
+
+// cutpoint/guiding_table/shader.comp:40-55: entry k = lower bound of (total / G) * k over the
+// whole CMF, with the shader's FP32 step and probe sequence.
+__global__ __launch_bounds__(kSampleThreads) void k_cutpoint_guide(const float* __restrict__ cmf,
+                                                                   uint32_t n, uint32_t G,
+                                                                   uint32_t* __restrict__ guide) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= G) return;
+    const float total = __ldg(cmf + n - 1u);
+    const float step = __fdiv_rn(total, __uint2float_rn(G));
+    guide[k] = bisect(cmf, 0, n - 1u, __fmul_rn(step, __uint2float_rn(k)));
+}
+
+// cutpoint/sampling/shader.comp:100-140.  The subgroup's elected lane (the first sample of the
+// aligned group of 32) draws u1, which picks guiding cell k = min(u1 * G, G - 1); the search
+// range is [guide[k], guide[k + 1]] (up to N - 1 for the last cell), and every sample bisects
+// it for u2 drawn inside the cell's CMF range.  RNG_REF: u1 = wang_hash(seed + g0), u2 =
+// wang_hash((seed ^ 0x79145147) + g) as the shader; RNG_PHILOX: u1 = x0 of the group's first
+// sample, u2 = x1 of the sample (Philox4x32-10, counter = sample index).
+template <uint32_t RNG>
+__global__ __launch_bounds__(kSampleThreads) void k_cutpoint_sample(
+    const float* __restrict__ cmf, uint32_t n, const uint32_t* __restrict__ guide, uint32_t G,
+    uint64_t S, uint64_t seed, uint64_t offset, uint32_t* __restrict__ out) {
+    const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const uint64_t g = offset + s, g0 = offset + (s & ~31ull);
+    float u1, uu;
+    if constexpr (RNG == RNG_REF) {
+        const uint32_t seed32 = static_cast<uint32_t>(seed);
+        u1 = unit_ref(wang_hash(seed32 + static_cast<uint32_t>(g0)));
+        uu = unit_ref(wang_hash((seed32 ^ 0x79145147u) + static_cast<uint32_t>(g)));
+    } else {
+        uint2 ks[10];
+        philox4x32_10_keys(seed, ks);
+        const uint4 r0 = philox4x32_10(
+            make_uint4(static_cast<uint32_t>(g0), static_cast<uint32_t>(g0 >> 32), 0u, 0u), ks);
+        const uint4 r = philox4x32_10(
+            make_uint4(static_cast<uint32_t>(g), static_cast<uint32_t>(g >> 32), 0u, 0u), ks);
+        u1 = unit_ref(r0.x);
+        uu = unit_ref(r.y);
+    }
+    uint32_t k = __float2uint_rz(__fmul_rn(u1, __uint2float_rn(G)));
+    k = k < G - 1u ? k : G - 1u;
+    const uint32_t x = __ldg(guide + k);
+    const uint32_t y = k != G - 1u ? __ldg(guide + k + 1u) : n - 1u;
+    const float u2 = search_range_u(cmf, x, y, uu);
+    __stcs(out + s, bisect(cmf, x, y, u2));
+}
+
+cudaError_t launch_cutpoint_guide(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
+                                  uint32_t* guide) {
+    const uint32_t blocks = (G + kSampleThreads - 1) / kSampleThreads;
+    k_cutpoint_guide<<<blocks, kSampleThreads, 0, st>>>(cmf, n, G, guide);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cutpoint_sample(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
+                                   const uint32_t* guide, uint32_t G, uint64_t S, uint64_t seed,
+                                   uint64_t offset, uint32_t* out) {
+    const uint64_t blocks = (S + kSampleThreads - 1) / kSampleThreads;
+    if (blocks == 0) return cudaSuccess;
+    if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
+    if (rng == RNG_REF)
+        k_cutpoint_sample<RNG_REF><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
+            cmf, n, guide, G, S, seed, offset, out);
+    else
+        k_cutpoint_sample<RNG_PHILOX><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
+            cmf, n, guide, G, S, seed, offset, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, const uint2* table,
                                 uint32_t n, uint64_t S, uint64_t seed, uint64_t offset,
                                 uint32_t* out) {

@@ -43,7 +43,7 @@ class WRSError(RuntimeError):
 class _Config(C.Structure):
     _fields_ = [(n, C.c_uint32) for n in (
         "method", "split_size", "use_partition_elements", "coop_size", "its_parray", "rng",
-        "scan_precision", "split_residual_f64", "split_full_light")]
+        "scan_precision", "split_residual_f64", "split_full_light", "guiding_entry_size")]
 
 
 class ServerConfig(C.Structure):
@@ -100,6 +100,9 @@ def lib() -> C.CDLL:
             "wrs_buffers_status": (i32, [vp, vp, C.POINTER(u32)]),
             "wrs_buffers_alias_table": (vp, [vp]),
             "wrs_buffers_cmf": (vp, [vp]),
+            "wrs_buffers_guide_table": (vp, [vp]),
+            "wrs_cutpoint_guide": (i32, [vp, vp, vp, u32, vp]),
+            "wrs_cutpoint_sample": (i32, [vp, vp, vp, u32, vp, u64, u64, u64, vp]),
             "wrs_buffers_partition_indices": (vp, [vp]),
             "wrs_buffers_partition_prefix": (vp, [vp]),
             "wrs_buffers_partition_elements": (vp, [vp]),
@@ -178,11 +181,13 @@ class WRSConfig:
     scan_precision: int = SCAN_FP32
     split_residual_f64: bool = False
     split_full_light: bool = False
+    guiding_entry_size: int = 32
 
     def c(self) -> _Config:
         return _Config(self.method, self.split_size, int(self.use_partition_elements),
                        self.coop_size, int(self.its_parray), self.rng, self.scan_precision,
-                       int(self.split_residual_f64), int(self.split_full_light))
+                       int(self.split_residual_f64), int(self.split_full_light),
+                       self.guiding_entry_size)
 
     def split_flags(self) -> int:
         """The oracle's split flags for this configuration."""
@@ -193,6 +198,8 @@ class WRSConfig:
             coop = f"-COOP-{self.coop_size}-{'PARRAY' if self.its_parray else 'BINARY'}" \
                 if self.coop_size else ""
             return f"ITS{coop}"
+        if self.method == METHOD_CUTPOINT:
+            return f"Cutpoint-{self.guiding_entry_size}"
         return f"AliasTable-PSA-split{self.split_size}-coop{self.coop_size}"
 
 
@@ -206,6 +213,11 @@ def AliasTableConfig(split_size: int = 2, use_partition_elements: bool = True,
 def ITSConfig(coop_size: int = 0, parray: bool = False, **kw) -> WRSConfig:
     """ITSConfig(DecoupledPrefixSumConfig(), InverseTransformSamplingConfig(512, coop, parray))."""
     return WRSConfig(METHOD_ITS, coop_size=coop_size, its_parray=parray, **kw)
+
+
+def CutpointConfig(guiding_entry_size: int = 32, **kw) -> WRSConfig:
+    """CutpointConfig(DecoupledPrefixSumConfig(), guidingEntrySize)."""
+    return WRSConfig(METHOD_CUTPOINT, guiding_entry_size=guiding_entry_size, **kw)
 
 
 class Handle:
@@ -251,6 +263,7 @@ class Internals:
         return {
             "alias_table": L.wrs_buffers_alias_table(self.ptr),
             "cmf": L.wrs_buffers_cmf(self.ptr),
+            "guide_table": L.wrs_buffers_guide_table(self.ptr),
             "partition_indices": L.wrs_buffers_partition_indices(self.ptr),
             "partition_prefix": L.wrs_buffers_partition_prefix(self.ptr),
             "partition_elements": L.wrs_buffers_partition_elements(self.ptr),
@@ -324,6 +337,14 @@ class WRS:
     def its_sample(self, stream, cmf, N, S, seed, offset, out) -> None:
         check(lib().wrs_its_sample(self.handle.ptr, _stream_ptr(stream), _dev_ptr(cmf), N, S,
                                    seed, offset, _dev_ptr(out)))
+
+    def cutpoint_guide(self, stream, cmf, N, guide) -> None:
+        check(lib().wrs_cutpoint_guide(self.handle.ptr, _stream_ptr(stream), _dev_ptr(cmf), N,
+                                       _dev_ptr(guide)))
+
+    def cutpoint_sample(self, stream, cmf, N, guide, S, seed, offset, out) -> None:
+        check(lib().wrs_cutpoint_sample(self.handle.ptr, _stream_ptr(stream), _dev_ptr(cmf), N,
+                                        _dev_ptr(guide), S, seed, offset, _dev_ptr(out)))
 
 
 class DistDesc(C.Structure):

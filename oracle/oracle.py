@@ -73,6 +73,8 @@ class Oracle:
                 "wrso_psa_build": (None, [vp, u32, u32, i32, i32, vp, vp, vp]),
                 "wrso_alias_sample": (None, [vp, u32, u64, u64, u64, u32, u32, i32, vp]),
                 "wrso_its_sample": (None, [vp, u32, u64, u64, u64, u32, u32, i32, i32, vp]),
+                "wrso_cutpoint_guide": (None, [vp, u32, u32, vp]),
+                "wrso_cutpoint_sample": (None, [vp, u32, vp, u32, u64, u64, u64, u32, i32, vp]),
                 "wrso_histogram": (None, [vp, u64, u32, vp]),
                 "wrso_chi_square": (f64, [vp, vp, u32, u64]),
                 "wrso_chi_square_binned": (f64, [vp, vp, u32, u64, f64, vp]),
@@ -201,6 +203,21 @@ class Oracle:
         out = np.empty(S, np.uint32)
         self.lib.wrso_its_sample(_ptr(cmf), cmf.size, S, seed, offset, rng, coop, int(parray),
                                  nthreads, _ptr(out))
+        return out
+
+    def cutpoint_guide(self, cmf, entry_size: int):
+        cmf = np.ascontiguousarray(cmf, np.float32)
+        G = (cmf.size + entry_size - 1) // entry_size
+        guide = np.empty(G, np.uint32)
+        self.lib.wrso_cutpoint_guide(_ptr(cmf), cmf.size, G, _ptr(guide))
+        return guide
+
+    def cutpoint_sample(self, cmf, guide, S, seed, rng=RNG_REFERENCE, offset=0, nthreads=1):
+        cmf = np.ascontiguousarray(cmf, np.float32)
+        guide = np.ascontiguousarray(guide, np.uint32)
+        out = np.empty(S, np.uint32)
+        self.lib.wrso_cutpoint_sample(_ptr(cmf), cmf.size, _ptr(guide), guide.size, S, seed,
+                                      offset, rng, nthreads, _ptr(out))
         return out
 
     # -- statistics -------------------------------------------------------------

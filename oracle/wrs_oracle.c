@@ -18,6 +18,8 @@
  *                           K = N / splitSize from .../inline/InlineSplitPack.hpp:116
  *   alias sampling          src/device/wrs/alias/sampling/shader.comp:68-111
  *   ITS sampling            src/device/wrs/its/sampling/shader.comp:80-177
+ *   Cutpoint guiding table  src/device/wrs/cutpoint/guiding_table/shader.comp:40-55
+ *   Cutpoint sampling       src/device/wrs/cutpoint/sampling/shader.comp:100-140
  *   chi-square statistic    src/host/statistics/chi_square.hpp:17-37
  *   RMSE                    src/dep/eval/rms.hpp:24-63
  *   JS divergence           src/host/statistics/js_divergence.hpp:48-92
@@ -802,6 +804,80 @@ void wrso_its_sample(const float* cmf, uint32_t N, uint64_t S, uint64_t seed, ui
                      uint32_t rng, uint32_t coop, int parray, int nthreads, uint32_t* out) {
     wrso_sample_ctx c = {NULL, cmf, N, S, seed, offset, rng, coop, parray, out};
     wrso_parallel(its_task, &c, nthreads < 1 ? 1 : nthreads);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Cutpoint                                                                  */
+/* ------------------------------------------------------------------------- */
+
+/* cutpoint/guiding_table/shader.comp:40-55: guide[k] = lower bound of u_k = step * k with
+ * step = cmf[N-1] / G, over the whole CMF with the shader's probe sequence. */
+void wrso_cutpoint_guide(const float* cmf, uint32_t N, uint32_t G, uint32_t* guide) {
+    const float total = cmf[N - 1];
+    volatile float step = total / (float)G;
+    for (uint32_t k = 0; k < G; ++k) {
+        volatile float u = step * (float)k;
+        guide[k] = wrso_bisect(cmf, 0, N - 1, u);
+    }
+}
+
+typedef struct {
+    const float* cmf;
+    const uint32_t* guide;
+    uint32_t N, G;
+    uint64_t S, seed, offset;
+    uint32_t rng;
+    uint32_t* out;
+} wrso_cutpoint_ctx;
+
+/* cutpoint/sampling/shader.comp:100-140: the subgroup's elected lane (first sample of the
+ * aligned group of 32) draws u1 = wang_hash(seed + g0) and picks cell min(u1 * G, G - 1);
+ * each sample draws u2 = wang_hash((seed ^ 0x079145147) + g) inside the cell's CMF range
+ * [cmf[guide[k] - 1], cmf[guide[k+1]]] and bisects [guide[k], guide[k+1]] (N - 1 for the last
+ * cell).  Philox4x32-10 mode: u1 = x0 of the group's first sample, u2 = x1 of the sample. */
+static void cutpoint_task(void* p, int t, int nt) {
+    wrso_cutpoint_ctx* c = (wrso_cutpoint_ctx*)p;
+    uint64_t warps = (c->S + 31) / 32, lo, hi;
+    wrso_range(warps, t, nt, &lo, &hi);
+    const uint32_t seed32 = (uint32_t)c->seed;
+    const uint32_t key[2] = {(uint32_t)c->seed, (uint32_t)(c->seed >> 32)};
+    for (uint64_t wi = lo; wi < hi; ++wi) {
+        uint64_t s0 = wi * 32, s1 = s0 + 32;
+        if (s1 > c->S) s1 = c->S;
+        const uint64_t g0 = c->offset + s0;
+        float u1;
+        if (c->rng == WRSO_RNG_REFERENCE) {
+            u1 = wrso_unit_ref(wrso_wang_hash(seed32 + (uint32_t)g0));
+        } else {
+            uint32_t ctr[4] = {(uint32_t)g0, (uint32_t)(g0 >> 32), 0u, 0u}, r[4];
+            wrso_philox4x32_10(ctr, key, r);
+            u1 = wrso_unit_ref(r[0]);
+        }
+        volatile float prod = u1 * (float)c->G;
+        uint32_t k = (uint32_t)prod;
+        if (k > c->G - 1) k = c->G - 1;
+        const uint32_t x = c->guide[k];
+        const uint32_t y = k != c->G - 1 ? c->guide[k + 1] : c->N - 1;
+        for (uint64_t s = s0; s < s1; ++s) {
+            const uint64_t g = c->offset + s;
+            float uu;
+            if (c->rng == WRSO_RNG_REFERENCE) {
+                uu = wrso_unit_ref(wrso_wang_hash((seed32 ^ 0x79145147u) + (uint32_t)g));
+            } else {
+                uint32_t ctr[4] = {(uint32_t)g, (uint32_t)(g >> 32), 0u, 0u}, r[4];
+                wrso_philox4x32_10(ctr, key, r);
+                uu = wrso_unit_ref(r[1]);
+            }
+            c->out[s] = wrso_bisect(c->cmf, x, y, wrso_search_range_u(c->cmf, x, y, uu));
+        }
+    }
+}
+
+void wrso_cutpoint_sample(const float* cmf, uint32_t N, const uint32_t* guide, uint32_t G,
+                          uint64_t S, uint64_t seed, uint64_t offset, uint32_t rng, int nthreads,
+                          uint32_t* out) {
+    wrso_cutpoint_ctx c = {cmf, guide, N, G, S, seed, offset, rng, out};
+    wrso_parallel(cutpoint_task, &c, nthreads < 1 ? 1 : nthreads);
 }
 
 /* ------------------------------------------------------------------------- */

@@ -67,6 +67,10 @@ void wrso_alias_sample(const wrso_entry* table, uint32_t N, uint64_t S, uint64_t
                        uint64_t offset, uint32_t rng, uint32_t coop, int nthreads, uint32_t* out);
 void wrso_its_sample(const float* cmf, uint32_t N, uint64_t S, uint64_t seed, uint64_t offset,
                      uint32_t rng, uint32_t coop, int parray, int nthreads, uint32_t* out);
+void wrso_cutpoint_guide(const float* cmf, uint32_t N, uint32_t G, uint32_t* guide);
+void wrso_cutpoint_sample(const float* cmf, uint32_t N, const uint32_t* guide, uint32_t G,
+                          uint64_t S, uint64_t seed, uint64_t offset, uint32_t rng, int nthreads,
+                          uint32_t* out);
 
 /* ---- statistics ------------------------------------------------------------------ */
 void wrso_histogram(const uint32_t* samples, uint64_t S, uint32_t N, uint64_t* hist);

@@ -39,8 +39,9 @@ def test_config_defaults_and_validation(pkg):
     assert L.wrs_config_init(C.byref(cfg), w.METHOD_ALIAS_TABLE) == 0
     assert (cfg.split_size, cfg.use_partition_elements, cfg.rng, cfg.coop_size) == (2, 1, 0, 0)
     assert L.wrs_config_init(C.byref(cfg), w.METHOD_ITS) == 0
-    # the Cutpoint alternative of WRSConfig is not implemented
-    assert L.wrs_config_init(C.byref(cfg), w.METHOD_CUTPOINT) == 5
+    # the Cutpoint alternative of WRSConfig (CutpointConfig(..., guidingEntrySize))
+    assert L.wrs_config_init(C.byref(cfg), w.METHOD_CUTPOINT) == 0
+    assert (cfg.method, cfg.guiding_entry_size, cfg.coop_size) == (w.METHOD_CUTPOINT, 32, 0)
     assert L.wrs_config_init(C.byref(cfg), 9) == 1
     assert L.wrs_config_init(None, 0) == 1
     bad = [
@@ -49,14 +50,14 @@ def test_config_defaults_and_validation(pkg):
         w.WRSConfig(coop_size=128, rng=w.RNG_PHILOX4X32_10),
         w.WRSConfig(rng=7),
         w.WRSConfig(scan_precision=3),
+        w.CutpointConfig(guiding_entry_size=0),
+        w.CutpointConfig(coop_size=64),  # the Cutpoint method has no cooperative size
     ]
     for c in bad:
         with pytest.raises(w.WRSError) as e:
             w.Handle(c)
         assert e.value.status == 1
-    with pytest.raises(w.WRSError) as e:
-        w.Handle(w.WRSConfig(method=w.METHOD_CUTPOINT))
-    assert e.value.status == 5
+    assert w.Handle(w.CutpointConfig(128)).ptr
     h = w.Handle(w.AliasTableConfig(split_size=32, coop_size=128))
     assert h.ptr
 
@@ -73,6 +74,10 @@ def test_argument_validation_without_device_work(pkg):
     assert L.wrs_alias_sample(h.ptr, None, 8, 0, 16, 1, 0, 8) == 1  # n == 0
     assert b"NULL" in L.wrs_last_error() or b"range" in L.wrs_last_error()
     assert L.wrs_status_string(3) == b"a lookback wait gave up"
+    cp = w.Handle(w.CutpointConfig())
+    assert L.wrs_cutpoint_guide(cp.ptr, None, None, 16, None) == 1
+    assert L.wrs_cutpoint_guide(h.ptr, None, 8, 16, 8) == 1  # alias handle
+    assert L.wrs_cutpoint_sample(cp.ptr, None, 8, 0, 8, 16, 1, 0, 8) == 1  # n == 0
     assert L.wrs_version() == 100
     # a buffers object needs ~20 B per weight for the alias method, ~4 B for ITS
     n = 1 << 20

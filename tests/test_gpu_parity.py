@@ -293,6 +293,56 @@ def test_its_sample_edge_sizes(pkg, cuda, oracle, N, rng):
     assert np.array_equal(got, ref)
 
 
+# ------------------------------------------------------------------- cutpoint ---
+
+@pytest.mark.parametrize("N,entry", [(1, 32), (5, 1), (1000, 32), (4097, 128), (300001, 32),
+                                     ((1 << 20) + 3, 7)])
+@pytest.mark.parametrize("rng", [RNG_REFERENCE, RNG_PHILOX4X32_10])
+def test_cutpoint_bit_exact(pkg, cuda, oracle, N, entry, rng):
+    """Cutpoint (guiding table + guided sampling): the guiding table equals the oracle's
+    restatement of cutpoint/guiding_table/shader.comp and the samples its restatement of
+    cutpoint/sampling/shader.comp, given the GPU's CMF."""
+    W = pkg.wrs
+    w = weights_uniform(N, N + entry)
+    cfg = pkg.CutpointConfig(entry, rng=rng)
+    wrs = W.WRS(cfg)
+    bufs = W.WRSBuffers.allocate(N, 1, cfg, handle=wrs.handle)
+    bufs.weights.copy_(h2d(w))
+    wrs.build(None, bufs, N)
+    v = bufs.internals.views()
+    cmf = d2h(v["cmf"], N, np.float32)
+    G = (N + entry - 1) // entry
+    guide = d2h(v["guide_table"], G, np.uint32)
+    assert np.array_equal(guide, oracle.cutpoint_guide(cmf, entry))
+    S = 100003
+    import torch
+    out = torch.empty(S, dtype=torch.int32, device="cuda")
+    bufs.samples = out
+    wrs.sample(None, bufs, N, S, 4242, offset=17)
+    got = t2h(out, np.uint32)
+    assert np.array_equal(got, oracle.cutpoint_sample(cmf, guide, S, 4242, rng=rng, offset=17))
+    assert got.max() < N
+    assert bufs.internals.status() == 0
+
+
+def test_cutpoint_primitives(pkg, cuda, oracle):
+    """wrs_cutpoint_guide / wrs_cutpoint_sample on a caller's CMF (an oracle prefix sum)."""
+    W = pkg.wrs
+    N, entry = 77777, 64
+    w = weights_lognormal(N, 3)
+    cmf = oracle.prefix_kahan(w)
+    wrs = W.WRS(pkg.CutpointConfig(entry))
+    G = (N + entry - 1) // entry
+    dcmf = h2d(cmf)
+    guide = empty(G, "i32")
+    wrs.cutpoint_guide(None, dcmf, N, guide)
+    g = t2h(guide, np.uint32)
+    assert np.array_equal(g, oracle.cutpoint_guide(cmf, entry))
+    out = empty(5000, "i32")
+    wrs.cutpoint_sample(None, dcmf, N, guide, 5000, 99, 0, out)
+    assert np.array_equal(t2h(out, np.uint32), oracle.cutpoint_sample(cmf, g, 5000, 99))
+
+
 # ----------------------------------------------------------------- statistics ---
 
 @pytest.mark.parametrize("gen", list(GENS))

@@ -240,3 +240,51 @@ def test_oracle_threaded_equals_serial(oracle):
     a1 = oracle.alias_sample(t1, 10000, 3, nthreads=1)
     a4 = oracle.alias_sample(t1, 10000, 3, nthreads=4)
     assert np.array_equal(a1, a4)
+
+
+def test_cutpoint_oracle_against_numpy(oracle):
+    """The oracle's guiding table is the lower bound of u_k = fl(fl(total / G) * k) in the CMF
+    (numpy searchsorted on the same FP32 values), and each sample lies in the cell its group
+    of 32 drew: [guide[k], guide[k+1]] (N - 1 for the last cell)."""
+    import numpy as np
+    from oracle.oracle import RNG_PHILOX4X32_10, RNG_REFERENCE
+    rng = np.random.default_rng(3)
+    for N, entry in [(1, 32), (7, 1), (1000, 32), (65537, 128)]:
+        w = rng.random(N).astype(np.float32)
+        w[rng.random(N) < 0.1] = 0.0
+        cmf = oracle.prefix_kahan(w)
+        G = (N + entry - 1) // entry
+        step = np.float32(cmf[-1]) / np.float32(G)
+        u = (step * np.arange(G, dtype=np.float32)).astype(np.float32)
+        guide = oracle.cutpoint_guide(cmf, entry)
+        assert np.array_equal(guide, np.searchsorted(cmf, u, side="left").astype(np.uint32))
+        for r in (RNG_REFERENCE, RNG_PHILOX4X32_10):
+            S = 3000
+            s = oracle.cutpoint_sample(cmf, guide, S, 11, rng=r)
+            assert s.max() < N
+            again = oracle.cutpoint_sample(cmf, guide, S, 11, rng=r, nthreads=4)
+            assert np.array_equal(s, again)
+            # all 32 samples of a group come from one cell
+            for g0 in range(0, S, 32):
+                grp = s[g0:g0 + 32]
+                ks = [k for k in range(G)
+                      if guide[k] <= grp.min() and grp.max() <= (guide[k + 1] if k + 1 < G else N - 1)]
+                assert ks, (N, entry, g0)
+
+
+def test_cutpoint_reference_stream(oracle):
+    """The reference mode draws u1 = wang_hash(seed + g0) for the cell and
+    u2 = wang_hash((seed ^ 0x079145147) + g) inside it (cutpoint/sampling/shader.comp)."""
+    import numpy as np
+    N, entry, seed = 5000, 50, 777
+    w = np.full(N, 1.0, np.float32)
+    cmf = oracle.prefix_kahan(w)
+    guide = oracle.cutpoint_guide(cmf, entry)
+    G = guide.size
+    s = oracle.cutpoint_sample(cmf, guide, 64, seed)
+    for i in range(64):
+        g0 = i & ~31
+        u1 = np.float32(oracle.wang_hash(seed + g0)) * np.float32(2.0 ** -32)
+        k = min(int(np.float32(u1) * np.float32(G)), G - 1)
+        lo, hi = int(guide[k]), int(guide[k + 1]) if k + 1 < G else N - 1
+        assert lo <= s[i] <= hi
