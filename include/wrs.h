@@ -204,7 +204,7 @@ wrs_status wrs_cutpoint_sample(const wrs_handle* h, void* stream, const float* c
  * pool already holds all device memory, code that must not take the device-wide
  * synchronisation of cudaMalloc/cudaFree, or code called from inside another allocator.  No
  * counterpart in the reference.  Instead of a wrs_buffers object it uses one fixed array
- * of about 512 KiB in this library's own device memory, so n must be <= 2^26 (67,108,864;
+ * of about 1.2 MiB in this library's own device memory, so n must be <= 2^26 (67,108,864;
  * larger n returns WRS_ERR_CAPACITY).  The first call on a device looks up that array's
  * address and caches it; make that first call before capturing the stream into a CUDA
  * graph.  All calls share the array: each call clears it on `stream` before use, and calls

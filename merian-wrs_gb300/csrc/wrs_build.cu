@@ -5,6 +5,8 @@
 //                       prefix sums + heavyCount, single pass with decoupled lookback
 //                                                          (src/device/prefix_partition/decoupled/shader.comp)
 //   k_scan              inclusive FP32 scan, single pass    (src/device/prefix_sum/decoupled/shader.comp)
+//   k_scan_exact        the compensated form: exact fixed-point carries, correctly rounded
+//                       outputs (after k_total_mass, which sets the grid)
 //   k_split_pack        PSA split search + pack, one thread per split
 //                                                          (src/device/wrs/alias/psa/splitpack/inline/shader.comp)
 //
@@ -826,14 +828,162 @@ __global__ __launch_bounds__(kTileThreads) void k_scan(const float* __restrict__
     lookback_end(&ctrl->scan);
 }
 
+// Compensated scan with exact carries (the ITS / Cutpoint CMF).  Thread t of warp w holds the
+// 16 consecutive items [w*512 + 16t, +16) (re-read from the parked tile) and runs an FP32
+// running sum r over them from zero; its total T is that sum's last value.  Every element's
+// value is RN(C + E + fx(r)): C the exact carry of the tiles before, E the exact sum of
+// fx(T) over the threads before it in the tile, all on the fixed-point grid of the
+// distribution's total mass.  A thread's last element and the next thread's (or tile's) first
+// element therefore differ by exactly that element's own FP32 increment: the CMF is
+// non-decreasing, equal across zero weights (which can never be drawn), and independent of
+// the lookback's timing.
+__device__ u128 scan_lookback_x(const ScanState* st, uint32_t tile, uint32_t* status,
+                                uint32_t spin_limit) {
+    return lookback_walk(
+        tile, 0u, status, spin_limit, static_cast<u128>(0),
+        [st](uint32_t pos, u128& v) -> int {
+            const unsigned long long* q = st[pos].q;
+            unsigned long long lo, hi;
+            ld_relaxed_v2(q + 2, lo, hi);
+            int s = 2;
+            if (!fx_ready(lo, hi)) {
+                ld_relaxed_v2(q + 0, lo, hi);
+                s = fx_ready(lo, hi) ? 1 : 0;
+            }
+            if (s) v = fx_unpack(lo, hi);
+            return s;
+        },
+        [](u128 v) {
+#pragma unroll
+            for (int m = 1; m < 32; m <<= 1) v += shfl_xor_u128(v, m);
+            return v;
+        },
+        [](u128 a, u128 b) { return a + b; });
+}
+
+__global__ __launch_bounds__(kTileThreads) void k_scan_exact(const float* __restrict__ in,
+                                                             uint32_t n, float* __restrict__ out,
+                                                             BuildCtrl* __restrict__ ctrl,
+                                                             ScanState* __restrict__ states,
+                                                             uint32_t cap_tiles,
+                                                             uint32_t spin_limit) {
+    __shared__ float4 s_x[kTileItems / 4];  // the tile (park_slot), later its outputs
+    __shared__ u128 s_e[kTileThreads];       // exact thread-exclusive sums within the warp
+    __shared__ u128 s_wt[kTileWarps];        // exact warp totals -> warp-exclusive sums
+    __shared__ u128 s_c;                     // exact carry of the tiles before
+    ScanState* cur;
+    const uint32_t tile = lookback_begin(&ctrl->scan, states, cap_tiles, cur);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grid = fx_grid(ctrl->total);
+    {
+        float x[4][4];
+        load_tile(in, n, tile, x);
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+            s_x[park_slot(warp * 128 + v * 32 + lane)] = make_float4(x[v][0], x[v][1], x[v][2], x[v][3]);
+    }
+    __syncwarp();
+    {
+        float t = 0.f;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float4 q = s_x[park_slot(warp * 128 + lane * 4 + j)];
+            t = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(t, q.x), q.y), q.z), q.w);
+        }
+        const u128 X = fx_from_float(t, grid);
+        u128 inc = X;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long lo =
+                __shfl_up_sync(0xffffffffu, static_cast<unsigned long long>(inc), d);
+            const unsigned long long hi =
+                __shfl_up_sync(0xffffffffu, static_cast<unsigned long long>(inc >> 64), d);
+            if (lane >= d) inc += (static_cast<u128>(hi) << 64) | lo;
+        }
+        s_e[threadIdx.x] = inc - X;
+        if (lane == 31) s_wt[warp] = inc;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        u128 agg = 0;
+        if (lane == 0) {
+            for (int k = 0; k < kTileWarps; ++k) {
+                const u128 t = s_wt[k];
+                s_wt[k] = agg;
+                agg += t;
+            }
+        }
+        __syncwarp();
+        const unsigned long long alo = __shfl_sync(0xffffffffu, static_cast<unsigned long long>(agg), 0);
+        const unsigned long long ahi =
+            __shfl_sync(0xffffffffu, static_cast<unsigned long long>(agg >> 64), 0);
+        agg = (static_cast<u128>(ahi) << 64) | alo;
+        unsigned long long* q = cur[tile].q;
+        u128 ex = 0;
+        if (tile == 0) {
+            if (lane == 0) {
+                st_relaxed_v2(q + 0, fx_word_lo(agg), fx_word_hi(agg));
+                st_relaxed_v2(q + 2, fx_word_lo(agg), fx_word_hi(agg));
+            }
+        } else {
+            if (lane == 0) st_relaxed_v2(q + 0, fx_word_lo(agg), fx_word_hi(agg));
+            ex = scan_lookback_x(cur, tile, &ctrl->status, spin_limit);
+            if (lane == 0) st_relaxed_v2(q + 2, fx_word_lo(ex + agg), fx_word_hi(ex + agg));
+        }
+        if (lane == 0) s_c = ex;
+    }
+    __syncthreads();
+    {
+        const u128 K = s_c + s_wt[warp] + s_e[threadIdx.x];
+        float r = 0.f;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float4& slot = s_x[park_slot(warp * 128 + lane * 4 + j)];
+            float4 q = slot;
+            r = __fadd_rn(r, q.x);
+            q.x = fx_round(K + fx_from_float(r, grid), grid);
+            r = __fadd_rn(r, q.y);
+            q.y = fx_round(K + fx_from_float(r, grid), grid);
+            r = __fadd_rn(r, q.z);
+            q.z = fx_round(K + fx_from_float(r, grid), grid);
+            r = __fadd_rn(r, q.w);
+            q.w = fx_round(K + fx_from_float(r, grid), grid);
+            slot = q;  // this thread's own chunks: no other thread touches them here
+        }
+    }
+    __syncthreads();
+    const uint32_t tbase = tile * kTileItems;
+    const bool full = (static_cast<uint64_t>(tbase) + kTileItems <= n) &&
+                      ((reinterpret_cast<uintptr_t>(out) & 15u) == 0);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        const uint32_t chunk = warp * 128 + v * 32 + lane;
+        const float4 y = s_x[park_slot(chunk)];
+        const uint32_t e0 = tbase + chunk * 4;
+        if (full) {
+            __stcs(reinterpret_cast<float4*>(out + e0), y);
+        } else {
+            const float yv[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (e0 + c < n) out[e0 + c] = yv[c];
+        }
+    }
+    lookback_end(&ctrl->scan);
+}
+
 cudaError_t launch_scan(cudaStream_t st, bool comp, const float* in, uint32_t n, float* out,
-                        BuildCtrl* ctrl, ScanState* states, uint32_t cap_tiles,
+                        BuildCtrl* ctrl, ScanState* states, uint32_t cap_tiles, double* partials,
                         uint32_t spin_limit) {
     const uint32_t tiles = tiles_for(n);
-    if (comp)
-        k_scan<true><<<tiles, kTileThreads, 0, st>>>(in, n, out, ctrl, states, cap_tiles, spin_limit);
-    else
+    if (comp) {
+        // the exact carries need the distribution's fixed-point grid: its total mass first
+        cudaError_t e = launch_total_mass(st, in, n, partials, ctrl);
+        if (e != cudaSuccess) return e;
+        k_scan_exact<<<tiles, kTileThreads, 0, st>>>(in, n, out, ctrl, states, cap_tiles, spin_limit);
+    } else {
         k_scan<false><<<tiles, kTileThreads, 0, st>>>(in, n, out, ctrl, states, cap_tiles, spin_limit);
+    }
     return cudaGetLastError();
 }
 

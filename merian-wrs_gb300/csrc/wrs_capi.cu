@@ -275,7 +275,7 @@ wrs_status wrs_prefix_sum(const wrs_handle* h, void* stream, const float* in, ui
     wrs_status s = check_n(b, n);
     if (s != WRS_OK) return s;
     WRS_CUDA(launch_scan(as_stream(stream), h->cfg.scan_precision != WRS_SCAN_FP32, in, n,
-                         out, b->ctrl, b->scan_states, b->cap_tiles),
+                         out, b->ctrl, b->scan_states, b->cap_tiles, b->partials),
              "prefix sum");
     return WRS_OK;
 }
@@ -387,7 +387,8 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
     const cudaStream_t st = as_stream(stream);
     const bool comp = compensated(h);
     if (h->cfg.method != WRS_METHOD_ALIAS_TABLE) {
-        WRS_CUDA(launch_scan(st, comp, weights, n, b->cmf, b->ctrl, b->scan_states, b->cap_tiles),
+        WRS_CUDA(launch_scan(st, comp, weights, n, b->cmf, b->ctrl, b->scan_states, b->cap_tiles,
+                             b->partials),
                  "ITS build");
         if (h->cfg.method == WRS_METHOD_CUTPOINT)
             WRS_CUDA(launch_cutpoint_guide(st, b->cmf, n, guide_entries(n, h->cfg.guiding_entry_size),
@@ -457,7 +458,7 @@ wrs_status wrs_test_prefix_sum_stalled(const wrs_handle* h, void* stream, const 
     WRS_CUDA(cudaMemcpyAsync(&b->ctrl->scan.ticket, &one, sizeof(one), cudaMemcpyHostToDevice, st),
              "ticket preset");
     WRS_CUDA(launch_scan(st, h->cfg.scan_precision != WRS_SCAN_FP32, in, n, out, b->ctrl,
-                         b->scan_states, b->cap_tiles, spin_limit),
+                         b->scan_states, b->cap_tiles, b->partials, spin_limit),
              "stalled prefix sum");
     return WRS_OK;
 }

@@ -175,6 +175,20 @@ __device__ __forceinline__ u128 fx_lead_int(float f, int nb) {
     return nb >= 64 ? static_cast<u128>(fi) << (nb - 64) : static_cast<u128>(fi >> (64 - nb));
 }
 
+// f * 2^e for the f of fx_lead (2^63 <= f <= 2^64): an exact power-of-two product where the
+// result is normal, ldexpf otherwise.
+__device__ __forceinline__ float fx_scale(float f, int e) {
+    return (e >= -126 && e <= 127) ? __fmul_rn(f, __int_as_float((e + 127) << 23)) : ldexpf(f, e);
+}
+
+// k * 2^g rounded to nearest FP32.
+__device__ __forceinline__ float fx_round(u128 k, int g) {
+    if (k == 0) return 0.0f;
+    int nb;
+    const float f = fx_lead(k, nb);
+    return fx_scale(f, nb - 64 + g);
+}
+
 // k * 2^g as a float-float pair: hi = RN(k * 2^g), lo = RN((k - hi) * 2^g).  Deterministic
 // (a function of k and g only).
 __device__ __forceinline__ ff fx_to_ff(u128 k, int g) {
@@ -182,14 +196,14 @@ __device__ __forceinline__ ff fx_to_ff(u128 k, int g) {
     int nb;
     const float f = fx_lead(k, nb);
     const u128 kh = fx_lead_int(f, nb);
-    const float hi = ldexpf(f, nb - 64 + g);
+    const float hi = fx_scale(f, nb - 64 + g);
     float lo = 0.0f;
     if (kh != k) {
         const bool neg = kh > k;
         const u128 r = neg ? kh - k : k - kh;
         int nr;
         const float fr = fx_lead(r, nr);
-        lo = ldexpf(neg ? -fr : fr, nr - 64 + g);
+        lo = fx_scale(neg ? -fr : fr, nr - 64 + g);
     }
     return {hi, lo};
 }

@@ -63,9 +63,11 @@ static_assert(sizeof(BuildCtrl) == 128, "BuildCtrl layout");
 struct alignas(128) PartState {
     unsigned long long q[16];
 };
-// Lookback state of one tile of the scan (16 B): {aggregate, inclusive prefix}.
-struct alignas(16) ScanState {
-    unsigned long long agg, pre;
+// Lookback state of one tile of the scan (32 B).  FP32 mode: q[0] = aggregate, q[1] =
+// inclusive prefix (ff words).  Compensated mode: q[0..1] = aggregate, q[2..3] = inclusive
+// prefix (fixed-point limbs).
+struct alignas(32) ScanState {
+    unsigned long long q[4];
 };
 
 // One distribution of a batch (device copy of wrs_dist_desc plus its place in the
@@ -112,8 +114,10 @@ cudaError_t launch_prefix_partition(cudaStream_t st, bool comp, const float* w, 
                                     BuildCtrl* ctrl, PartState* states, uint32_t cap_tiles,
                                     uint32_t* idx_out, float* prefix_out, float* elems_out,
                                     float* prefix_lo_out);
+// comp: runs k_total_mass first (into `partials`, >= tiles_for(n) doubles) for the grid of the
+// exact carries
 cudaError_t launch_scan(cudaStream_t st, bool comp, const float* in, uint32_t n, float* out,
-                        BuildCtrl* ctrl, ScanState* states, uint32_t cap_tiles,
+                        BuildCtrl* ctrl, ScanState* states, uint32_t cap_tiles, double* partials,
                         uint32_t spin_limit = kSpinLimit);
 cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const float* w,
                               const uint32_t* idx, const float* elems, const float* prefix,

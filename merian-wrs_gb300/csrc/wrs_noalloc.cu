@@ -6,10 +6,10 @@
 // the device-wide synchronisation of cudaMalloc/cudaFree is not acceptable, or code called
 // from inside another allocator or a driver callback, where calling back into the CUDA
 // allocator is not allowed.  wrs_prefix_sum_noalloc serves them: its scratch (the control
-// block and the double-buffered lookback states) is a fixed-size array in this library's own
-// device memory, sized for up to kNoAllocMaxN weights.  The array is a file-scope
-// __device__ variable, so every GPU that loads the library holds it (about 512 KiB) until
-// the process exits.
+// block, the per-tile total-mass partials of the compensated mode and the double-buffered
+// lookback states) is a fixed-size array in this library's own device memory, sized for up
+// to kNoAllocMaxN weights.  The array is a file-scope __device__ variable, so every GPU that
+// loads the library holds it (about 1.2 MiB) until the process exits.
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -24,7 +24,9 @@ namespace {
 
 constexpr uint32_t kNoAllocMaxN = 1u << 26;  // 67,108,864 weights
 constexpr uint32_t kNoAllocTiles = (kNoAllocMaxN + kTileItems - 1) / kTileItems + 1;
-constexpr size_t kNoAllocStatesOffset = sizeof(BuildCtrl);
+constexpr size_t kNoAllocPartialsOffset = sizeof(BuildCtrl);
+constexpr size_t kNoAllocStatesOffset =
+    (kNoAllocPartialsOffset + kNoAllocTiles * sizeof(double) + 255) / 256 * 256;
 constexpr size_t kNoAllocBytes = kNoAllocStatesOffset + 2ull * kNoAllocTiles * sizeof(ScanState);
 
 static_assert(kNoAllocStatesOffset % alignof(ScanState) == 0, "state alignment");
@@ -77,15 +79,18 @@ extern "C" wrs_status wrs_prefix_sum_noalloc(void* stream, const float* in, uint
     if (scratch_address(&base) != cudaSuccess)
         return fail(WRS_ERR_CUDA, "cudaGetSymbolAddress of the scratch failed");
     BuildCtrl* ctrl = static_cast<BuildCtrl*>(base);
+    double* partials =
+        reinterpret_cast<double*>(static_cast<unsigned char*>(base) + kNoAllocPartialsOffset);
     ScanState* states =
         reinterpret_cast<ScanState*>(static_cast<unsigned char*>(base) + kNoAllocStatesOffset);
     // The array keeps whatever the previous call left.  Zero the control block (tickets,
-    // epoch, status) and the half of the states this launch uses (epoch 0 -> first half).
-    if (cudaMemsetAsync(base, 0, kNoAllocStatesOffset + kNoAllocTiles * sizeof(ScanState), st) !=
-        cudaSuccess)
+    // epoch, mass counter, status) and the half of the states this launch uses (epoch 0 ->
+    // first half); the partials need no clearing.
+    if (cudaMemsetAsync(base, 0, sizeof(BuildCtrl), st) != cudaSuccess ||
+        cudaMemsetAsync(states, 0, kNoAllocTiles * sizeof(ScanState), st) != cudaSuccess)
         return fail(WRS_ERR_CUDA, "clearing the scratch failed");
     if (launch_scan(st, scan_precision != WRS_SCAN_FP32, in, n, out, ctrl, states, kNoAllocTiles,
-                    kSpinLimit) != cudaSuccess)
+                    partials, kSpinLimit) != cudaSuccess)
         return fail(WRS_ERR_CUDA, "scan launch failed");
     if (device_status &&
         cudaMemcpyAsync(device_status, &ctrl->status, sizeof(uint32_t), cudaMemcpyDeviceToDevice,

@@ -261,6 +261,29 @@ def test_scan_precision(pkg, cuda, oracle, N, comp):
     assert err.max() <= (1e-6 if comp else 1e-4), err.max()
 
 
+@pytest.mark.parametrize("N", [4097, (1 << 22) + 5])
+def test_compensated_cmf_is_exactly_monotone(pkg, cuda, oracle, N):
+    """The compensated CMF is non-decreasing, equal across every zero weight (also at thread
+    and tile boundaries), bit-identical across builds, and the Philox ITS sampler never draws
+    a zero-weight index."""
+    w = weights_precision(N, 9)
+    w[::4096] = 0.0                   # zero weights at every tile start
+    w[16::4096] = 0.0                 # ... and at a thread boundary inside every tile
+    w[0] = 1.0
+    cfg = pkg.ITSConfig(scan_precision=1, rng=RNG_PHILOX4X32_10)
+    a = Built(pkg, w, cfg)
+    b = Built(pkg, w, cfg)
+    assert np.array_equal(a.cmf.view(np.uint32), b.cmf.view(np.uint32))
+    d = np.diff(a.cmf.astype(np.float64))
+    assert np.all(d >= 0)
+    zero = np.nonzero(w[1:] == 0)[0]
+    assert np.all(d[zero] == 0)
+    s = a.sample(1 << 22, 3)
+    assert not np.any(w[s] == 0)
+    ref = oracle.prefix_f64(w)
+    assert np.abs(a.cmf.astype(np.float64) - ref).max() <= 1e-6 * ref[-1]
+
+
 @pytest.mark.parametrize("rng,coop,parray", [(RNG_REFERENCE, 0, False),
                                              (RNG_REFERENCE, 128, False),
                                              (RNG_REFERENCE, 4096, True),
