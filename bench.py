@@ -71,6 +71,10 @@ def parse_args():
                    help="skip the batched mixed-size configuration (4096 distributions)")
     p.add_argument("--no-served", action="store_true",
                    help="skip the served request-stream configuration (200k requests)")
+    p.add_argument("--no-small", action="store_true",
+                   help="skip the plain small configuration (N = 65,536)")
+    p.add_argument("--no-precision", action="store_true",
+                   help="skip the precision study (N = 2^28, S = 2^30)")
     return p.parse_args()
 
 
@@ -379,8 +383,9 @@ def main() -> None:
                                       max(3, args.warmup))
     if not args.no_served:
         line["served"] = served_leg(W, cfg, dev)
-    if not args.no_extras:
+    if not args.no_small:
         line["small"] = small_leg(W, dev)
+    if not args.no_precision:
         line["precision"] = precision_leg(W, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         w0 = weights[0].cpu().numpy()
