@@ -1094,6 +1094,85 @@ __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, 
     jo = j;
 }
 
+// compute_split for kSplitPerThread splits at once: the bisections advance in lockstep so the
+// probes of all of them are in flight together (the search is latency-bound); each split
+// follows exactly compute_split's probe sequence and arithmetic.
+template <bool R64, bool FF, int V>
+__device__ __forceinline__ void compute_splits(const PackIn& c, const uint32_t (&nsplit)[V],
+                                               const bool (&on)[V], uint32_t (&io)[V],
+                                               uint32_t (&jo)[V], float (&spill)[V]) {
+    int a[V], b[V];
+    float target[V];
+    ff tff[V];
+    const uint32_t lcm1 = c.lcap;
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        a[v] = 0;
+        b[v] = on[v] ? static_cast<int>(c.hc) - 1 : -1;
+        target[v] = __fmul_rn(c.mean, __uint2float_rn(nsplit[v]));
+        tff[v] = FF ? ff_target(c.mean, c.mean_lo, nsplit[v]) : ff{0.f, 0.f};
+    }
+    for (;;) {
+        bool any = false;
+        float heavy[V], light[V], hl[V], ll[V];
+        uint32_t jv[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            heavy[v] = light[v] = hl[v] = ll[v] = 0.f;
+            jv[v] = 0;
+            if (a[v] <= b[v]) {
+                any = true;
+                const uint32_t j = static_cast<uint32_t>(a[v] + ((b[v] - a[v]) >> 1));
+                const uint32_t i = j > nsplit[v] ? lcm1 : min(nsplit[v] - j, lcm1);
+                jv[v] = j;
+                if (j) heavy[v] = __ldg(c.prefix + j - 1);
+                if (i) light[v] = __ldg(c.prefix + c.n - i);
+                if constexpr (FF) {
+                    if (j) hl[v] = __ldg(c.prefix_lo + j - 1);
+                    if (i) ll[v] = __ldg(c.prefix_lo + c.n - i);
+                }
+            }
+        }
+        if (!any) break;
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            if (a[v] <= b[v]) {
+                bool le;
+                if constexpr (FF)
+                    le = ff_sigma_minus(heavy[v], hl[v], light[v], ll[v], tff[v].hi, tff[v].lo) <= 0.0f;
+                else
+                    le = __fadd_rn(light[v], heavy[v]) <= target[v];
+                if (le)
+                    a[v] = static_cast<int>(jv[v]) + 1;
+                else
+                    b[v] = static_cast<int>(jv[v]) - 1;
+            }
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        if (!on[v]) continue;
+        const uint32_t j = b[v] < 0 ? 0u : static_cast<uint32_t>(b[v]);
+        const uint32_t i = j > nsplit[v] ? lcm1 : min(nsplit[v] - j, lcm1);
+        const float light = i == 0 ? 0.f : __ldg(c.prefix + c.n - i);
+        const float heavy2 = __ldg(c.prefix + j);
+        if constexpr (FF) {
+            const float hl2 = __ldg(c.prefix_lo + j);
+            const float l2 = i == 0 ? 0.f : __ldg(c.prefix_lo + c.n - i);
+            spill[v] = ff_sigma_minus(heavy2, hl2, light, l2, tff[v].hi, tff[v].lo);
+        } else if constexpr (R64) {
+            const double target64 =
+                __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit[v]));
+            spill[v] = __double2float_rn(__dsub_rn(
+                __dadd_rn(static_cast<double>(heavy2), static_cast<double>(light)), target64));
+        } else {
+            spill[v] = __fsub_rn(__fadd_rn(heavy2, light), target[v]);
+        }
+        io[v] = i;
+        jo[v] = j;
+    }
+}
+
 // splitpack/inline/shader.comp:130-211.  The shader's closing "last heavy -> (1, self)"
 // write (:212-222) is not performed: in subproblem order it is always overwritten by the
 // final subproblem, which packs the last heavy item itself (the oracle keeps the write and
@@ -1175,14 +1254,15 @@ struct SplitArgs {
     uint32_t full_light;
 };
 
-// Thread t of CTA b computes split k = b*kSplitPack + t (k in [0, K]) and packs subproblem
-// k = [split_k, split_{k+1}) for t < kSplitPack, k < K; split_{k+1} comes from the
-// neighbouring thread through shared memory (shader.comp:225-270).  The last
-// kSplitLook + 1 threads only compute look-ahead splits for the ownership window.
+// Slot t of CTA b (t < kSplitSlots; thread t % kSplitThreads holds slots t and t + 512) holds
+// split k = b*kSplitPack + t (k in [0, K]) and packs subproblem k = [split_k, split_{k+1})
+// for t < kSplitPack, k < K; split_{k+1} comes from the next slot through shared memory
+// (shader.comp:225-270).  The last kSplitLook + 1 slots only hold look-ahead splits for the
+// ownership window.
 template <bool R64, bool FF, bool BATCH>
 __global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, BatchView bv) {
-    __shared__ uint32_t s_i[kSplitThreads], s_j[kSplitThreads];
-    __shared__ float s_spill[kSplitThreads];
+    __shared__ uint32_t s_i[kSplitSlots], s_j[kSplitSlots];
+    __shared__ float s_spill[kSplitSlots];
     const float* w = a.w;
     uint32_t n = a.n;
     const BuildCtrl* ctrl = a.ctrl;
@@ -1218,31 +1298,45 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, Batch
     }
     PackIn c{w,      idx,    elems,  prefix, prefix_lo, n, hc,
              n - hc, a.full_light ? n - hc : n - hc - 1u, ctrl->mean, ctrl->mean_lo};
-    const uint32_t k = blk * kSplitPack + threadIdx.x;
-    uint32_t si = c.lc, sj = hc;  // past split K: the final split
-    float sp = 0.f;
-    if (k == 0u) {
-        si = 0;
-        sj = 0;
-    } else if (k < K) {
-        compute_split<R64, FF>(c, k * a.split_size, si, sj, sp);
+    // slot t + v * kSplitThreads of this CTA holds split k = blk * kSplitPack + slot
+    uint32_t kv[kSplitPerThread], nsplit[kSplitPerThread], si[kSplitPerThread], sj[kSplitPerThread];
+    float sp[kSplitPerThread];
+    bool on[kSplitPerThread];
+#pragma unroll
+    for (int v = 0; v < kSplitPerThread; ++v) {
+        kv[v] = blk * kSplitPack + threadIdx.x + v * kSplitThreads;
+        on[v] = kv[v] != 0u && kv[v] < K;
+        nsplit[v] = on[v] ? kv[v] * a.split_size : 0u;
+        si[v] = kv[v] == 0u ? 0u : c.lc;  // past split K: the final split
+        sj[v] = kv[v] == 0u ? 0u : hc;
+        sp[v] = 0.f;
     }
-    s_i[threadIdx.x] = si;
-    s_j[threadIdx.x] = sj;
-    s_spill[threadIdx.x] = sp;
+    compute_splits<R64, FF, kSplitPerThread>(c, nsplit, on, si, sj, sp);
+#pragma unroll
+    for (int v = 0; v < kSplitPerThread; ++v) {
+        const int slot = threadIdx.x + v * kSplitThreads;
+        s_i[slot] = si[v];
+        s_j[slot] = sj[v];
+        s_spill[slot] = sp[v];
+    }
     __syncthreads();
-    const int t = threadIdx.x;
-    if (t >= kSplitPack || k >= K) return;
-    const uint32_t i1 = max(s_i[t + 1], si), j1 = max(s_j[t + 1], sj);
-    const int count = static_cast<int>(min(static_cast<uint32_t>(kSplitLook), K - 1u - k));
-    bool clean = true;
-    for (int d = 1; d <= count; ++d)
-        clean = clean && s_i[t + d] >= i1 && s_j[t + d] >= j1;
-    // a step back reaching past the window cannot be resolved here: report it
-    if (k + kSplitLook + 1u < K && (s_i[t + kSplitLook + 1] < i1 || s_j[t + kSplitLook + 1] < j1))
-        atomicOr(a.status, kStatusNonMonotone);
-    const LaterSplits later{s_i, s_j, t, count};
-    pack(c, table, si, i1, sj, j1, sp, clean ? nullptr : &later);
+#pragma unroll 1
+    for (int v = 0; v < kSplitPerThread; ++v) {
+        const int t = threadIdx.x + v * kSplitThreads;
+        const uint32_t k = kv[v];
+        if (t >= kSplitPack || k >= K) continue;
+        const uint32_t i1 = max(s_i[t + 1], si[v]), j1 = max(s_j[t + 1], sj[v]);
+        const int count = static_cast<int>(min(static_cast<uint32_t>(kSplitLook), K - 1u - k));
+        bool clean = true;
+        for (int d = 1; d <= count; ++d)
+            clean = clean && s_i[t + d] >= i1 && s_j[t + d] >= j1;
+        // a step back reaching past the window cannot be resolved here: report it
+        if (k + kSplitLook + 1u < K &&
+            (s_i[t + kSplitLook + 1] < i1 || s_j[t + kSplitLook + 1] < j1))
+            atomicOr(a.status, kStatusNonMonotone);
+        const LaterSplits later{s_i, s_j, t, count};
+        pack(c, table, si[v], i1, sj[v], j1, sp[v], clean ? nullptr : &later);
+    }
 }
 
 template <bool BATCH>

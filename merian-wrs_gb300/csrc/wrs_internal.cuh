@@ -17,11 +17,14 @@ constexpr int kTileWarps = kTileThreads / 32;
 constexpr int kTileItems = 4096;
 constexpr int kWarpItems = kTileItems / kTileWarps;  // 512 contiguous items per warp
 
-// Split+pack: one thread per split; kSplitThreads - kSplitLook - 1 subproblems packed per CTA,
-// the remaining threads compute look-ahead splits (see k_split_pack).
+// Split+pack: kSplitPerThread splits per thread (their bisections interleaved);
+// kSplitSlots - kSplitLook - 1 subproblems packed per CTA, the remaining slots hold look-ahead
+// splits (see k_split_pack).
 constexpr int kSplitThreads = 512;
+constexpr int kSplitPerThread = 2;
+constexpr int kSplitSlots = kSplitThreads * kSplitPerThread;
 constexpr int kSplitLook = 32;
-constexpr int kSplitPack = kSplitThreads - kSplitLook - 1;
+constexpr int kSplitPack = kSplitSlots - kSplitLook - 1;
 
 // Alias sampling: 256 threads x 4 samples per CTA.
 constexpr int kSampleThreads = 256;
