@@ -145,7 +145,10 @@ void wrs_buffers_destroy(wrs_buffers* b);
 /* Build the sampler (alias table or CMF) of `weights[0..n)` (device, FP32, >= 0) into b. */
 wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, uint32_t n,
                      wrs_buffers* b);
-/* Draw s samples (uint32 indices, device) for sample indices [0, s). */
+/* Draw s samples (uint32 indices) for sample indices [0, s).  `samples` is any address the
+ * device can store to: device memory, or pinned host memory (cudaHostAlloc /
+ * cudaHostRegister; on NVLink-C2C systems the kernel then writes the samples straight into
+ * host memory, with no separate device-to-host copy). */
 wrs_status wrs_sample(const wrs_handle* h, void* stream, const wrs_buffers* b, uint32_t n,
                       uint64_t s, uint64_t seed, uint32_t* samples);
 /* Same for sample indices [offset, offset + s) of the stream. */

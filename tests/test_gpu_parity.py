@@ -407,6 +407,25 @@ def test_precision_weights_never_sample_zero(pkg, cuda, oracle):
         assert np.all(w[s] > 0), cfg.name()
 
 
+@pytest.mark.parametrize("method", ["alias", "its"])
+def test_sample_into_pinned_host_memory(pkg, cuda, method):
+    """wrs_sample with a pinned host buffer as the output writes the same samples as with a
+    device buffer."""
+    import torch
+    W = pkg.wrs
+    w = weights_lognormal(100003, 4)
+    cfg = (pkg.AliasTableConfig(split_size=8, rng=W.RNG_PHILOX4X32_10)
+           if method == "alias" else pkg.ITSConfig(rng=W.RNG_PHILOX4X32_10))
+    b = Built(pkg, w, cfg)
+    S = (1 << 20) + 3
+    dev = b.sample(S, 77)
+    host = torch.zeros(S, dtype=torch.int32).pin_memory()
+    b.wrs.sample(None, W.WRSBuffers(b.buffers.weights, host.data_ptr(), b.buffers.internals),
+                 b.N, S, 77)
+    torch.cuda.synchronize()
+    assert np.array_equal(host.numpy().view(np.uint32), dev)
+
+
 # ------------------------------------------------------------ determinism, status ---
 
 @pytest.mark.parametrize("precision", [1, 2])
