@@ -376,11 +376,19 @@ def main() -> None:
     samp_s = statistics.mean(sample_ms) / 1e3
     achieved = 12.0 * s / samp_s / 1e9
     traffic = profiled_traffic()
+    gather_rate = random_gather_rate(W, internals, n, s, stream)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
                 "kernel": "k_alias_sample", "bytes_model": "12 B/sample (8 B entry + 4 B index)",
                 "peak_source": pk["source"],
-                "sector_model_frac": (36.0 * s / samp_s / 1e9) / pk["hbm_gbs"]}
+                "sector_model_frac": (36.0 * s / samp_s / 1e9) / pk["hbm_gbs"],
+                "random_gather": {
+                    "rate": gather_rate, "unit": "gathers/s",
+                    "frac": (s / samp_s) / gather_rate,
+                    "model": "random 8-byte loads from the same 512 MB table, one per thread "
+                             "(wrs_probe_random_gather, CUDA events): the bound of sampling "
+                             "from a table larger than L2, where each gather costs a DRAM burst "
+                             "of ~107 B whatever its width"}}
 
     line = {
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world,
@@ -737,6 +745,28 @@ def small_leg(W, dev, steps: int = 20) -> dict:
             "chi2": chi2, "df": n - 1, "p_value": pval,
             "rmse": float(np.sqrt(np.mean((hist / s - p) ** 2))),
             "rmse_ideal": float(np.sqrt(np.mean(p * (1 - p) / s)))}
+
+
+def random_gather_rate(W, internals, n: int, s: int, stream) -> float:
+    """Random 8-byte gathers per second from the alias table itself (wrs_probe_random_gather),
+    mean of 3 timed launches of s gathers after 2 warm-up launches."""
+    import torch
+    sink = torch.zeros(1, dtype=torch.int32, device="cuda")
+    table = internals.views()["alias_table"]
+
+    def launch():
+        W.check(W.lib().wrs_probe_random_gather(stream.cuda_stream, table, 8 * n, s,
+                                                sink.data_ptr()))
+
+    for _ in range(2):
+        launch()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(3):
+        launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return s / (e0.elapsed_time(e1) / 3 / 1e3)
 
 
 def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, peak, args):

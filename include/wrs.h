@@ -346,6 +346,14 @@ wrs_status wrs_server_run_trace(wrs_server* s, const wrs_request* reqs,
                                 const double* arrival_s, uint32_t count,
                                 wrs_completion* out);
 
+/* ---- device calibration ----------------------------------------------------------------
+ * Launches one 8-byte load per thread from a hashed position in `buffer` (device memory,
+ * `bytes` long, 8-byte aligned), `accesses` threads in all; `sink` is a device word the kernel
+ * may write.  Time it with events on `stream`: the result is the device's random-gather rate,
+ * the bound of alias sampling from tables larger than L2.  No counterpart in the reference. */
+wrs_status wrs_probe_random_gather(void* stream, const void* buffer, uint64_t bytes,
+                                   uint64_t accesses, uint32_t* sink);
+
 #ifdef __cplusplus
 }
 #endif

@@ -128,6 +128,7 @@ def lib() -> C.CDLL:
             "wrs_batch_build": (i32, [vp, vp, vp]),
             "wrs_batch_sample": (i32, [vp, vp, vp]),
             "wrs_batch_status": (i32, [vp, vp, C.POINTER(u32)]),
+            "wrs_probe_random_gather": (i32, [vp, vp, u64, u64, vp]),
             "wrs_server_config_init": (i32, [C.POINTER(ServerConfig)]),
             "wrs_server_create": (i32, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
             "wrs_server_destroy": (None, [vp]),
