@@ -1116,21 +1116,19 @@ __device__ __forceinline__ void compute_splits(const PackIn& c, const uint32_t (
         bool any = false;
         float heavy[V], light[V], hl[V], ll[V];
         uint32_t jv[V];
+        uint32_t iv[V];
 #pragma unroll
         for (int v = 0; v < V; ++v) {
             heavy[v] = light[v] = hl[v] = ll[v] = 0.f;
-            jv[v] = 0;
+            jv[v] = iv[v] = 0;
             if (a[v] <= b[v]) {
                 any = true;
                 const uint32_t j = static_cast<uint32_t>(a[v] + ((b[v] - a[v]) >> 1));
                 const uint32_t i = j > nsplit[v] ? lcm1 : min(nsplit[v] - j, lcm1);
                 jv[v] = j;
+                iv[v] = i;
                 if (j) heavy[v] = __ldg(c.prefix + j - 1);
                 if (i) light[v] = __ldg(c.prefix + c.n - i);
-                if constexpr (FF) {
-                    if (j) hl[v] = __ldg(c.prefix_lo + j - 1);
-                    if (i) ll[v] = __ldg(c.prefix_lo + c.n - i);
-                }
             }
         }
         if (!any) break;
@@ -1138,10 +1136,29 @@ __device__ __forceinline__ void compute_splits(const PackIn& c, const uint32_t (
         for (int v = 0; v < V; ++v) {
             if (a[v] <= b[v]) {
                 bool le;
-                if constexpr (FF)
-                    le = ff_sigma_minus(heavy[v], hl[v], light[v], ll[v], tff[v].hi, tff[v].lo) <= 0.0f;
-                else
+                if constexpr (FF) {
+                    // FP32 pre-test: d = (h + l) - t differs from the float-float value
+                    // (h + hl) + (l + ll) - (t + tl) by at most 3u(h + l) + 2u t (u = 2^-24,
+                    // |lo| <= u |hi|), and the float-float evaluation is accurate to O(u^2);
+                    // beyond 8u(h + l + t) both have d's sign, so the low words are only
+                    // read near the split point and the result is unchanged.
+                    const float d = __fsub_rn(__fadd_rn(heavy[v], light[v]), tff[v].hi);
+                    const float m = __fmul_rn(4.76837158203125e-07f,  // 8 * 2^-24
+                                              __fadd_rn(__fadd_rn(heavy[v], light[v]), tff[v].hi));
+                    if (d > m) {
+                        le = false;
+                    } else if (d < -m) {
+                        le = true;
+                    } else {
+                        const uint32_t j = jv[v], i = iv[v];
+                        if (j) hl[v] = __ldg(c.prefix_lo + j - 1);
+                        if (i) ll[v] = __ldg(c.prefix_lo + c.n - i);
+                        le = ff_sigma_minus(heavy[v], hl[v], light[v], ll[v], tff[v].hi,
+                                            tff[v].lo) <= 0.0f;
+                    }
+                } else {
                     le = __fadd_rn(light[v], heavy[v]) <= target[v];
+                }
                 if (le)
                     a[v] = static_cast<int>(jv[v]) + 1;
                 else
