@@ -75,6 +75,8 @@ def parse_args():
                    help="skip the plain small configuration (N = 65,536)")
     p.add_argument("--no-precision", action="store_true",
                    help="skip the precision study (N = 2^28, S = 2^30)")
+    p.add_argument("--probe-gather", action="store_true",
+                   help="only measure the random-gather rate per load width and exit")
     return p.parse_args()
 
 
@@ -235,10 +237,41 @@ def run_reference(args) -> None:
 
 # ------------------------------------------------------------------ GPU ---
 
+def probe_gather(args) -> None:
+    """--probe-gather: random-gather rate per load width (4 .. 128 B) from a 512 MB buffer,
+    one JSON line (the calibration behind the alias sampler's roofline)."""
+    import torch
+    pkg = importlib.import_module("merian-wrs_gb300")
+    pkg.build()
+    W = pkg.wrs
+    nbytes, acc = 512 << 20, 1 << 26
+    buf = torch.zeros(nbytes // 4, dtype=torch.int32, device="cuda")
+    sink = torch.zeros(1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    out = {}
+    for width in (4, 8, 16, 32, 64, 128):
+        def launch():
+            W.check(W.lib().wrs_probe_random_gather(stream.cuda_stream, buf.data_ptr(), nbytes,
+                                                    acc, width, sink.data_ptr()))
+        for _ in range(3):
+            launch()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[str(width)] = acc / (e0.elapsed_time(e1) / 1e3)
+    print(json.dumps({"probe": "random gathers/s by load width (bytes), 512 MB buffer",
+                      "gathers_per_s": out}), flush=True)
+
+
 def main() -> None:
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.probe_gather:
+        probe_gather(args)
         return
     import numpy as np
     import torch
@@ -755,7 +788,7 @@ def random_gather_rate(W, internals, n: int, s: int, stream) -> float:
     table = internals.views()["alias_table"]
 
     def launch():
-        W.check(W.lib().wrs_probe_random_gather(stream.cuda_stream, table, 8 * n, s,
+        W.check(W.lib().wrs_probe_random_gather(stream.cuda_stream, table, 8 * n, s, 8,
                                                 sink.data_ptr()))
 
     for _ in range(2):

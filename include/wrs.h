@@ -346,13 +346,31 @@ wrs_status wrs_server_run_trace(wrs_server* s, const wrs_request* reqs,
                                 const double* arrival_s, uint32_t count,
                                 wrs_completion* out);
 
+/* ---- sample statistics on the device (src/device/statistics) --------------------------
+ * wrs_histogram: hist[samples[i]] += 1 for i < s (Histogram / AtomicHistogram,
+ * statistics/histogram/atomic/shader.comp); hist is n device uint64 counters the caller zeroes
+ * first; an index >= n is counted nowhere and sets bit 4 of *device_status (a device word).
+ * wrs_sample_statistics: from a histogram of s samples and the n weights, writes four device
+ * doubles to out: the chi-square statistic sum over e_i > 0 of (o_i - e_i)^2 / e_i with
+ * e_i = w_i * s / total (ChiSquare, statistics/chi_square/reduce/shader.comp), the RMSE
+ * sqrt(mean((w_i / total - o_i / s)^2)) (statistics/rmse/mse/shader.comp), the number of
+ * draws on zero-weight items, and the total weight.  Deterministic (fixed-order reductions,
+ * where the reference adds with FP32 atomics).  scratch: wrs_statistics_scratch_bytes(n)
+ * device bytes, 128-byte aligned, zeroed before its first use (the kernels leave it reusable). */
+wrs_status wrs_histogram(void* stream, const uint32_t* samples, uint64_t s, uint32_t n,
+                         uint64_t* hist, uint32_t* device_status);
+size_t wrs_statistics_scratch_bytes(uint32_t n);
+wrs_status wrs_sample_statistics(void* stream, const uint64_t* hist, const float* weights,
+                                 uint32_t n, uint64_t s, void* scratch, double* out);
+
 /* ---- device calibration ----------------------------------------------------------------
- * Launches one 8-byte load per thread from a hashed position in `buffer` (device memory,
- * `bytes` long, 8-byte aligned), `accesses` threads in all; `sink` is a device word the kernel
- * may write.  Time it with events on `stream`: the result is the device's random-gather rate,
- * the bound of alias sampling from tables larger than L2.  No counterpart in the reference. */
+ * Launches one `width`-byte load (4, 8, 16, 32, 64 or 128) per thread from a hashed,
+ * width-aligned position in `buffer` (device memory, `bytes` long), `accesses` threads in
+ * all; `sink` is a device word the kernel may write.  Time it with events on `stream`: with
+ * width 8 the result is the device's random-gather rate, the bound of alias sampling from
+ * tables larger than L2.  No counterpart in the reference. */
 wrs_status wrs_probe_random_gather(void* stream, const void* buffer, uint64_t bytes,
-                                   uint64_t accesses, uint32_t* sink);
+                                   uint64_t accesses, uint32_t width, uint32_t* sink);
 
 #ifdef __cplusplus
 }

@@ -128,7 +128,10 @@ def lib() -> C.CDLL:
             "wrs_batch_build": (i32, [vp, vp, vp]),
             "wrs_batch_sample": (i32, [vp, vp, vp]),
             "wrs_batch_status": (i32, [vp, vp, C.POINTER(u32)]),
-            "wrs_probe_random_gather": (i32, [vp, vp, u64, u64, vp]),
+            "wrs_probe_random_gather": (i32, [vp, vp, u64, u64, u32, vp]),
+            "wrs_histogram": (i32, [vp, vp, u64, u32, vp, vp]),
+            "wrs_statistics_scratch_bytes": (sz, [u32]),
+            "wrs_sample_statistics": (i32, [vp, vp, vp, u32, u64, vp, vp]),
             "wrs_server_config_init": (i32, [C.POINTER(ServerConfig)]),
             "wrs_server_create": (i32, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
             "wrs_server_destroy": (None, [vp]),
@@ -459,3 +462,34 @@ class Server:
         out = (Completion * max(1, n))()
         check(lib().wrs_server_run_trace(self.ptr, reqs, arr, n, out))
         return out
+
+
+class Statistics:
+    """Histogram, chi-square and RMSE of a sample set on the device (wrs_histogram /
+    wrs_sample_statistics; the reference's device::ChiSquare and RMSE passes)."""
+
+    def __init__(self, n: int, device="cuda"):
+        import torch
+        self.n = n
+        nbytes = lib().wrs_statistics_scratch_bytes(n)
+        self._scratch = torch.zeros((nbytes + 127) // 8 + 16, dtype=torch.float64, device=device)
+        off = (-self._scratch.data_ptr()) % 128
+        self.scratch = self._scratch.data_ptr() + off
+        self.hist = torch.zeros(n, dtype=torch.int64, device=device)
+        self.out = torch.zeros(4, dtype=torch.float64, device=device)
+        self.status = torch.zeros(1, dtype=torch.int32, device=device)
+
+    def __call__(self, stream, samples, s: int, weights) -> dict:
+        """samples: device tensor or address of s uint32 indices; returns chi2, rmse,
+        zero-weight draws and total weight (synchronises)."""
+        import torch
+        self.hist.zero_()
+        check(lib().wrs_histogram(_stream_ptr(stream), _dev_ptr(samples), s, self.n,
+                                  self.hist.data_ptr(), self.status.data_ptr()))
+        check(lib().wrs_sample_statistics(_stream_ptr(stream), self.hist.data_ptr(),
+                                          _dev_ptr(weights), self.n, s, self.scratch,
+                                          self.out.data_ptr()))
+        torch.cuda.synchronize()
+        o = self.out.cpu().tolist()
+        return {"chi2": o[0], "rmse": o[1], "zero_weight_draws": int(o[2]), "total": o[3],
+                "out_of_range": bool(int(self.status.item()) & 4)}

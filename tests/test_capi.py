@@ -157,3 +157,15 @@ def test_served_workload_shape(pkg):
         j = wl["table_id"][i]
         assert wl["n"][i] == wl["n"][j] and wl["w_off"][i] == wl["w_off"][j]
     assert np.all(wl["w_off"] % 32 == 0) and wl["w"].numel() == 1 << 20
+
+
+def test_statistics_and_probe_argument_checks_on_host(pkg):
+    w = pkg.wrs
+    L = w.lib()
+    assert L.wrs_histogram(None, None, 5, 10, None, None) == 1
+    assert L.wrs_histogram(None, 8, 5, 0, 8, 8) == 1           # n == 0
+    assert L.wrs_statistics_scratch_bytes(1 << 20) >= 128 + 4 * 8 * 256
+    assert L.wrs_sample_statistics(None, 8, 8, 10, 5, 8 + 64, 8) == 1  # misaligned scratch
+    assert L.wrs_sample_statistics(None, 8, 8, 0, 5, 128, 8) == 1      # n == 0
+    assert L.wrs_probe_random_gather(None, 256, 1 << 20, 16, 12, 8) == 1   # width 12
+    assert L.wrs_probe_random_gather(None, 8, 1 << 20, 16, 16, 8) == 1    # misaligned buffer
