@@ -684,7 +684,9 @@ def precision_leg(W, dev, log2n: int = 28, log2s: int = 30) -> dict:
     total = float(ref[-1])
     target = w.double() / total
     out = {"workload": f"precision study: N=2^{log2n} log-normal(0,3), 1% zeros, 0.01% x1e6; "
-                       f"S=2^{log2s} draws per sampler", "N": n, "S": s}
+                       f"S=2^{log2s} draws per sampler", "N": n, "S": s,
+           "statistics": "wrs_histogram + wrs_sample_statistics on the device"}
+    stats = W.Statistics(n)
     cmf = torch.empty(n, dtype=torch.float32, device=dev)
     scans = {}
     for name, prec in (("fp32", W.SCAN_FP32), ("compensated", W.SCAN_COMPENSATED)):
@@ -698,10 +700,10 @@ def precision_leg(W, dev, log2n: int = 28, log2s: int = 30) -> dict:
         if prec == W.SCAN_COMPENSATED:
             samples = torch.empty(s, dtype=torch.int32, device=dev)
             its.its_sample(None, cmf, n, s, 11, 0, samples)
-            hist = torch.bincount(samples.long(), minlength=n).double() / s
-            scans[name]["its_rmse"] = float(torch.sqrt(torch.mean((hist - target) ** 2)))
-            scans[name]["its_zero_weight_draws"] = int(hist[w == 0].sum() * s)
-            del samples, hist
+            r = stats(None, samples, s, w)
+            scans[name]["its_rmse"] = r["rmse"]
+            scans[name]["its_zero_weight_draws"] = r["zero_weight_draws"]
+            del samples
         del internals
     out["scan"] = scans
     tables = {}
@@ -721,13 +723,13 @@ def precision_leg(W, dev, log2n: int = 28, log2s: int = 30) -> dict:
         _dev_copy(table_t, internals.views()["alias_table"], 8 * n)
         imp = _implied(table_t, n)
         err = (imp - mean_units).abs()
-        hist = torch.bincount(samples.long(), minlength=n).double() / s
+        r = stats(None, samples, s, w)
         tables[name] = {"max_abs_err_mean_units": float(err.max()),
                         "max_rel_err_w_ge_mean": float((err / mean_units)[mean_units >= 1].max()),
-                        "alias_rmse": float(torch.sqrt(torch.mean((hist - target) ** 2))),
-                        "zero_weight_draws": int(hist[w == 0].sum() * s),
+                        "alias_rmse": r["rmse"], "chi2": r["chi2"],
+                        "zero_weight_draws": r["zero_weight_draws"],
                         "status": internals.status()}
-        del internals, samples, hist, table_t, imp, err
+        del internals, samples, table_t, imp, err
         torch.cuda.empty_cache()
     out["alias"] = tables
     out["rmse_ideal"] = float(torch.sqrt(torch.mean(target * (1 - target) / s)))
@@ -761,23 +763,21 @@ def small_leg(W, dev, steps: int = 20) -> dict:
     torch.cuda.synchronize()
     build_s = e[0].elapsed_time(e[1]) / steps / 1e3
     sample_s = e[1].elapsed_time(e[2]) / steps / 1e3
-    hist = torch.bincount(samples.long(), minlength=n).double().cpu().numpy()
+    st = W.Statistics(n)(stream, samples, s, w)  # on-device histogram, chi-square, RMSE
     p = w.double().cpu().numpy()
     p /= p.sum()
-    exp = p * s
-    chi2 = float(((hist - exp) ** 2 / exp).sum())
     try:
         from scipy.stats import chi2 as chi2_dist
-        pval = float(chi2_dist.sf(chi2, n - 1))
+        pval = float(chi2_dist.sf(st["chi2"], n - 1))
     except ImportError:
         pval = None
     return {"workload": "plain path, small: N=65,536 uniform(0,1] (seed 1), PSA build (split 2) "
                         "+ S=2^20 Philox4x32-10 samples (seed 1)",
             "builds_per_s": 1.0 / build_s, "samples_per_s": s / sample_s,
             "build_us": build_s * 1e6, "sample_us": sample_s * 1e6,
-            "chi2": chi2, "df": n - 1, "p_value": pval,
-            "rmse": float(np.sqrt(np.mean((hist / s - p) ** 2))),
-            "rmse_ideal": float(np.sqrt(np.mean(p * (1 - p) / s)))}
+            "chi2": st["chi2"], "df": n - 1, "p_value": pval, "rmse": st["rmse"],
+            "rmse_ideal": float(np.sqrt(np.mean(p * (1 - p) / s))),
+            "statistics": "wrs_histogram + wrs_sample_statistics on the device"}
 
 
 def random_gather_rate(W, internals, n: int, s: int, stream) -> float:
