@@ -481,6 +481,47 @@ BATCH_LOG2_S = 30
 BATCH_SEED = 6
 
 
+CPU_SAMPLE_ITEMS = 256
+
+
+def cpu_batch_baseline(items, total_s: int, what: str, reuse=None, seed: int = 60) -> dict:
+    """The CPU port (oracle, float-float split 8, Philox4x32-10) on a seeded uniform sample of
+    CPU_SAMPLE_ITEMS of the distributions / requests, all host cores in a thread pool over
+    the items (one item per thread, as independent distributions shard); the time is scaled
+    by items / sampled items.  items: (device weights, s, seed); reuse: items whose table is
+    resident (sampled only)."""
+    import concurrent.futures as cf
+    import numpy as np
+    from oracle.oracle import RNG_PHILOX4X32_10, SPLIT_FLOAT_FLOAT, SPLIT_FULL_LIGHT, Oracle
+    orc = Oracle()
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(len(items), min(CPU_SAMPLE_ITEMS, len(items)), replace=False)
+    host = [(items[i][0].cpu().numpy(), items[i][1], items[i][2],
+             bool(reuse[i]) if reuse is not None else False) for i in pick]
+    def one(k):
+        """seconds of CPU work for item k: build + sampling, or sampling alone for a request
+        whose table is resident (its build is done untimed)"""
+        w, s, seed_k, reused = host[k]
+        t0 = time.perf_counter()
+        table, _, _ = orc.psa_build(w, SPLIT_SIZE, nthreads=1,
+                                    flags=SPLIT_FLOAT_FLOAT | SPLIT_FULL_LIGHT)
+        t1 = time.perf_counter()
+        orc.alias_sample(table, s, seed_k, rng=RNG_PHILOX4X32_10, nthreads=1)
+        t2 = time.perf_counter()
+        return (t2 - t1) if reused else (t2 - t0)
+
+    nthreads = cpu_threads()
+    with cf.ThreadPoolExecutor(max_workers=nthreads) as ex:
+        work = sum(ex.map(one, range(len(host))))
+    elapsed = work / nthreads * len(items) / len(host)  # perfectly balanced over the threads
+    return {"value": total_s / elapsed, "unit": "samples/s", "cores": nthreads, "kind": "port",
+            "sample": f"{len(host)} of {len(items)} {what} (seeded uniform choice), one per "
+                      f"thread on {nthreads} threads; CPU seconds summed, divided by the threads "
+                      f"and scaled by {len(items) / len(host):.1f}" +
+                      ("; requests on a resident table count their sampling only"
+                       if reuse is not None else "")}
+
+
 def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
     """The batched configuration: all 4096 distributions built and sampled by one CUDA graph
     (wrs_batch_build + wrs_batch_sample: 4 launches), against 4096 per-call wrs_build +
@@ -574,6 +615,9 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
         "rmse_mean": statistics.mean(rmse), "rmse_max": max(rmse),
         "per_call_driver": "Python loop over the C ABI (wrs_build + wrs_sample_at per "
                            "distribution), one reused buffers object",
+        "cpu_baseline": cpu_batch_baseline(
+            [(w[int(w_off[d]):int(w_off[d]) + int(sizes[d])], int(counts[d]), seeds[d])
+             for d in range(D)], total_s, "distributions"),
     }
 
 
@@ -642,6 +686,10 @@ def served_leg(W, cfg, dev, n_requests: int = SERVED_REQUESTS) -> dict:
         "evictions": st["evictions"], "table_bytes_peak": st["table_bytes_peak"],
         "scratch_bytes": st["scratch_bytes"], "device_status": st["device_status"],
         "alone_vs_mix_equal": f"{equal}/{len(pick)}",
+        "cpu_baseline": cpu_batch_baseline(
+            [(w[int(wl["w_off"][i]):int(wl["w_off"][i]) + int(wl["n"][i])], int(wl["s"][i]),
+              int(wl["seeds"][i])) for i in range(n_requests)], total_s, "requests",
+            reuse=[bool(wl["table_id"][i] != i) for i in range(n_requests)]),
     }
 
 
