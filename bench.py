@@ -895,6 +895,12 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
     rec("scan", timed(lambda: its.prefix_sum(stream, w, n, cmf, internals)), 8 * n, n, "weights")
     rec("its_sample", timed(lambda: its.its_sample(stream, cmf, n, s, 99, 0, samples)), 4 * s, s,
         "samples")
+    # through the buffers API: the compensated build also makes the guiding table, and
+    # sampling runs the guided search (same samples as the bisection)
+    its_bufs = W.WRSBuffers(w, samples, W.Internals(its.handle, n))
+    its.build(stream, its_bufs, n)
+    rec("its_sample_guided", timed(lambda: its.sample(stream, its_bufs, n, s, seed=99)), 4 * s,
+        s, "samples")
     cp = W.WRS(W.CutpointConfig(128))
     G = (n + 127) // 128
     guide = torch.empty(G, dtype=torch.int32, device=w.device)

@@ -101,8 +101,11 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
         L.table = take(sizeof(uint2) * static_cast<size_t>(max_n));
     } else {
         L.cmf = take(sizeof(float) * static_cast<size_t>(max_n));
-        if (cfg.method == WRS_METHOD_CUTPOINT)
-            L.guide = take(sizeof(uint32_t) * guide_entries(max_n, cfg.guiding_entry_size));
+        // Cutpoint: its guiding table; ITS: the table that guides sampling on the
+        // compensated (exactly non-decreasing) CMF
+        L.guide = take(sizeof(uint32_t) *
+                       guide_entries(max_n, cfg.method == WRS_METHOD_CUTPOINT ? cfg.guiding_entry_size
+                                                                              : kItsGuideEntry));
     }
     L.total = off;
     return L;
@@ -234,7 +237,7 @@ wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers**
         b->table = reinterpret_cast<uint2*>(p + L.table);
     } else {
         b->cmf = reinterpret_cast<float*>(p + L.cmf);
-        if (h->cfg.method == WRS_METHOD_CUTPOINT) b->guide = reinterpret_cast<uint32_t*>(p + L.guide);
+        b->guide = reinterpret_cast<uint32_t*>(p + L.guide);
     }
     e = cudaMemset(b->base, 0, zeroed_bytes(h->cfg, max_n));
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -394,6 +397,9 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
             WRS_CUDA(launch_cutpoint_guide(st, b->cmf, n, guide_entries(n, h->cfg.guiding_entry_size),
                                            b->guide),
                      "guiding table");
+        else if (comp)
+            WRS_CUDA(launch_cutpoint_guide(st, b->cmf, n, guide_entries(n, kItsGuideEntry), b->guide),
+                     "ITS guiding table");
         return WRS_OK;
     }
     if (h->cfg.use_partition_elements && !b->elems)
@@ -420,8 +426,19 @@ wrs_status wrs_sample_at(const wrs_handle* h, void* stream, const wrs_buffers* b
     if (st != WRS_OK) return st;
     if (b->cfg.method != h->cfg.method)
         return fail(WRS_ERR_INVALID_ARG, "buffers were created for another method");
-    if (h->cfg.method == WRS_METHOD_ITS)
+    if (h->cfg.method == WRS_METHOD_ITS) {
+        if (compensated(h) && h->cfg.coop_size == 0 && s) {
+            // the compensated CMF is non-decreasing: the guided search returns the bisection's
+            // index (see k_its_sample_guided)
+            if (!samples) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+            WRS_CUDA(launch_its_sample_guided(as_stream(stream), h->cfg.rng, b->cmf, n, b->guide,
+                                              guide_entries(n, kItsGuideEntry), s, seed, offset,
+                                              samples),
+                     "its sample");
+            return WRS_OK;
+        }
         return wrs_its_sample(h, stream, b->cmf, n, s, seed, offset, samples);
+    }
     if (h->cfg.method == WRS_METHOD_CUTPOINT)
         return wrs_cutpoint_sample(h, stream, b->cmf, n, b->guide, s, seed, offset, samples);
     return wrs_alias_sample(h, stream, reinterpret_cast<const wrs_alias_entry*>(b->table), n, s,

@@ -136,6 +136,11 @@ cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool
 
 cudaError_t launch_cutpoint_guide(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
                                   uint32_t* guide);
+// ITS on a non-decreasing CMF with a guiding table of kItsGuideEntry weights per entry
+constexpr uint32_t kItsGuideEntry = 32;
+cudaError_t launch_its_sample_guided(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
+                                     const uint32_t* guide, uint32_t G, uint64_t S, uint64_t seed,
+                                     uint64_t offset, uint32_t* out);
 cudaError_t launch_cutpoint_sample(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
                                    const uint32_t* guide, uint32_t G, uint64_t S, uint64_t seed,
                                    uint64_t offset, uint32_t* out);

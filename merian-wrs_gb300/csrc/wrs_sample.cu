@@ -387,6 +387,72 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_tree(const float*
     }
 }
 
+// ---- ITS on an exactly non-decreasing CMF, guided ---------------------------------------
+//
+// On a non-decreasing CMF every lower-bound search returns the same index, so the bisection
+// can start from a guiding-table cell instead of [0, N - 1] (the compensated scan's CMF is
+// non-decreasing by construction).  guide[k] = lower bound of fl(fl(total / G) * k) (the
+// Cutpoint guiding table, G = ceil(N / 32)); the target's cell comes from an FP32 estimate and
+// is accepted only if cmf[x - 1] < T <= cmf[y] holds for its range [x, y] (exact comparisons),
+// else the search falls back to the whole CMF.  Results equal k_its_sample_tree's.
+template <uint32_t RNG>
+__global__ __launch_bounds__(kSampleThreads) void k_its_sample_guided(
+    const float* __restrict__ cmf, uint32_t n, const uint32_t* __restrict__ guide, uint32_t G,
+    uint64_t S, uint64_t seed, uint64_t offset, uint32_t* __restrict__ out) {
+    const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const uint32_t last = n - 1u;
+    const float total = __ldg(cmf + last);
+    const uint64_t g = offset + s;
+    float t_hi;
+    int t_sgn = 0;
+    if constexpr (RNG == RNG_REF) {
+        const uint32_t seed32 = static_cast<uint32_t>(seed);
+        t_hi = search_range_u(cmf, 0, last,
+                              unit_ref(wang_hash((seed32 ^ 0xA9EC5C80u) + static_cast<uint32_t>(g))));
+    } else {
+        uint2 ks[10];
+        philox4x32_10_keys(seed, ks);
+        const uint4 r = philox4x32_10(
+            make_uint4(static_cast<uint32_t>(g), static_cast<uint32_t>(g >> 32), 0u, 0u), ks);
+        exact_target(r.x, total, t_hi, t_sgn);
+    }
+    // "T > c" for the target T = (t_hi, t_sgn) (RNG_REF: t_sgn = 0, the shader's u > cmf[mid])
+    auto above = [&](float c) { return t_hi > c || (t_hi == c && t_sgn > 0); };
+    const float scale = __fdiv_rn(__uint2float_rn(G), total);
+    uint32_t k = __float2uint_rz(__fmul_rn(t_hi, scale));
+    k = k < G - 1u ? k : G - 1u;
+    uint32_t x = __ldg(guide + k);
+    uint32_t y = k + 1u < G ? __ldg(guide + k + 1u) : last;
+    if (!((x == 0 || above(__ldg(cmf + x - 1u))) && !above(__ldg(cmf + y)))) {
+        x = 0;
+        y = last;
+    }
+    while (x < y) {
+        const uint32_t mid = x + ((y - x) >> 1);
+        if (above(__ldg(cmf + mid)))
+            x = mid + 1;
+        else
+            y = mid;
+    }
+    __stcs(out + s, x);
+}
+
+cudaError_t launch_its_sample_guided(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
+                                     const uint32_t* guide, uint32_t G, uint64_t S, uint64_t seed,
+                                     uint64_t offset, uint32_t* out) {
+    const uint64_t blocks = (S + kSampleThreads - 1) / kSampleThreads;
+    if (blocks == 0) return cudaSuccess;
+    if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
+    if (rng == RNG_REF)
+        k_its_sample_guided<RNG_REF><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
+            cmf, n, guide, G, S, seed, offset, out);
+    else
+        k_its_sample_guided<RNG_PHILOX><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
+            cmf, n, guide, G, S, seed, offset, out);
+    return cudaGetLastError();
+}
+
 // ---- Cutpoint (guiding table) -----------------------------------------------------------
 
 // cutpoint/guiding_table/shader.comp:40-55: entry k = lower bound of (total / G) * k over the

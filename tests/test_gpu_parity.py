@@ -301,6 +301,22 @@ def test_its_sample_bit_exact(pkg, cuda, oracle, rng, coop, parray):
     assert np.array_equal(got, ref)
 
 
+@pytest.mark.parametrize("N", [1, 2, 33, 4097, 300001, (1 << 22) + 3])
+@pytest.mark.parametrize("rng", [RNG_REFERENCE, RNG_PHILOX4X32_10])
+def test_its_guided_sampling_on_the_compensated_cmf(pkg, cuda, oracle, N, rng):
+    """ITS on the compensated (non-decreasing) CMF runs the guided search (a guiding-table cell
+    instead of the whole range): samples equal the oracle's plain bisection, also with runs of
+    zero weights and a heavy tail."""
+    w = weights_precision(N, N)
+    w[0] = max(w[0], np.float32(0.25))
+    b = Built(pkg, w, pkg.ITSConfig(rng=rng, scan_precision=1))
+    assert np.all(np.diff(b.cmf.astype(np.float64)) >= 0)
+    S = (1 << 20) + 11
+    got = b.sample(S, 4242, 7)
+    ref = oracle.its_sample(b.cmf, S, 4242, rng=rng, offset=7, nthreads=8)
+    assert np.array_equal(got, ref)
+
+
 @pytest.mark.parametrize("N", [1, 2, 3, 7, 4095, 4096, 4097, 8191, 8193, 70001])
 @pytest.mark.parametrize("rng", [RNG_REFERENCE, RNG_PHILOX4X32_10])
 def test_its_sample_edge_sizes(pkg, cuda, oracle, N, rng):
