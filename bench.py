@@ -31,6 +31,7 @@ Multi-GPU runs are independent replicas (the path does not shard one distributio
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import importlib
 import json
 import os
@@ -51,9 +52,12 @@ WORKLOAD = ("single large distribution: N=2^26 FP32 weights x 3 seeded distribut
             "(uniform(0,1], Zipf s=1.1 permuted, log-normal(0,2)); step = PSA alias build + "
             "S=2^28 alias samples (Philox4x32-10, uint32 indices)")
 METRIC = "samples/s"
-# PSA split size: 8 minimises split+pack time on GB300 at N = 2^26 (2.12 ms at 2, 0.80 ms at 8,
-# 1.16 ms at 32; float-float table accuracy does not depend on it)
-SPLIT_SIZE = 8
+# PSA split size of the single-distribution configuration, fixed so that the line's config is
+# the same in every run: 12 is the autotuner's pick on GB300 at N = 2^26 (split+pack 0.70 ms
+# uniform / 0.60 ms log-normal at 12, 0.72 / 0.67 at 8, 1.11 / 1.04 at 4, 0.88 / 0.85 at 24;
+# float-float table accuracy does not depend on it).  The batched configuration tunes its
+# split size live.
+SPLIT_SIZE = 12
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "alias_sample_n26_s28.md")
 
 
@@ -300,6 +304,11 @@ def main() -> None:
     samples = torch.empty(s, dtype=torch.int32, device=dev)
     bufs = [W.WRSBuffers(weights[d], samples, internals) for d in range(3)]
 
+    # the context's L2 fetch granularity, tuned live on the first distribution (the split
+    # size stays fixed); it changes no result
+    tune = W.autotune_alias(cfg, stream, weights[0], n, s, samples, split_sizes=[],
+                            l2_fetch=None, warmup=1, reps=2)
+
     def step(k: int, ev=None):
         b = bufs[k % 3]
         if ev is not None:
@@ -432,7 +441,12 @@ def main() -> None:
                    "rng": "philox4x32-10", "precision": "float-float partition prefix",
                    "split": "float-float residual, light cap fixed",
                    "l2": "inputs larger than L2 (256 MB weights, 512 MB table, 1 GB samples)",
+                   "l2_fetch_granularity": tune["l2_fetch"],
                    "parallelism": f"replicas x{world}"},
+        "autotune": {"l2_fetch": tune["l2_fetch"], "trials": tune["trials"],
+                     "method": "wrs_autotune_alias over L2 fetch granularity 32/64/128 B at "
+                               f"split size {SPLIT_SIZE} (CUDA events, 1 warm-up + 2 timed "
+                               "build+sample calls each), before the warm-up steps"},
         "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * s,
                 "method": "weights: pinned host -> device copy per step on a copy stream, "
@@ -484,8 +498,9 @@ BATCH_SEED = 6
 CPU_SAMPLE_ITEMS = 256
 
 
-def cpu_batch_baseline(items, total_s: int, what: str, reuse=None, seed: int = 60) -> dict:
-    """The CPU port (oracle, float-float split 8, Philox4x32-10) on a seeded uniform sample of
+def cpu_batch_baseline(items, total_s: int, what: str, reuse=None, seed: int = 60,
+                       split_size: int = SPLIT_SIZE) -> dict:
+    """The CPU port (oracle, float-float split, Philox4x32-10) on a seeded uniform sample of
     CPU_SAMPLE_ITEMS of the distributions / requests, all host cores in a thread pool over
     the items (one item per thread, as independent distributions shard); the time is scaled
     by items / sampled items.  items: (device weights, s, seed); reuse: items whose table is
@@ -503,7 +518,7 @@ def cpu_batch_baseline(items, total_s: int, what: str, reuse=None, seed: int = 6
         whose table is resident (its build is done untimed)"""
         w, s, seed_k, reused = host[k]
         t0 = time.perf_counter()
-        table, _, _ = orc.psa_build(w, SPLIT_SIZE, nthreads=1,
+        table, _, _ = orc.psa_build(w, split_size, nthreads=1,
                                     flags=SPLIT_FLOAT_FLOAT | SPLIT_FULL_LIGHT)
         t1 = time.perf_counter()
         orc.alias_sample(table, s, seed_k, rng=RNG_PHILOX4X32_10, nthreads=1)
@@ -537,11 +552,17 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
     out_b = torch.empty(int(s_off[-1]), dtype=torch.int32, device=dev)
     out_p = torch.empty_like(out_b)
     seeds = [77 + d for d in range(D)]
+    wp, tp, bp, pp = w.data_ptr(), tables.data_ptr(), out_b.data_ptr(), out_p.data_ptr()
+    dists = [(wp + 4 * int(w_off[d]), tp + 8 * int(w_off[d]), bp + 4 * int(s_off[d]),
+              int(sizes[d]), int(counts[d]), seeds[d]) for d in range(D)]
+    # autotuned: split size and L2 fetch granularity measured on this batch; both arms then
+    # run the chosen configuration
+    tune = W.autotune_batch(cfg, stream, dists, split_sizes=None, l2_fetch=None, warmup=1,
+                            reps=2)
+    cfg = dataclasses.replace(cfg, split_size=tune["split_size"])
     h = W.Handle(cfg)
     batch = W.Batch(h, D, int(sizes.sum()), int(counts.sum()))
-    wp, tp, bp, pp = w.data_ptr(), tables.data_ptr(), out_b.data_ptr(), out_p.data_ptr()
-    batch.set(stream, [(wp + 4 * int(w_off[d]), tp + 8 * int(w_off[d]), bp + 4 * int(s_off[d]),
-                        int(sizes[d]), int(counts[d]), seeds[d]) for d in range(D)])
+    batch.set(stream, dists)
     batch.build(stream)
     batch.sample(stream)
     torch.cuda.synchronize()
@@ -605,6 +626,11 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
                     f"(sum {int(sizes.sum())}), uniform(0,1] or Zipf s=1.1 per distribution "
                     f"by seed; S_d proportional to N_d, sum 2^{BATCH_LOG2_S}; Philox4x32-10",
         "distributions": D, "weights": int(sizes.sum()), "samples": total_s,
+        "autotune": {"split_size": tune["split_size"], "l2_fetch": tune["l2_fetch"],
+                     "trials": tune["trials"],
+                     "method": "wrs_autotune_batch: L2 fetch granularity 32/64/128 B at split "
+                               f"size {SPLIT_SIZE}, then split sizes 4-32 at the best L2 value "
+                               "(CUDA events, 1 warm-up + 2 timed batch build+sample each)"},
         "graph_ms": batched_ms, "per_call_ms": per_call_ms,
         "samples_per_s": total_s / (batched_ms / 1e3),
         "per_call_samples_per_s": total_s / (per_call_ms / 1e3),
@@ -617,7 +643,7 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
                            "distribution), one reused buffers object",
         "cpu_baseline": cpu_batch_baseline(
             [(w[int(w_off[d]):int(w_off[d]) + int(sizes[d])], int(counts[d]), seeds[d])
-             for d in range(D)], total_s, "distributions"),
+             for d in range(D)], total_s, "distributions", split_size=cfg.split_size),
     }
 
 

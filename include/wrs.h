@@ -372,6 +372,63 @@ wrs_status wrs_sample_statistics(void* stream, const uint64_t* hist, const float
 wrs_status wrs_probe_random_gather(void* stream, const void* buffer, uint64_t bytes,
                                    uint64_t accesses, uint32_t width, uint32_t* sink);
 
+/* ---- autotuning (alias method) -----------------------------------------------------------
+ * No counterpart in the reference, whose WRSConfig is fixed at construction
+ * (src/device/wrs/WRS.hpp:116-119).  Two knobs are tuned by measurement (CUDA events on
+ * `stream`, objective = build + sample milliseconds per call):
+ *   split size  PSA InlineSplitPackConfig::splitSize (src/device/wrs/alias/psa/PSA.hpp:19-41):
+ *               pack items per split.  Part of the table's definition: tables built with
+ *               different split sizes differ in their bits, so per-call and batched builds
+ *               that must agree use the same value.
+ *   L2 fetch    the CUDA context's cudaLimitMaxL2FetchGranularity hint (bytes the L2 fetches
+ *               from HBM per miss; alias sampling from tables larger than L2 is bound by
+ *               it).  Context-wide, lasts as long as the context, changes no result.
+ * The search is coordinate-wise: each L2 candidate at the configured split size, then each
+ * split size at the best L2 value; the context's L2 limit is left at the chosen value.  The
+ * tuner allocates (one handle and buffers or batch per candidate), synchronises the stream,
+ * and overwrites the samples (and, for batches, the tables) its inputs name; not for use
+ * inside a stream capture. */
+typedef struct wrs_tune_space {
+    const uint32_t* split_sizes; /* candidates; NULL = 4, 6, 8, 12, 16, 24, 32 (with count
+                                    0 and NULL: only the configured size) */
+    uint32_t split_count;
+    const uint32_t* l2_fetch;    /* candidate granularities in bytes (0..128); NULL = 32, 64,
+                                    128 (with count 0 and NULL: the L2 limit is not touched) */
+    uint32_t l2_count;
+    uint32_t warmup;             /* untimed calls per candidate (0 = 1) */
+    uint32_t reps;               /* timed calls per candidate (0 = 3) */
+} wrs_tune_space;
+
+typedef struct wrs_tune_trial {
+    uint32_t split_size;
+    uint32_t l2_fetch;           /* 0 when the L2 limit was not tuned */
+    float build_ms;              /* mean per call */
+    float sample_ms;
+} wrs_tune_trial;
+
+typedef struct wrs_tune_result {
+    uint32_t split_size;         /* the fastest candidate */
+    uint32_t l2_fetch;           /* its L2 fetch granularity (0 when not tuned) */
+    float build_ms;
+    float sample_ms;
+    uint32_t trials;             /* candidates measured */
+} wrs_tune_result;
+
+/* Sets / reads the current CUDA context's L2 fetch-granularity hint (bytes, <= 128). */
+wrs_status wrs_set_l2_fetch_granularity(uint32_t bytes);
+wrs_status wrs_get_l2_fetch_granularity(uint32_t* bytes);
+/* Tunes one distribution: n device weights, s samples into `samples` (device, s entries;
+ * s = 0 tunes the build alone).  `base` is an alias-method configuration; space NULL = the
+ * defaults above; up to max_trials measurements are written to trials (may be NULL). */
+wrs_status wrs_autotune_alias(const wrs_config* base, void* stream, const float* weights,
+                              uint32_t n, uint64_t s, uint32_t* samples,
+                              const wrs_tune_space* space, wrs_tune_result* out,
+                              wrs_tune_trial* trials, uint32_t max_trials);
+/* Tunes a batch: the distributions are those wrs_batch_set would take. */
+wrs_status wrs_autotune_batch(const wrs_config* base, void* stream, const wrs_dist_desc* descs,
+                              uint32_t count, const wrs_tune_space* space, wrs_tune_result* out,
+                              wrs_tune_trial* trials, uint32_t max_trials);
+
 #ifdef __cplusplus
 }
 #endif

@@ -70,6 +70,22 @@ class ServerStats(C.Structure):
         "table_arena_bytes", "table_bytes_peak", "scratch_bytes", "device_status")]
 
 
+class TuneSpace(C.Structure):
+    _fields_ = [("split_sizes", C.POINTER(C.c_uint32)), ("split_count", C.c_uint32),
+                ("l2_fetch", C.POINTER(C.c_uint32)), ("l2_count", C.c_uint32),
+                ("warmup", C.c_uint32), ("reps", C.c_uint32)]
+
+
+class TuneTrial(C.Structure):
+    _fields_ = [("split_size", C.c_uint32), ("l2_fetch", C.c_uint32), ("build_ms", C.c_float),
+                ("sample_ms", C.c_float)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("split_size", C.c_uint32), ("l2_fetch", C.c_uint32), ("build_ms", C.c_float),
+                ("sample_ms", C.c_float), ("trials", C.c_uint32)]
+
+
 _lib: C.CDLL | None = None
 
 
@@ -141,6 +157,12 @@ def lib() -> C.CDLL:
             "wrs_server_get_stats": (i32, [vp, C.POINTER(ServerStats)]),
             "wrs_server_run_trace": (i32, [vp, C.POINTER(Request), C.POINTER(C.c_double), u32,
                                            C.POINTER(Completion)]),
+            "wrs_set_l2_fetch_granularity": (i32, [u32]),
+            "wrs_get_l2_fetch_granularity": (i32, [C.POINTER(u32)]),
+            "wrs_autotune_alias": (i32, [cfgp, vp, vp, u32, u64, vp, C.POINTER(TuneSpace),
+                                         C.POINTER(TuneResult), C.POINTER(TuneTrial), u32]),
+            "wrs_autotune_batch": (i32, [cfgp, vp, vp, u32, C.POINTER(TuneSpace),
+                                         C.POINTER(TuneResult), C.POINTER(TuneTrial), u32]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -493,3 +515,75 @@ class Statistics:
         o = self.out.cpu().tolist()
         return {"chi2": o[0], "rmse": o[1], "zero_weight_draws": int(o[2]), "total": o[3],
                 "out_of_range": bool(int(self.status.item()) & 4)}
+
+
+def set_l2_fetch_granularity(nbytes: int) -> None:
+    """The CUDA context's L2 fetch-granularity hint (bytes, <= 128); context-wide."""
+    check(lib().wrs_set_l2_fetch_granularity(nbytes))
+
+
+def get_l2_fetch_granularity() -> int:
+    v = C.c_uint32()
+    check(lib().wrs_get_l2_fetch_granularity(C.byref(v)))
+    return v.value
+
+
+def _tune_space(split_sizes, l2_fetch, warmup, reps):
+    sp = TuneSpace()
+    keep = []
+    if split_sizes is not None:
+        arr = (C.c_uint32 * max(1, len(split_sizes)))(*split_sizes)
+        keep.append(arr)
+        sp.split_sizes = C.cast(arr, C.POINTER(C.c_uint32)) if len(split_sizes) else None
+        sp.split_count = len(split_sizes)
+    else:
+        sp.split_count = 1  # NULL with a nonzero count: the default candidates
+    if l2_fetch is not None:
+        arr = (C.c_uint32 * max(1, len(l2_fetch)))(*l2_fetch)
+        keep.append(arr)
+        sp.l2_fetch = C.cast(arr, C.POINTER(C.c_uint32)) if len(l2_fetch) else None
+        sp.l2_count = len(l2_fetch)
+    else:
+        sp.l2_count = 1
+    sp.warmup, sp.reps = warmup, reps
+    return sp, keep
+
+
+def _tune_out(res: TuneResult, trials) -> dict:
+    return {"split_size": res.split_size, "l2_fetch": res.l2_fetch,
+            "build_ms": res.build_ms, "sample_ms": res.sample_ms,
+            "trials": [{"split_size": t.split_size, "l2_fetch": t.l2_fetch,
+                        "build_ms": t.build_ms, "sample_ms": t.sample_ms}
+                       for t in trials[:min(res.trials, len(trials))]]}
+
+
+def autotune_alias(config: WRSConfig, stream, weights, n: int, s: int = 0, samples=None,
+                   split_sizes=None, l2_fetch=None, warmup: int = 1, reps: int = 3) -> dict:
+    """wrs_autotune_alias: fastest split size and L2 fetch granularity for building n weights
+    and drawing s samples (the context's L2 limit is left at the chosen value).
+    split_sizes / l2_fetch None = the library's candidates, [] = not tuned."""
+    sp, keep = _tune_space(split_sizes, l2_fetch, warmup, reps)
+    res = TuneResult()
+    trials = (TuneTrial * 32)()
+    cfg = config.c()
+    check(lib().wrs_autotune_alias(C.byref(cfg), _stream_ptr(stream), _dev_ptr(weights), n, s,
+                                   _dev_ptr(samples), C.byref(sp), C.byref(res), trials, 32))
+    del keep
+    return _tune_out(res, trials)
+
+
+def autotune_batch(config: WRSConfig, stream, dists, split_sizes=None, l2_fetch=None,
+                   warmup: int = 1, reps: int = 3) -> dict:
+    """wrs_autotune_batch over dists as Batch.set takes them."""
+    dists = list(dists)
+    arr = (DistDesc * max(1, len(dists)))()
+    for i, (w, t, out, n, s, seed) in enumerate(dists):
+        arr[i] = DistDesc(_dev_ptr(w), _dev_ptr(t), _dev_ptr(out), s, seed, n, 0)
+    sp, keep = _tune_space(split_sizes, l2_fetch, warmup, reps)
+    res = TuneResult()
+    trials = (TuneTrial * 32)()
+    cfg = config.c()
+    check(lib().wrs_autotune_batch(C.byref(cfg), _stream_ptr(stream), arr, len(dists),
+                                   C.byref(sp), C.byref(res), trials, 32))
+    del keep
+    return _tune_out(res, trials)

@@ -169,3 +169,30 @@ def test_statistics_and_probe_argument_checks_on_host(pkg):
     assert L.wrs_sample_statistics(None, 8, 8, 0, 5, 128, 8) == 1      # n == 0
     assert L.wrs_probe_random_gather(None, 256, 1 << 20, 16, 12, 8) == 1   # width 12
     assert L.wrs_probe_random_gather(None, 8, 1 << 20, 16, 16, 8) == 1    # misaligned buffer
+
+
+def test_autotune_argument_checks_on_host(pkg):
+    w = pkg.wrs
+    L = w.lib()
+    assert L.wrs_set_l2_fetch_granularity(200) == 1             # above 128 bytes
+    assert L.wrs_get_l2_fetch_granularity(None) == 1
+    res = w.TuneResult()
+    alias = w.AliasTableConfig(split_size=8).c()
+    its = w.ITSConfig().c()
+    assert L.wrs_autotune_alias(None, None, 8, 16, 0, None, None, C.byref(res), None, 0) == 1
+    assert L.wrs_autotune_alias(C.byref(its), None, 8, 16, 0, None, None, C.byref(res), None,
+                                0) == 5                          # alias method only
+    assert L.wrs_autotune_alias(C.byref(alias), None, None, 16, 0, None, None, C.byref(res),
+                                None, 0) == 1                    # no weights
+    assert L.wrs_autotune_alias(C.byref(alias), None, 8, 0, 0, None, None, C.byref(res), None,
+                                0) == 1                          # n == 0
+    assert L.wrs_autotune_alias(C.byref(alias), None, 8, 16, 4, None, None, C.byref(res), None,
+                                0) == 1                          # samples without a buffer
+    bad_l2, keep = w._tune_space(None, [64, 256], 1, 1)
+    assert L.wrs_autotune_alias(C.byref(alias), None, 8, 16, 0, None, C.byref(bad_l2),
+                                C.byref(res), None, 0) == 1      # L2 candidate above 128
+    bad_split, keep2 = w._tune_space([0, 8], [], 1, 1)
+    assert L.wrs_autotune_alias(C.byref(alias), None, 8, 16, 0, None, C.byref(bad_split),
+                                C.byref(res), None, 0) == 1      # split size 0
+    assert L.wrs_autotune_batch(C.byref(alias), None, None, 0, None, C.byref(res), None,
+                                0) == 1                          # no distributions
