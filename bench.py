@@ -58,6 +58,8 @@ METRIC = "samples/s"
 # float-float table accuracy does not depend on it).  The batched configuration tunes its
 # split size live.
 SPLIT_SIZE = 12
+# end-to-end: the samples of a step leave the device in this many pieces
+E2E_CHUNKS = 8
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "alias_sample_n26_s28.md")
 
 
@@ -357,18 +359,26 @@ def main() -> None:
 
     # ---- end to end through the C ABI with host buffers.  Every step copies its weights from
     # pinned host memory (cudaMemcpyAsync on a copy stream, into one of two device buffers, so
-    # the next step's copy overlaps this step's work) and hands wrs_sample the pinned host
-    # buffer as the output: the sampling kernel writes the samples straight into host memory
-    # over NVLink-C2C.  e2e_serial: the same with one device buffer and a separate D2H copy,
-    # all on one stream.
+    # the next step's copy overlaps this step's work), builds, and samples in E2E_CHUNKS
+    # pieces (wrs_sample_at with the piece's offset) into one of two device sample buffers;
+    # each piece's device-to-host copy into pinned host memory starts on an output stream as
+    # soon as the piece is drawn, so the host link carries the samples while the device draws
+    # the rest and builds the next step.  The last step's copies end inside the timed region.
+    # e2e_kernel_to_host: the sampling kernel writes straight into pinned host memory;
+    # e2e_serial: one device buffer, copies and work all on one stream.
     host_w = [weights[d].cpu().pin_memory() for d in range(3)]
     host_s = torch.empty(s, dtype=torch.int32).pin_memory()
     dev_w2 = [torch.empty(n, dtype=torch.float32, device=dev) for _ in range(2)]
+    dev_s2 = [samples, torch.empty(s, dtype=torch.int32, device=dev)]
     cstream = torch.cuda.Stream(device=dev)
+    ostream = torch.cuda.Stream(device=dev)
     ready = [torch.cuda.Event() for _ in range(2)]
     free = [torch.cuda.Event() for _ in range(2)]
+    copied = [torch.cuda.Event() for _ in range(2)]
+    drawn = [[torch.cuda.Event() for _ in range(E2E_CHUNKS)] for _ in range(2)]
+    L = W.lib()
 
-    def e2e_step(k: int):
+    def load_build(k: int) -> int:
         b = k % 2
         cstream.wait_event(free[b])
         with torch.cuda.stream(cstream):
@@ -377,6 +387,24 @@ def main() -> None:
         stream.wait_event(ready[b])
         wrs.build(stream, W.WRSBuffers(dev_w2[b], None, internals), n)
         free[b].record(stream)
+        return b
+
+    def e2e_step(k: int):
+        b = load_build(k)
+        stream.wait_event(copied[b])  # the buffer's previous samples have left the device
+        piece = s // E2E_CHUNKS
+        for c in range(E2E_CHUNKS):
+            off = c * piece
+            W.check(L.wrs_sample_at(wrs.handle.ptr, stream.cuda_stream, internals.ptr, n, piece,
+                                    1234 + k, off, dev_s2[b].data_ptr() + 4 * off))
+            drawn[b][c].record(stream)
+            ostream.wait_event(drawn[b][c])
+            with torch.cuda.stream(ostream):
+                host_s[off:off + piece].copy_(dev_s2[b][off:off + piece], non_blocking=True)
+        copied[b].record(ostream)
+
+    def e2e_kernel_to_host_step(k: int):
+        b = load_build(k)
         wrs.sample(stream, W.WRSBuffers(dev_w2[b], host_s.data_ptr(), internals), n, s,
                    seed=1234 + k)
 
@@ -387,17 +415,20 @@ def main() -> None:
         host_s.copy_(samples, non_blocking=True)
 
     def e2e_time(fn) -> float:
-        for e in free:
+        for e in free + copied:
             e.record(stream)
         for k in range(min(args.warmup, 2)):
             fn(k)
+        stream.wait_stream(ostream)
         barrier()
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record(stream)
         cstream.wait_stream(stream)  # no copy starts before t0
+        ostream.wait_stream(stream)
         for k in range(args.steps):
             fn(k)
+        stream.wait_stream(ostream)  # the last samples are in host memory
         t1.record(stream)
         torch.cuda.synchronize()
         ms = t0.elapsed_time(t1)
@@ -409,7 +440,9 @@ def main() -> None:
 
     e2e_ms = e2e_time(e2e_step)
     e2e_value = world * args.steps * s / (e2e_ms / 1e3)
+    e2e_k2h_value = world * args.steps * s / (e2e_time(e2e_kernel_to_host_step) / 1e3)
     e2e_serial_value = world * args.steps * s / (e2e_time(e2e_serial_step) / 1e3)
+    link = host_link_rates(host_s, samples, host_w[0], dev_w2[0], stream)
     check = host_s[:1024].numpy().view(np.uint32)
     assert int(check.max()) < n, "samples written to host memory out of range"
 
@@ -450,9 +483,13 @@ def main() -> None:
         "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 4 * n,
                 "d2h_bytes_per_step": 4 * s,
                 "method": "weights: pinned host -> device copy per step on a copy stream, "
-                          "double-buffered (overlaps the previous step); samples: written by "
-                          "the sampling kernel directly into pinned host memory (NVLink-C2C)",
-                "serial_value": e2e_serial_value},
+                          "double-buffered (overlaps the previous step); samples: drawn in "
+                          f"{E2E_CHUNKS} pieces into one of two device buffers, each piece "
+                          "copied to pinned host memory on an output stream as soon as it is "
+                          "drawn (overlaps the rest of the step and the next build)",
+                "kernel_to_host_value": e2e_k2h_value,
+                "serial_value": e2e_serial_value,
+                "host_link": link},
         "roofline": roofline,
         "alias_builds_per_s": world / (statistics.mean(build_ms) / 1e3),
         "build_ms_mean": statistics.mean(build_ms),
@@ -852,6 +889,25 @@ def small_leg(W, dev, steps: int = 20) -> dict:
             "chi2": st["chi2"], "df": n - 1, "p_value": pval, "rmse": st["rmse"],
             "rmse_ideal": float(np.sqrt(np.mean(p * (1 - p) / s))),
             "statistics": "wrs_histogram + wrs_sample_statistics on the device"}
+
+
+def host_link_rates(host_s, dev_s, host_w, dev_w, stream) -> dict:
+    """Pinned host <-> device copy rates (cudaMemcpyAsync, CUDA events, 3 copies each after
+    one warm-up): the bound of the end-to-end figure, which moves 4 B per sample off the
+    device and 4 B per weight onto it every step."""
+    import torch
+    out = {}
+    for name, dst, src in (("d2h_GBs", host_s, dev_s), ("h2d_GBs", dev_w, host_w)):
+        dst.copy_(src, non_blocking=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = 3 * src.numel() * src.element_size() / (e0.elapsed_time(e1) / 1e3) / 1e9
+    out["e2e_bound_samples_per_s"] = out["d2h_GBs"] * 1e9 / 4.0
+    return out
 
 
 def random_gather_rate(W, internals, n: int, s: int, stream) -> float:
