@@ -980,9 +980,18 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
     # through the buffers API: the compensated build also makes the guiding table, and
     # sampling runs the guided search (same samples as the bisection)
     its_bufs = W.WRSBuffers(w, samples, W.Internals(its.handle, n))
-    its.build(stream, its_bufs, n)
-    rec("its_sample_guided", timed(lambda: its.sample(stream, its_bufs, n, s, seed=99)), 4 * s,
+    rec("its_build", timed(lambda: its.build(stream, its_bufs, n)), 8 * n, n, "weights")
+    rec("its_sample_cells", timed(lambda: its.sample(stream, its_bufs, n, s, seed=99)), 4 * s,
         s, "samples")
+    # guiding-table granularity of the guided search: build (scan + table) and sampling time
+    sweep = {}
+    for entry in (2, 3, 4, 6, 8):
+        h = W.WRS(W.ITSConfig(rng=W.RNG_PHILOX4X32_10, scan_precision=W.SCAN_COMPENSATED,
+                              guiding_entry_size=entry))
+        bufs = W.WRSBuffers(w, samples, W.Internals(h.handle, n))
+        sweep[entry] = {"build_ms": timed(lambda: h.build(stream, bufs, n)) * 1e3,
+                        "sample_ms": timed(lambda: h.sample(stream, bufs, n, s, seed=99)) * 1e3}
+    out["its_guide_entry_sweep"] = sweep
     cp = W.WRS(W.CutpointConfig(128))
     G = (n + 127) // 128
     guide = torch.empty(G, dtype=torch.int32, device=w.device)

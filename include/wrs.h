@@ -114,7 +114,13 @@ typedef struct wrs_config {
                                         light bucket extra mass; 0 = reference behaviour */
     uint32_t guiding_entry_size;     /* Cutpoint: CutpointConfig::guidingEntrySize, weights per
                                         guiding-table entry (table size ceil(N / this));
-                                        default 32 */
+                                        default 32.  ITS in the compensated precisions with
+                                        coop 0: the CMF is cut into as many equal-mass cells,
+                                        each stored as a 32-byte block (its first index and 7
+                                        CMF values), and each sample reads the block of its
+                                        cell instead of bisecting the whole CMF (indices
+                                        unchanged, the CMF being exactly non-decreasing);
+                                        0 = no cells, every search bisects; default 4 */
 } wrs_config;
 
 typedef struct wrs_alias_entry {

@@ -5,9 +5,11 @@
 // caller-owned weights and samples) in a single device allocation.  Launch sequences:
 //   alias build : k_total_mass -> k_prefix_partition -> k_split_pack
 //                 (PSA::run, src/device/wrs/alias/psa/PSA.hpp:170-237)
-//   ITS build   : k_scan (ITS::build, src/device/wrs/its/ITS.hpp:90-108)
-//   Cutpoint    : k_scan -> k_cutpoint_guide (Cutpoint::build, src/device/wrs/cutpoint/Cutpoint.hpp:108-138)
-//   sample      : k_alias_sample | k_its_sample | k_cutpoint_sample
+//   ITS build   : k_scan (ITS::build, src/device/wrs/its/ITS.hpp:90-108), then in the
+//                 compensated precisions k_its_cells (the cell blocks k_its_sample_cells reads)
+//   Cutpoint    : k_scan -> k_cutpoint_guide, or k_guide_monotone on the compensated CMF
+//                 (Cutpoint::build, src/device/wrs/cutpoint/Cutpoint.hpp:108-138)
+//   sample      : k_alias_sample | k_its_sample (k_its_sample_cells) | k_cutpoint_sample
 //                 (WRS::sample, src/device/wrs/WRS.hpp:145-168)
 //   batch       : k_batch_maps (wrs_batch_set), then the same three build kernels and the
 //                 alias sampler over all distributions of a batch, one launch each
@@ -44,6 +46,8 @@ struct wrs_buffers {
     uint2* table = nullptr;
     float* cmf = nullptr;
     uint32_t* guide = nullptr;
+    ItsCell* cells = nullptr;
+    uint32_t* coarse = nullptr;  // scratch of the guiding-table / cell construction
 };
 
 namespace {
@@ -72,7 +76,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct Layout {
     size_t ctrl, partials, part_states, scan_states, idx, prefix, elems, prefix_lo, table, cmf,
-        guide, total;
+        guide, cells, coarse, total;
 };
 
 Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
@@ -101,11 +105,15 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
         L.table = take(sizeof(uint2) * static_cast<size_t>(max_n));
     } else {
         L.cmf = take(sizeof(float) * static_cast<size_t>(max_n));
-        // Cutpoint: its guiding table; ITS: the table that guides sampling on the
-        // compensated (exactly non-decreasing) CMF
-        L.guide = take(sizeof(uint32_t) *
-                       guide_entries(max_n, cfg.method == WRS_METHOD_CUTPOINT ? cfg.guiding_entry_size
-                                                                              : kItsGuideEntry));
+        // Cutpoint: its guiding table; ITS: the cell blocks that steer sampling on the
+        // compensated (exactly non-decreasing) CMF (none with guiding_entry_size 0)
+        const uint32_t G = cfg.guiding_entry_size ? guide_entries(max_n, cfg.guiding_entry_size) : 0;
+        if (cfg.method == WRS_METHOD_CUTPOINT)
+            L.guide = take(sizeof(uint32_t) * G);
+        else if (G && cfg.scan_precision != WRS_SCAN_FP32)
+            L.cells = take(sizeof(ItsCell) * G);
+        if (G && cfg.scan_precision != WRS_SCAN_FP32)
+            L.coarse = take(sizeof(uint32_t) * coarse_entries(G));
     }
     L.total = off;
     return L;
@@ -180,7 +188,7 @@ wrs_status wrs_config_init(wrs_config* cfg, uint32_t method) {
     cfg->scan_precision = WRS_SCAN_FP32;
     cfg->split_residual_f64 = 0;
     cfg->split_full_light = 0;
-    cfg->guiding_entry_size = 32;
+    cfg->guiding_entry_size = method == WRS_METHOD_ITS ? 4u : 32u;
     return check_config(cfg);
 }
 
@@ -237,7 +245,9 @@ wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers**
         b->table = reinterpret_cast<uint2*>(p + L.table);
     } else {
         b->cmf = reinterpret_cast<float*>(p + L.cmf);
-        b->guide = reinterpret_cast<uint32_t*>(p + L.guide);
+        b->guide = L.guide ? reinterpret_cast<uint32_t*>(p + L.guide) : nullptr;
+        b->cells = L.cells ? reinterpret_cast<ItsCell*>(p + L.cells) : nullptr;
+        b->coarse = L.coarse ? reinterpret_cast<uint32_t*>(p + L.coarse) : nullptr;
     }
     e = cudaMemset(b->base, 0, zeroed_bytes(h->cfg, max_n));
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -288,6 +298,24 @@ static bool float_float(const wrs_handle* h) {
 }
 static bool compensated(const wrs_handle* h) {
     return h->cfg.scan_precision != WRS_SCAN_FP32;
+}
+// ITS sampling steered by a guiding table: the compensated CMF is exactly non-decreasing, so
+// any lower-bound search returns the bisection's index
+static bool its_guided(const wrs_handle* h) {
+    return h->cfg.method == WRS_METHOD_ITS && compensated(h) && h->cfg.coop_size == 0 &&
+           h->cfg.guiding_entry_size != 0;
+}
+// the guiding table / cell blocks the handle will use exist in b and have its size
+static wrs_status check_tables(const wrs_handle* h, const wrs_buffers* b) {
+    if ((h->cfg.method == WRS_METHOD_CUTPOINT || its_guided(h)) &&
+        b->cfg.guiding_entry_size != h->cfg.guiding_entry_size)
+        return fail(WRS_ERR_INVALID_ARG, "buffers were created for another guiding_entry_size");
+    if ((its_guided(h) && !b->cells) ||
+        ((h->cfg.method == WRS_METHOD_CUTPOINT || its_guided(h)) && compensated(h) && !b->coarse))
+        return fail(WRS_ERR_INVALID_ARG,
+                    "buffers were created for the FP32 precision (no cells or construction "
+                    "scratch for the compensated CMF)");
+    return WRS_OK;
 }
 
 wrs_status wrs_prefix_partition(const wrs_handle* h, void* stream, const float* weights,
@@ -387,19 +415,22 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
     if (s != WRS_OK) return s;
     if (b->cfg.method != h->cfg.method)
         return fail(WRS_ERR_INVALID_ARG, "buffers were created for another method");
+    if ((s = check_tables(h, b)) != WRS_OK) return s;
     const cudaStream_t st = as_stream(stream);
     const bool comp = compensated(h);
     if (h->cfg.method != WRS_METHOD_ALIAS_TABLE) {
         WRS_CUDA(launch_scan(st, comp, weights, n, b->cmf, b->ctrl, b->scan_states, b->cap_tiles,
                              b->partials),
                  "ITS build");
+        // the compensated CMF is exactly non-decreasing: the galloping construction gives
+        // the bisection's entries
+        const uint32_t G = guide_entries(n, h->cfg.guiding_entry_size);
         if (h->cfg.method == WRS_METHOD_CUTPOINT)
-            WRS_CUDA(launch_cutpoint_guide(st, b->cmf, n, guide_entries(n, h->cfg.guiding_entry_size),
-                                           b->guide),
+            WRS_CUDA(comp ? launch_guide_monotone(st, b->cmf, n, G, b->coarse, b->guide)
+                          : launch_cutpoint_guide(st, b->cmf, n, G, b->guide),
                      "guiding table");
-        else if (comp)
-            WRS_CUDA(launch_cutpoint_guide(st, b->cmf, n, guide_entries(n, kItsGuideEntry), b->guide),
-                     "ITS guiding table");
+        else if (its_guided(h))
+            WRS_CUDA(launch_its_cells(st, b->cmf, n, G, b->coarse, b->cells), "ITS cells");
         return WRS_OK;
     }
     if (h->cfg.use_partition_elements && !b->elems)
@@ -426,14 +457,15 @@ wrs_status wrs_sample_at(const wrs_handle* h, void* stream, const wrs_buffers* b
     if (st != WRS_OK) return st;
     if (b->cfg.method != h->cfg.method)
         return fail(WRS_ERR_INVALID_ARG, "buffers were created for another method");
+    if ((st = check_tables(h, b)) != WRS_OK) return st;
     if (h->cfg.method == WRS_METHOD_ITS) {
-        if (compensated(h) && h->cfg.coop_size == 0 && s) {
-            // the compensated CMF is non-decreasing: the guided search returns the bisection's
-            // index (see k_its_sample_guided)
+        if (its_guided(h) && s) {
+            // the compensated CMF is non-decreasing: the cell-block search returns the
+            // bisection's index (see k_its_sample_cells)
             if (!samples) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
-            WRS_CUDA(launch_its_sample_guided(as_stream(stream), h->cfg.rng, b->cmf, n, b->guide,
-                                              guide_entries(n, kItsGuideEntry), s, seed, offset,
-                                              samples),
+            WRS_CUDA(launch_its_sample_cells(as_stream(stream), h->cfg.rng, b->cmf, n, b->cells,
+                                             guide_entries(n, h->cfg.guiding_entry_size), s,
+                                             seed, offset, samples),
                      "its sample");
             return WRS_OK;
         }

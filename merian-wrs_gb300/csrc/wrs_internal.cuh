@@ -136,11 +136,29 @@ cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool
 
 cudaError_t launch_cutpoint_guide(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
                                   uint32_t* guide);
-// ITS on a non-decreasing CMF with a guiding table of kItsGuideEntry weights per entry
-constexpr uint32_t kItsGuideEntry = 32;
-cudaError_t launch_its_sample_guided(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
-                                     const uint32_t* guide, uint32_t G, uint64_t S, uint64_t seed,
-                                     uint64_t offset, uint32_t* out);
+// the same table for an exactly non-decreasing CMF (galloping searches)
+// (coarse: scratch of coarse_entries(G) words: every kCoarseStride-th entry, bracketing the
+// searches of the others)
+constexpr uint32_t kCoarseStride = 1024;
+__host__ __device__ inline uint32_t coarse_entries(uint32_t G) {
+    return (G + kCoarseStride - 1) / kCoarseStride + 1;
+}
+cudaError_t launch_guide_monotone(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
+                                  uint32_t* coarse, uint32_t* guide);
+// ITS on a non-decreasing CMF through cell blocks: cell k of G equal-mass cells (the Cutpoint
+// guiding table's) = its candidate range [x, y] and the CMF at the last index of each of the
+// range's kCellParts parts of d = ceil((y - x + 1) / kCellParts) indices; one 32-byte sector
+constexpr int kCellParts = 6;
+struct alignas(32) ItsCell {
+    uint32_t x, y;
+    float v[kCellParts];
+};
+static_assert(sizeof(ItsCell) == 32, "one cell block is one 32-byte sector");
+cudaError_t launch_its_cells(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
+                             uint32_t* coarse, ItsCell* cells);
+cudaError_t launch_its_sample_cells(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
+                                    const ItsCell* cells, uint32_t G, uint64_t S, uint64_t seed,
+                                    uint64_t offset, uint32_t* out);
 cudaError_t launch_cutpoint_sample(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
                                    const uint32_t* guide, uint32_t G, uint64_t S, uint64_t seed,
                                    uint64_t offset, uint32_t* out);

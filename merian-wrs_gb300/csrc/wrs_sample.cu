@@ -387,17 +387,88 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_tree(const float*
     }
 }
 
-// ---- ITS on an exactly non-decreasing CMF, guided ---------------------------------------
+// ---- ITS on an exactly non-decreasing CMF: cell blocks ----------------------------------
 //
-// On a non-decreasing CMF every lower-bound search returns the same index, so the bisection
-// can start from a guiding-table cell instead of [0, N - 1] (the compensated scan's CMF is
-// non-decreasing by construction).  guide[k] = lower bound of fl(fl(total / G) * k) (the
-// Cutpoint guiding table, G = ceil(N / 32)); the target's cell comes from an FP32 estimate and
-// is accepted only if cmf[x - 1] < T <= cmf[y] holds for its range [x, y] (exact comparisons),
-// else the search falls back to the whole CMF.  Results equal k_its_sample_tree's.
+// On a non-decreasing CMF every lower-bound search returns the same index, so the search can
+// start anywhere that brackets the answer (the compensated scan's CMF is non-decreasing by
+// construction).  The CMF's range is cut into G = ceil(N / entry) cells of equal mass, the
+// Cutpoint guiding table's: cell k starts at x_k = lower bound of c_k = fl(fl(total / G) * k),
+// and a target T with c_k < T <= c_{k+1} has its lower bound in [x_k, y_k], y_k = x_{k+1}
+// (N - 1 for the last cell).  Cell k is stored as one 32-byte block (ItsCell): x_k, y_k and,
+// for the range cut into kCellParts parts of d = ceil((y - x + 1) / kCellParts) indices, the
+// CMF at the last index of each part (min(x + (j + 1) d - 1, y)).  A sample finds its cell (an
+// FP32 estimate moved by exact comparisons against c_k), reads the block with one 32-byte
+// load -- one random sector, what an alias-table entry costs (a random 64-byte read costs
+// about twice that on GB300) -- and the first part whose last value is >= T holds the lower
+// bound: with d = 1 (cells of at most kCellParts candidates) that is the answer, otherwise a
+// bisection of the part's d indices of the CMF finds it.  A target above the block's last
+// value (a cell estimate that did not settle) falls back to the bisection of [0, N - 1].
+// Results equal the bisection's (k_its_sample_tree's).
+
+// Starts x_k = lower bound of c_k = fl(step * k) (clamped to N - 1) of the equal-mass cells of
+// a non-decreasing CMF, in two passes.  k_cell_coarse bisects the whole CMF for every
+// kCoarseStride-th start (coarse[j] = x_{j * kCoarseStride}, coarse[ceil(G / stride)] = N - 1);
+// then each cell's start lies in [coarse[j], coarse[j + 1]] (c_k is non-decreasing in k) and
+// one thread per cell bisects only that bracket.  Consecutive cells' threads share the top of
+// their searches and finish within a few hundred bytes of each other, in L1.
+__device__ __forceinline__ float cell_step(const float* __restrict__ cmf, uint32_t n, uint32_t G) {
+    return __fdiv_rn(__ldg(cmf + n - 1u), __uint2float_rn(G));
+}
+
+__global__ __launch_bounds__(kSampleThreads) void k_cell_coarse(const float* __restrict__ cmf,
+                                                                uint32_t n, uint32_t G,
+                                                                uint32_t* __restrict__ coarse) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= coarse_entries(G)) return;
+    const uint64_t k = static_cast<uint64_t>(j) * kCoarseStride;
+    coarse[j] = k < G ? bisect(cmf, 0, n - 1u,
+                               __fmul_rn(cell_step(cmf, n, G), __uint2float_rn(static_cast<uint32_t>(k))))
+                      : n - 1u;
+}
+
+__device__ __forceinline__ uint32_t cell_start(const float* __restrict__ cmf, uint32_t n,
+                                               uint32_t G, const uint32_t* __restrict__ coarse,
+                                               uint32_t k) {
+    const uint32_t j = k / kCoarseStride;
+    const uint32_t lo = __ldg(coarse + j);
+    if (k % kCoarseStride == 0u) return lo;
+    return bisect(cmf, lo, __ldg(coarse + j + 1u),
+                  __fmul_rn(cell_step(cmf, n, G), __uint2float_rn(k)));
+}
+
+__device__ __forceinline__ uint32_t cell_part(uint32_t x, uint32_t y) {
+    return (y - x + kCellParts) / kCellParts;  // ceil((y - x + 1) / kCellParts)
+}
+
+__global__ __launch_bounds__(kSampleThreads) void k_its_cells(const float* __restrict__ cmf,
+                                                              uint32_t n, uint32_t G,
+                                                              const uint32_t* __restrict__ coarse,
+                                                              ItsCell* __restrict__ cells) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;  // whole warps are launched
+    const uint32_t x = k < G ? cell_start(cmf, n, G, coarse, k) : n - 1u;
+    // the end of a cell is the next cell's start: the next lane's, except for the last lane
+    uint32_t y = __shfl_down_sync(0xffffffffu, x, 1);
+    if ((threadIdx.x & 31u) == 31u) y = k + 1u < G ? cell_start(cmf, n, G, coarse, k + 1u) : n - 1u;
+    if (k >= G) return;
+    if (k + 1u >= G) y = n - 1u;
+    const uint32_t d = cell_part(x, y);
+    float v[kCellParts];
+#pragma unroll
+    for (int j = 0; j < kCellParts; ++j)
+        v[j] = __ldg(cmf + min(x + (j + 1) * d - 1u, y));
+    uint4* dst = reinterpret_cast<uint4*>(cells + k);
+    dst[0] = make_uint4(x, y, __float_as_uint(v[0]), __float_as_uint(v[1]));
+    dst[1] = make_uint4(__float_as_uint(v[2]), __float_as_uint(v[3]), __float_as_uint(v[4]),
+                        __float_as_uint(v[5]));
+}
+
+// steps of the cell correction (beyond them the bracket check sends the sample to the
+// bisection, so the bound only caps the work)
+constexpr int kCellFix = 8;
+
 template <uint32_t RNG>
-__global__ __launch_bounds__(kSampleThreads) void k_its_sample_guided(
-    const float* __restrict__ cmf, uint32_t n, const uint32_t* __restrict__ guide, uint32_t G,
+__global__ __launch_bounds__(kSampleThreads) void k_its_sample_cells(
+    const float* __restrict__ cmf, uint32_t n, const ItsCell* __restrict__ cells, uint32_t G,
     uint64_t S, uint64_t seed, uint64_t offset, uint32_t* __restrict__ out) {
     const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (s >= S) return;
@@ -419,18 +490,46 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_guided(
     }
     // "T > c" for the target T = (t_hi, t_sgn) (RNG_REF: t_sgn = 0, the shader's u > cmf[mid])
     auto above = [&](float c) { return t_hi > c || (t_hi == c && t_sgn > 0); };
+    // the cell holding T: c_k < T <= c_{k+1} with the build's c_k = fl(step * k), from an FP32
+    // estimate (off by a few cells at most) moved by exact comparisons
+    const float step = __fdiv_rn(total, __uint2float_rn(G));
     const float scale = __fdiv_rn(__uint2float_rn(G), total);
     uint32_t k = __float2uint_rz(__fmul_rn(t_hi, scale));
     k = k < G - 1u ? k : G - 1u;
-    uint32_t x = __ldg(guide + k);
-    uint32_t y = k + 1u < G ? __ldg(guide + k + 1u) : last;
-    if (!((x == 0 || above(__ldg(cmf + x - 1u))) && !above(__ldg(cmf + y)))) {
+    for (int it = 0; it < kCellFix && k > 0u && !above(__fmul_rn(step, __uint2float_rn(k))); ++it)
+        --k;
+    for (int it = 0; it < kCellFix && k + 1u < G && above(__fmul_rn(step, __uint2float_rn(k + 1u)));
+         ++it)
+        ++k;
+    // c_k < T (then cmf[x_k - 1] < c_k < T); the upper side is checked on the block
+    const bool settled = k == 0u || above(__fmul_rn(step, __uint2float_rn(k)));
+    const uint64_t once = l2_policy_evict_first();
+    uint4 q0, q1;
+    ld_u32x8_policy(reinterpret_cast<const uint32_t*>(cells + k), once, q0, q1);
+    uint32_t x = q0.x, y = q0.y;
+    const float v[kCellParts] = {__uint_as_float(q0.z), __uint_as_float(q0.w),
+                                 __uint_as_float(q1.x), __uint_as_float(q1.y),
+                                 __uint_as_float(q1.z), __uint_as_float(q1.w)};
+    if (settled && !above(v[kCellParts - 1])) {
+        // the first part whose last value is >= T (the values are non-decreasing)
+        uint32_t part = 0;
+#pragma unroll
+        for (int j = 0; j < kCellParts; ++j) part += above(v[j]) ? 1u : 0u;
+        const uint32_t d = cell_part(x, y);
+        const uint32_t lo = x + part * d;
+        if (d == 1u) {
+            __stcs(out + s, lo);
+            return;
+        }
+        y = min(lo + d - 1u, y);  // cmf[y] >= T and cmf[lo - 1] < T
+        x = lo;
+    } else {
         x = 0;
         y = last;
     }
     while (x < y) {
         const uint32_t mid = x + ((y - x) >> 1);
-        if (above(__ldg(cmf + mid)))
+        if (above(ld_f32_policy(cmf + mid, once)))
             x = mid + 1;
         else
             y = mid;
@@ -438,18 +537,46 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_guided(
     __stcs(out + s, x);
 }
 
-cudaError_t launch_its_sample_guided(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
-                                     const uint32_t* guide, uint32_t G, uint64_t S, uint64_t seed,
-                                     uint64_t offset, uint32_t* out) {
+// Guiding table of an exactly non-decreasing CMF: the same entries as k_cutpoint_guide
+// (guide[k] = lower bound of fl(fl(total / G) * k), clamped to N - 1), where every lower-bound
+// search gives the same index, so the bracketed searches of cell_start apply.
+__global__ __launch_bounds__(kSampleThreads) void k_guide_monotone(const float* __restrict__ cmf,
+                                                                   uint32_t n, uint32_t G,
+                                                                   const uint32_t* __restrict__ coarse,
+                                                                   uint32_t* __restrict__ guide) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < G) guide[k] = cell_start(cmf, n, G, coarse, k);
+}
+
+static cudaError_t launch_cell_coarse(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
+                                      uint32_t* coarse) {
+    const uint32_t m = coarse_entries(G);
+    k_cell_coarse<<<(m + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(cmf, n, G,
+                                                                                        coarse);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_its_cells(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
+                             uint32_t* coarse, ItsCell* cells) {
+    const cudaError_t e = launch_cell_coarse(st, cmf, n, G, coarse);
+    if (e != cudaSuccess) return e;
+    k_its_cells<<<(G + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(cmf, n, G,
+                                                                                      coarse, cells);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_its_sample_cells(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
+                                    const ItsCell* cells, uint32_t G, uint64_t S, uint64_t seed,
+                                    uint64_t offset, uint32_t* out) {
     const uint64_t blocks = (S + kSampleThreads - 1) / kSampleThreads;
     if (blocks == 0) return cudaSuccess;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
     if (rng == RNG_REF)
-        k_its_sample_guided<RNG_REF><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
-            cmf, n, guide, G, S, seed, offset, out);
+        k_its_sample_cells<RNG_REF><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
+            cmf, n, cells, G, S, seed, offset, out);
     else
-        k_its_sample_guided<RNG_PHILOX><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
-            cmf, n, guide, G, S, seed, offset, out);
+        k_its_sample_cells<RNG_PHILOX><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
+            cmf, n, cells, G, S, seed, offset, out);
     return cudaGetLastError();
 }
 
@@ -507,6 +634,15 @@ cudaError_t launch_cutpoint_guide(cudaStream_t st, const float* cmf, uint32_t n,
                                   uint32_t* guide) {
     const uint32_t blocks = (G + kSampleThreads - 1) / kSampleThreads;
     k_cutpoint_guide<<<blocks, kSampleThreads, 0, st>>>(cmf, n, G, guide);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_guide_monotone(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
+                                  uint32_t* coarse, uint32_t* guide) {
+    const cudaError_t e = launch_cell_coarse(st, cmf, n, G, coarse);
+    if (e != cudaSuccess) return e;
+    k_guide_monotone<<<(G + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(
+        cmf, n, G, coarse, guide);
     return cudaGetLastError();
 }
 

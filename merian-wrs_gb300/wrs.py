@@ -236,9 +236,13 @@ def AliasTableConfig(split_size: int = 2, use_partition_elements: bool = True,
     return WRSConfig(METHOD_ALIAS_TABLE, split_size, use_partition_elements, coop_size, **kw)
 
 
-def ITSConfig(coop_size: int = 0, parray: bool = False, **kw) -> WRSConfig:
-    """ITSConfig(DecoupledPrefixSumConfig(), InverseTransformSamplingConfig(512, coop, parray))."""
-    return WRSConfig(METHOD_ITS, coop_size=coop_size, its_parray=parray, **kw)
+def ITSConfig(coop_size: int = 0, parray: bool = False, guiding_entry_size: int = 4,
+              **kw) -> WRSConfig:
+    """ITSConfig(DecoupledPrefixSumConfig(), InverseTransformSamplingConfig(512, coop, parray)).
+    guiding_entry_size: weights per entry of the table that steers the compensated CMF's
+    searches (0 = none); indices do not depend on it."""
+    return WRSConfig(METHOD_ITS, coop_size=coop_size, its_parray=parray,
+                     guiding_entry_size=guiding_entry_size, **kw)
 
 
 def CutpointConfig(guiding_entry_size: int = 32, **kw) -> WRSConfig:

@@ -39,6 +39,8 @@ def test_config_defaults_and_validation(pkg):
     assert L.wrs_config_init(C.byref(cfg), w.METHOD_ALIAS_TABLE) == 0
     assert (cfg.split_size, cfg.use_partition_elements, cfg.rng, cfg.coop_size) == (2, 1, 0, 0)
     assert L.wrs_config_init(C.byref(cfg), w.METHOD_ITS) == 0
+    assert cfg.guiding_entry_size == 4  # the ITS search's cell size (0 = no cells)
+    assert w.Handle(w.ITSConfig(guiding_entry_size=0, scan_precision=w.SCAN_COMPENSATED)).ptr
     # the Cutpoint alternative of WRSConfig (CutpointConfig(..., guidingEntrySize))
     assert L.wrs_config_init(C.byref(cfg), w.METHOD_CUTPOINT) == 0
     assert (cfg.method, cfg.guiding_entry_size, cfg.coop_size) == (w.METHOD_CUTPOINT, 32, 0)

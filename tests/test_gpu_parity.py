@@ -303,18 +303,60 @@ def test_its_sample_bit_exact(pkg, cuda, oracle, rng, coop, parray):
 
 @pytest.mark.parametrize("N", [1, 2, 33, 4097, 300001, (1 << 22) + 3])
 @pytest.mark.parametrize("rng", [RNG_REFERENCE, RNG_PHILOX4X32_10])
-def test_its_guided_sampling_on_the_compensated_cmf(pkg, cuda, oracle, N, rng):
+@pytest.mark.parametrize("entry", [1, 4, 8, 32, 0])
+def test_its_guided_sampling_on_the_compensated_cmf(pkg, cuda, oracle, N, rng, entry):
     """ITS on the compensated (non-decreasing) CMF runs the guided search (a guiding-table cell
-    instead of the whole range): samples equal the oracle's plain bisection, also with runs of
-    zero weights and a heavy tail."""
+    instead of the whole range, its values read with vector loads when the cell is short):
+    samples equal the oracle's plain bisection for every guiding-table granularity (entry 0:
+    no table), also with runs of zero weights and a heavy tail."""
     w = weights_precision(N, N)
     w[0] = max(w[0], np.float32(0.25))
-    b = Built(pkg, w, pkg.ITSConfig(rng=rng, scan_precision=1))
+    b = Built(pkg, w, pkg.ITSConfig(rng=rng, scan_precision=1, guiding_entry_size=entry))
     assert np.all(np.diff(b.cmf.astype(np.float64)) >= 0)
     S = (1 << 20) + 11
     got = b.sample(S, 4242, 7)
     ref = oracle.its_sample(b.cmf, S, 4242, rng=rng, offset=7, nthreads=8)
     assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("gen", ["zipf", "lognormal"])
+@pytest.mark.parametrize("entry", [3, 8])
+def test_its_cells_heavy_heads_and_crowded_cells(pkg, cuda, oracle, gen, entry):
+    """Cell blocks under skewed weights: heavy items span many one-item cells, light regions
+    give crowded cells (more than a block holds) that take the bisection; samples equal the
+    oracle's bisection."""
+    N = (1 << 20) + 7
+    w = GENS[gen](N, 77 + entry)
+    b = Built(pkg, w, pkg.ITSConfig(rng=RNG_PHILOX4X32_10, scan_precision=1,
+                                    guiding_entry_size=entry))
+    S = (1 << 20) + 3
+    got = b.sample(S, 99, 3)
+    assert np.array_equal(got, oracle.its_sample(b.cmf, S, 99, rng=RNG_PHILOX4X32_10, offset=3,
+                                                 nthreads=8))
+
+
+def test_its_buffers_must_hold_the_handles_cells(pkg, cuda):
+    """A compensated ITS handle refuses buffers made without cell blocks (an FP32 handle's)
+    or with another guiding-table granularity, instead of reading past them."""
+    W = pkg.wrs
+    N = 10000
+    w = h2d(weights_uniform(N, 3))
+    fp32 = W.WRS(pkg.ITSConfig(scan_precision=0))
+    comp8 = W.WRS(pkg.ITSConfig(scan_precision=1, guiding_entry_size=8))
+    comp4 = W.WRS(pkg.ITSConfig(scan_precision=1, guiding_entry_size=4))
+    b32 = W.WRSBuffers.allocate(N, 16, fp32.config, handle=fp32.handle)
+    b8 = W.WRSBuffers.allocate(N, 16, comp8.config, handle=comp8.handle)
+    for h, b in ((comp8, b32), (comp4, b8)):
+        b.weights.copy_(w)
+        with pytest.raises(W.WRSError) as e:
+            h.build(None, b, N)
+        assert e.value.status == 1
+        with pytest.raises(W.WRSError):
+            h.sample(None, b, N, 16, 1)
+    b8.weights.copy_(w)
+    comp8.build(None, b8, N)
+    comp8.sample(None, b8, N, 16, 1)
+    assert b8.internals.status() == 0
 
 
 @pytest.mark.parametrize("N", [1, 2, 3, 7, 4095, 4096, 4097, 8191, 8193, 70001])
@@ -337,13 +379,18 @@ def test_its_sample_edge_sizes(pkg, cuda, oracle, N, rng):
 @pytest.mark.parametrize("N,entry", [(1, 32), (5, 1), (1000, 32), (4097, 128), (300001, 32),
                                      ((1 << 20) + 3, 7)])
 @pytest.mark.parametrize("rng", [RNG_REFERENCE, RNG_PHILOX4X32_10])
-def test_cutpoint_bit_exact(pkg, cuda, oracle, N, entry, rng):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_cutpoint_bit_exact(pkg, cuda, oracle, N, entry, rng, precision):
     """Cutpoint (guiding table + guided sampling): the guiding table equals the oracle's
     restatement of cutpoint/guiding_table/shader.comp and the samples its restatement of
-    cutpoint/sampling/shader.comp, given the GPU's CMF."""
+    cutpoint/sampling/shader.comp, given the GPU's CMF.  On the compensated (non-decreasing)
+    CMF the table is built by galloping searches; it must still equal the bisections'."""
     W = pkg.wrs
     w = weights_uniform(N, N + entry)
-    cfg = pkg.CutpointConfig(entry, rng=rng)
+    if precision:
+        w[np.random.default_rng(N).random(N) < 0.3] = 0.0  # runs of equal CMF values
+        w[0] = np.float32(0.5)
+    cfg = pkg.CutpointConfig(entry, rng=rng, scan_precision=precision)
     wrs = W.WRS(cfg)
     bufs = W.WRSBuffers.allocate(N, 1, cfg, handle=wrs.handle)
     bufs.weights.copy_(h2d(w))
