@@ -972,6 +972,26 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
     rec("alias_sample",
         timed(lambda: wrs.alias_sample(stream, table, n, s, 99, 0, samples)), 12 * s, s,
         "samples")
+    # serial split-pack (split records + pack from them), the two pack strategies, against the
+    # inline split-pack at the same split size
+    serial = {}
+    records = torch.empty(3 * (n // 2 + 1), dtype=torch.int32, device=w.device)
+    for split in (SPLIT_SIZE, 256, 1024):
+        row = {}
+        for name, mode in (("inline", W.SPLITPACK_INLINE), ("scalar", W.SPLITPACK_SERIAL),
+                           ("warp", W.SPLITPACK_SERIAL_SUBGROUP)):
+            h = W.WRS(dataclasses.replace(wrs.config, split_size=split, split_pack_mode=mode))
+            if mode == W.SPLITPACK_INLINE:
+                row[name] = timed(lambda: h.split_pack(stream, w, idx, prefix, elems, n, table,
+                                                       internals, lo)) * 1e3
+            else:
+                row["split_records"] = timed(lambda: h.split(stream, prefix, n, records,
+                                                             internals, prefix_lo=lo)) * 1e3
+                row[name] = timed(lambda: h.pack(stream, w, idx, elems, records, n, table,
+                                                 internals)) * 1e3
+        serial[split] = row
+    out["split_pack_modes_ms"] = serial
+    wrs.split_pack(stream, w, idx, prefix, elems, n, table, internals, lo)  # the inline table
     its = W.WRS(W.ITSConfig(rng=W.RNG_PHILOX4X32_10, scan_precision=W.SCAN_COMPENSATED))
     cmf = torch.empty(n, dtype=torch.float32, device=w.device)
     rec("scan", timed(lambda: its.prefix_sum(stream, w, n, cmf, internals)), 8 * n, n, "weights")

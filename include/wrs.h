@@ -91,6 +91,20 @@ typedef enum wrs_scan_precision {
                                   is exact to FP64 rounding; ITS: as COMPENSATED */
 } wrs_scan_precision;
 
+/* PSA split + pack (PSAConfig::splitPack, src/device/wrs/alias/psa/splitpack/SplitPack.hpp) */
+typedef enum wrs_split_pack_mode {
+    WRS_SPLITPACK_INLINE = 0,         /* InlineSplitPack: splits computed and packed in one kernel
+                                         (splitpack/inline/shader.comp), N / splitSize splits */
+    WRS_SPLITPACK_SERIAL = 1,         /* SerialSplitPack = ScalarSplit + ScalarPack: ceil(N /
+                                         splitSize) split records written to device memory
+                                         (split/scalar/shader.comp), then one thread per
+                                         subproblem packs from them (pack/scalar/float.comp) */
+    WRS_SPLITPACK_SERIAL_SUBGROUP = 2 /* ScalarSplit + SubgroupPack's strategy: one warp per
+                                         subproblem, items loaded 32 at a time and shuffled to the
+                                         lockstep walk (pack/subgroup/shader.comp); the table is
+                                         bit-identical to WRS_SPLITPACK_SERIAL's */
+} wrs_split_pack_mode;
+
 /* device status bits (wrs_buffers_status) */
 #define WRS_DEVICE_TIMEOUT 1u
 #define WRS_DEVICE_NONMONOTONE_SPLIT 2u
@@ -121,12 +135,23 @@ typedef struct wrs_config {
                                         cell instead of bisecting the whole CMF (indices
                                         unchanged, the CMF being exactly non-decreasing);
                                         0 = no cells, every search bisects; default 4 */
+    uint32_t split_pack_mode;        /* wrs_split_pack_mode: PSAConfig's splitPack alternative;
+                                        default WRS_SPLITPACK_INLINE */
 } wrs_config;
 
 typedef struct wrs_alias_entry {
     float p;    /* keep-probability of the bucket (alias_table.hpp layout, 8 bytes) */
     uint32_t a; /* alias index */
 } wrs_alias_entry;
+
+/* A split between PSA subproblems: i light and j heavy items before it, spill = the residual of
+ * heavy j (host::Split<float, uint32>, src/host/types/split.hpp:9-37; the std430 layout of the
+ * shaders' Split, 12 bytes). */
+typedef struct wrs_split_record {
+    uint32_t i;
+    uint32_t j;
+    float spill;
+} wrs_split_record;
 
 typedef struct wrs_handle wrs_handle;
 typedef struct wrs_buffers wrs_buffers;
@@ -169,6 +194,8 @@ wrs_status wrs_buffers_status(wrs_buffers* b, void* stream, uint32_t* device_sta
 const wrs_alias_entry* wrs_buffers_alias_table(const wrs_buffers* b);
 const float* wrs_buffers_cmf(const wrs_buffers* b);              /* ITS and Cutpoint */
 const uint32_t* wrs_buffers_guide_table(const wrs_buffers* b);   /* Cutpoint: ceil(N / entry) */
+/* serial split-pack modes: the split records of the last build (wrs_split_records_count) */
+const wrs_split_record* wrs_buffers_split_records(const wrs_buffers* b);
 const uint32_t* wrs_buffers_partition_indices(const wrs_buffers* b);
 const float* wrs_buffers_partition_prefix(const wrs_buffers* b);
 const float* wrs_buffers_partition_elements(const wrs_buffers* b);
@@ -194,6 +221,21 @@ wrs_status wrs_split_pack(const wrs_handle* h, void* stream, const float* weight
                           const uint32_t* partition_indices, const float* partition_prefix,
                           const float* partition_elements, const float* partition_prefix_lo,
                           uint32_t n, wrs_alias_entry* table, wrs_buffers* b);
+/* Serial split-pack (SerialSplitPack::run, src/device/wrs/alias/psa/splitpack/serial/
+ * SerialSplitPack.hpp:52-93): wrs_split writes the K = wrs_split_records_count(n, split_size)
+ * = ceil(n / split_size) records of ScalarSplit (split/scalar/shader.comp:72-133): record k - 1
+ * for k in [1, K) at n_k = ceil(n * k / K), record K - 1 = (lightCount, heavyCount, 0); mean and
+ * heavy count are read from b, the precision options are the handle's.  wrs_pack packs the K
+ * subproblems [record k - 1, record k) from them (ScalarPack, pack/scalar/float.comp; with
+ * WRS_SPLITPACK_SERIAL_SUBGROUP the warp-cooperative strategy of SubgroupPack, same table). */
+uint32_t wrs_split_records_count(uint32_t n, uint32_t split_size);
+wrs_status wrs_split(const wrs_handle* h, void* stream, const float* partition_prefix,
+                     const float* partition_prefix_lo, uint32_t n, wrs_split_record* records,
+                     wrs_buffers* b);
+wrs_status wrs_pack(const wrs_handle* h, void* stream, const float* weights,
+                    const uint32_t* partition_indices, const float* partition_elements,
+                    const wrs_split_record* records, uint32_t n, wrs_alias_entry* table,
+                    wrs_buffers* b);
 wrs_status wrs_alias_sample(const wrs_handle* h, void* stream, const wrs_alias_entry* table,
                             uint32_t n, uint64_t s, uint64_t seed, uint64_t offset,
                             uint32_t* samples);

@@ -38,12 +38,14 @@ inline void check(wrs_status s) {
 using WRSConfig = wrs_config;
 
 inline WRSConfig AliasTableConfig(uint32_t split_size = 2, uint32_t coop_size = 0,
-                                  bool use_partition_elements = true) {
+                                  bool use_partition_elements = true,
+                                  uint32_t split_pack_mode = WRS_SPLITPACK_INLINE) {
     WRSConfig c;
     check(wrs_config_init(&c, WRS_METHOD_ALIAS_TABLE));
     c.split_size = split_size;
     c.coop_size = coop_size;
     c.use_partition_elements = use_partition_elements ? 1u : 0u;
+    c.split_pack_mode = split_pack_mode;
     return c;
 }
 

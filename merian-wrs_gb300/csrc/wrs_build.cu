@@ -1269,6 +1269,7 @@ struct SplitArgs {
     uint32_t* status;
     uint32_t split_size;
     uint32_t full_light;
+    SplitRecord* records;  // serial split-pack: the split records (split k = records[k - 1])
 };
 
 // Slot t of CTA b (t < kSplitSlots; thread t % kSplitThreads holds slots t and t + 512) holds
@@ -1276,7 +1277,7 @@ struct SplitArgs {
 // for t < kSplitPack, k < K; split_{k+1} comes from the next slot through shared memory
 // (shader.comp:225-270).  The last kSplitLook + 1 slots only hold look-ahead splits for the
 // ownership window.
-template <bool R64, bool FF, bool BATCH>
+template <bool R64, bool FF, bool BATCH, bool RECORDS = false>
 __global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, BatchView bv) {
     __shared__ uint32_t s_i[kSplitSlots], s_j[kSplitSlots];
     __shared__ float s_spill[kSplitSlots];
@@ -1304,7 +1305,9 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, Batch
         blk -= D->split0;
         nblk = split_blocks_for(n, a.split_size);
     }
-    const uint32_t K = splits_for(n, a.split_size);
+    // RECORDS (serial split-pack): K = ceil(N / splitSize) subproblems whose splits were
+    // written by k_split_records; otherwise the inline split-pack's K = N / splitSize
+    const uint32_t K = RECORDS ? records_for(n, a.split_size) : splits_for(n, a.split_size);
     const uint32_t hc = ctrl->heavy_count;
     if (hc == 0u || hc >= n) {
         // degenerate (all items light or all heavy): every bucket keeps itself
@@ -1328,7 +1331,18 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, Batch
         sj[v] = kv[v] == 0u ? 0u : hc;
         sp[v] = 0.f;
     }
-    compute_splits<R64, FF, kSplitPerThread>(c, nsplit, on, si, sj, sp);
+    if constexpr (RECORDS) {
+#pragma unroll
+        for (int v = 0; v < kSplitPerThread; ++v) {
+            if (!on[v]) continue;
+            const SplitRecord r = a.records[kv[v] - 1u];
+            si[v] = r.i;
+            sj[v] = r.j;
+            sp[v] = r.spill;
+        }
+    } else {
+        compute_splits<R64, FF, kSplitPerThread>(c, nsplit, on, si, sj, sp);
+    }
 #pragma unroll
     for (int v = 0; v < kSplitPerThread; ++v) {
         const int slot = threadIdx.x + v * kSplitThreads;
@@ -1376,6 +1390,241 @@ cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const 
                       full_light ? 1u : 0u};
     split_dispatch<false>(st, r64, prefix_lo != nullptr, split_blocks_for(n, split_size), a,
                           BatchView{});
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------
+// serial split-pack: split records persisted between two kernels
+// ---------------------------------------------------------------------------------
+
+// split/scalar/shader.comp:72-133 (ScalarSplit): K = ceil(N / splitSize) records; record k - 1
+// (k in [1, K)) is computeSplit at n = ceil(N * k / K) (ceilMulDiv, 64-bit), record K - 1 =
+// (lightCount, heavyCount, 0).  Each split is compute_split's bisection (the same probe
+// sequence, comparisons and precision options as the inline kernel).  All heavy or all
+// light: every record is the final one (the shader's bisection would underflow).
+template <bool R64, bool FF>
+__global__ __launch_bounds__(256) void k_split_records(SplitArgs a) {
+    const uint32_t n = a.n;
+    const uint32_t K = records_for(n, a.split_size);
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;  // record t: split k = t + 1
+    if (t >= K) return;
+    const uint32_t hc = a.ctrl->heavy_count;
+    SplitRecord r{n - min(hc, n), min(hc, n), 0.0f};
+    if (t + 1u < K && hc != 0u && hc < n) {
+        const PackIn c{a.w,    a.idx, a.elems, a.prefix, a.prefix_lo, n, hc, n - hc,
+                       a.full_light ? n - hc : n - hc - 1u, a.ctrl->mean, a.ctrl->mean_lo};
+        const uint32_t nk = static_cast<uint32_t>(
+            (static_cast<uint64_t>(n) * (t + 1u) + K - 1u) / K);
+        compute_split<R64, FF>(c, nk, r.i, r.j, r.spill);
+    }
+    a.records[t] = r;
+}
+
+cudaError_t launch_split_records(cudaStream_t st, bool r64, bool full_light, const float* prefix,
+                                 const float* prefix_lo, const BuildCtrl* ctrl, uint32_t n,
+                                 uint32_t split_size, SplitRecord* records) {
+    const SplitArgs a{nullptr, n,         ctrl,    nullptr, nullptr,    nullptr,
+                      prefix,  prefix_lo, nullptr, split_size, full_light ? 1u : 0u, records};
+    const uint32_t K = records_for(n, split_size);
+    const uint32_t blocks = (K + 255u) / 256u;
+    if (prefix_lo)
+        k_split_records<true, true><<<blocks, 256, 0, st>>>(a);
+    else if (r64)
+        k_split_records<true, false><<<blocks, 256, 0, st>>>(a);
+    else
+        k_split_records<false, false><<<blocks, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// pack/scalar/float.comp (ScalarPack): one thread per subproblem [split_k, split_{k+1}) with the
+// splits read from the records; the same pack loop, ownership window and status bit as the
+// inline kernel (whose slot machinery k_split_pack<..., RECORDS> reuses).
+cudaError_t launch_pack_records(cudaStream_t st, const float* w, const uint32_t* idx,
+                                const float* elems, const BuildCtrl* ctrl, uint32_t* status,
+                                uint32_t n, uint32_t split_size, const SplitRecord* records,
+                                uint2* table) {
+    const SplitArgs a{w,       n,       ctrl,   table,      idx, elems,
+                      nullptr, nullptr, status, split_size, 0u,  const_cast<SplitRecord*>(records)};
+    const uint32_t blocks = (records_for(n, split_size) + kSplitPack - 1) / kSplitPack;
+    k_split_pack<false, false, false, true><<<blocks, kSplitThreads, 0, st>>>(a, BatchView{});
+    return cudaGetLastError();
+}
+
+// SubgroupPack's strategy (pack/subgroup/shader.comp): one warp per subproblem.  The lanes load
+// the subproblem's heavy and light items 32 at a time (coalesced; without partition elements
+// the 32 weight gathers are in flight together), the walk runs in lockstep with every item
+// fetched from its lane by a shuffle, and each lane keeps one table entry of every 32 steps,
+// written together.  Decisions and arithmetic are the scalar pack's operation for operation,
+// so the table is bit-identical to launch_pack_records'.  (The reference's subgroup shader
+// updates the residual as w + (weight - mean) and keeps a zero spill; here one arithmetic
+// serves both strategies.)  Ownership: a later subproblem within kWarpLook overrides, as in
+// the scalar kernel; a step back beyond that raises kStatusNonMonotone.
+constexpr uint32_t kWarpLook = 31;
+
+__device__ __forceinline__ void split_at(const SplitRecord* __restrict__ rec, uint32_t K,
+                                         uint32_t k, uint32_t lc, uint32_t hc, uint32_t& i,
+                                         uint32_t& j, float& spill) {
+    if (k == 0u) {
+        i = j = 0u;
+        spill = 0.0f;
+    } else if (k >= K) {
+        i = lc;
+        j = hc;
+        spill = 0.0f;
+    } else {
+        const SplitRecord r = rec[k - 1u];
+        i = r.i;
+        j = r.j;
+        spill = r.spill;
+    }
+}
+
+// Is the entry at light rank / heavy position `pos` packed by one of the later subproblems
+// k + 1 .. k + count?  Lane d holds split_{k+1+d} in (li, lj); subproblem k + d covers
+// [split_{k+d}, max(split_{k+d+1}, split_{k+d})).  Called by all lanes of the warp.
+__device__ __forceinline__ bool covered_later_warp(uint32_t li, uint32_t lj, uint32_t count,
+                                                   uint32_t pos, bool light) {
+    bool covered = false;
+    for (uint32_t d = 1; d <= count; ++d) {
+        const uint32_t ai = __shfl_sync(0xffffffffu, li, d - 1u);
+        const uint32_t aj = __shfl_sync(0xffffffffu, lj, d - 1u);
+        const uint32_t bi = max(__shfl_sync(0xffffffffu, li, d), ai);
+        const uint32_t bj = max(__shfl_sync(0xffffffffu, lj, d), aj);
+        covered = covered || (light ? (ai <= pos && pos < bi) : (aj <= pos && pos < bj));
+    }
+    return covered;
+}
+
+__global__ __launch_bounds__(256) void k_pack_records_warp(SplitArgs a) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // subproblem
+    const uint32_t n = a.n;
+    const uint32_t K = records_for(n, a.split_size);
+    if (k >= K) return;  // whole warps
+    const uint32_t hc = a.ctrl->heavy_count;
+    uint2* table = a.table;
+    if (hc == 0u || hc >= n) {
+        const uint32_t per = (n + K - 1u) / K;
+        for (uint32_t e = k * per + lane; e < min(n, (k + 1u) * per); e += 32u)
+            table[e] = make_uint2(__float_as_uint(1.0f), e);
+        return;
+    }
+    const uint32_t lc = n - hc, last = n - 1u;
+    const float mean = a.ctrl->mean;
+    const SplitRecord* rec = a.records;
+    uint32_t i0, j0, i1, j1;
+    float spill, dummy;
+    split_at(rec, K, k, lc, hc, i0, j0, spill);
+    split_at(rec, K, k + 1u, lc, hc, i1, j1, dummy);
+    i1 = max(i1, i0);
+    j1 = max(j1, j0);
+    // later splits: lane d holds split_{k + 1 + d}; subproblem k + d (d >= 1) covers
+    // [split_{k+d}, max(split_{k+d+1}, split_{k+d}))
+    const uint32_t count = min(kWarpLook, K - 1u - k);
+    uint32_t li, lj;
+    split_at(rec, K, k + 1u + lane, lc, hc, li, lj, dummy);
+    const bool clean = __all_sync(0xffffffffu, lane >= count || (li >= i1 && lj >= j1));
+    if (lane == 0 && k + kWarpLook + 1u < K) {
+        uint32_t bi, bj;
+        split_at(rec, K, k + kWarpLook + 1u, lc, hc, bi, bj, dummy);
+        if (bi < i1 || bj < j1) atomicOr(a.status, kStatusNonMonotone);
+    }
+    const uint32_t* idx = a.idx;
+    const float* elems = a.elems;
+    const float* w = a.w;
+    auto elem_at = [&](uint32_t pos, uint32_t widx) -> float {
+        return elems ? __ldg(elems + pos) : (widx < n ? __ldg(w + widx) : 0.0f);
+    };
+    // chunks: heavy positions hb + lane, light ranks lb + lane
+    uint32_t hb = j0, lb = i0;
+    uint32_t hidx = 0, lidx = 0;
+    float hw = 0.0f, lw = 0.0f;
+    auto load_heavy = [&]() {
+        const uint32_t pos = hb + lane;
+        hidx = pos < n ? __ldg(idx + pos) : 0u;
+        hw = pos < n ? elem_at(pos, hidx) : 0.0f;
+    };
+    auto load_light = [&]() {
+        const uint32_t r = lb + lane;
+        lidx = r < n ? __ldg(idx + last - r) : 0u;
+        lw = r < n ? elem_at(last - r, lidx) : 0.0f;
+    };
+    load_heavy();
+    load_light();
+    uint32_t i = i0, j = j0;
+    float wv = spill;
+    if (wv == 0.0f) wv = __shfl_sync(0xffffffffu, hw, 0);  // elem(j0): lane 0 of the heavy chunk
+    // pending entries: lane e holds step e of the current group of 32
+    uint32_t e_out = 0u, e_a = 0u, e_pos = 0u;
+    float e_p = 0.0f;
+    bool e_light = false;
+    uint32_t pend = 0;
+    while (i < i1 || j < j1) {
+        bool heavy_step;
+        if (j == j1 || j == hc)
+            heavy_step = false;
+        else if (i == i1 || i == lc)
+            heavy_step = true;
+        else
+            heavy_step = wv <= mean;
+        if (j + 1u - hb >= 32u) {  // keep j and j + 1 inside the heavy chunk
+            hb = j;
+            load_heavy();
+        }
+        const uint32_t h = __shfl_sync(0xffffffffu, hidx, j - hb);
+        uint32_t widx;
+        float weight;
+        if (heavy_step) {
+            widx = __shfl_sync(0xffffffffu, hidx, j + 1u - hb);
+            weight = __shfl_sync(0xffffffffu, hw, j + 1u - hb);
+        } else {
+            if (i - lb >= 32u) {
+                lb = i;
+                load_light();
+            }
+            widx = __shfl_sync(0xffffffffu, lidx, i - lb);
+            weight = __shfl_sync(0xffffffffu, lw, i - lb);
+        }
+        if (lane == pend) {
+            if (heavy_step) {
+                e_p = __fdiv_rn(wv, mean);
+                e_a = widx;
+                e_out = h;
+                e_pos = j;
+                e_light = false;
+            } else {
+                e_p = __fdiv_rn(weight, mean);
+                e_a = h;
+                e_out = widx;
+                e_pos = i;
+                e_light = true;
+            }
+        }
+        if (heavy_step)
+            ++j;
+        else
+            ++i;
+        wv = __fsub_rn(__fadd_rn(wv, weight), mean);
+        if (++pend == 32u) {
+            // whole warp: the shuffles of the ownership test need every lane
+            const bool owned = clean || !covered_later_warp(li, lj, count, e_pos, e_light);
+            if (owned && e_out < n) table[e_out] = make_uint2(__float_as_uint(e_p), e_a);
+            pend = 0;
+        }
+    }
+    // the last, partial group
+    const bool owned = clean || !covered_later_warp(li, lj, count, e_pos, e_light);
+    if (lane < pend && owned && e_out < n) table[e_out] = make_uint2(__float_as_uint(e_p), e_a);
+}
+
+cudaError_t launch_pack_records_warp(cudaStream_t st, const float* w, const uint32_t* idx,
+                                     const float* elems, const BuildCtrl* ctrl, uint32_t* status,
+                                     uint32_t n, uint32_t split_size, const SplitRecord* records,
+                                     uint2* table) {
+    const SplitArgs a{w,       n,       ctrl,   table,      idx, elems,
+                      nullptr, nullptr, status, split_size, 0u,  const_cast<SplitRecord*>(records)};
+    const uint64_t threads = static_cast<uint64_t>(records_for(n, split_size)) * 32u;
+    k_pack_records_warp<<<static_cast<unsigned>((threads + 255u) / 256u), 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -44,6 +44,7 @@ struct wrs_buffers {
     float* elems = nullptr;
     float* prefix_lo = nullptr;
     uint2* table = nullptr;
+    SplitRecord* records = nullptr;  // serial split-pack
     float* cmf = nullptr;
     uint32_t* guide = nullptr;
     ItsCell* cells = nullptr;
@@ -75,8 +76,8 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct Layout {
-    size_t ctrl, partials, part_states, scan_states, idx, prefix, elems, prefix_lo, table, cmf,
-        guide, cells, coarse, total;
+    size_t ctrl, partials, part_states, scan_states, idx, prefix, elems, prefix_lo, table, records,
+        cmf, guide, cells, coarse, total;
 };
 
 Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
@@ -103,6 +104,9 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
                           ? take(sizeof(float) * static_cast<size_t>(max_n))
                           : 0;
         L.table = take(sizeof(uint2) * static_cast<size_t>(max_n));
+        L.records = cfg.split_pack_mode != WRS_SPLITPACK_INLINE
+                        ? take(sizeof(SplitRecord) * records_for(max_n, cfg.split_size))
+                        : 0;
     } else {
         L.cmf = take(sizeof(float) * static_cast<size_t>(max_n));
         // Cutpoint: its guiding table; ITS: the cell blocks that steer sampling on the
@@ -137,6 +141,8 @@ wrs_status check_config(const wrs_config* c) {
                     "the Cutpoint method has no cooperative-size setting (coop_size must be 0)");
     if (c->method == WRS_METHOD_ALIAS_TABLE && c->split_size == 0)
         return fail(WRS_ERR_INVALID_ARG, "split_size must be >= 1");
+    if (c->split_pack_mode > WRS_SPLITPACK_SERIAL_SUBGROUP)
+        return fail(WRS_ERR_INVALID_ARG, "unknown split_pack_mode");
     if (c->rng > WRS_RNG_PHILOX4X32_10) return fail(WRS_ERR_INVALID_ARG, "unknown rng");
     if (c->scan_precision > WRS_SCAN_FLOAT_FLOAT)
         return fail(WRS_ERR_INVALID_ARG, "unknown scan precision");
@@ -243,6 +249,7 @@ wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers**
                            ? reinterpret_cast<float*>(p + L.prefix_lo)
                            : nullptr;
         b->table = reinterpret_cast<uint2*>(p + L.table);
+        b->records = L.records ? reinterpret_cast<SplitRecord*>(p + L.records) : nullptr;
     } else {
         b->cmf = reinterpret_cast<float*>(p + L.cmf);
         b->guide = L.guide ? reinterpret_cast<uint32_t*>(p + L.guide) : nullptr;
@@ -358,6 +365,50 @@ wrs_status wrs_split_pack(const wrs_handle* h, void* stream, const float* weight
     return WRS_OK;
 }
 
+uint32_t wrs_split_records_count(uint32_t n, uint32_t split_size) {
+    return split_size ? records_for(n, split_size) : 0u;
+}
+
+wrs_status wrs_split(const wrs_handle* h, void* stream, const float* partition_prefix,
+                     const float* partition_prefix_lo, uint32_t n, wrs_split_record* records,
+                     wrs_buffers* b) {
+    if (!h || !partition_prefix || !records) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    if ((partition_prefix_lo != nullptr) != float_float(h))
+        return fail(WRS_ERR_INVALID_ARG,
+                    "partition_prefix_lo is required exactly with WRS_SCAN_FLOAT_FLOAT");
+    wrs_status s = check_n(b, n);
+    if (s != WRS_OK) return s;
+    if (h->cfg.split_size == 0) return fail(WRS_ERR_INVALID_ARG, "split_size must be >= 1");
+    WRS_CUDA(launch_split_records(as_stream(stream), h->cfg.split_residual_f64 != 0,
+                                  h->cfg.split_full_light != 0, partition_prefix,
+                                  partition_prefix_lo, b->ctrl, n, h->cfg.split_size,
+                                  reinterpret_cast<SplitRecord*>(records)),
+             "split records");
+    return WRS_OK;
+}
+
+wrs_status wrs_pack(const wrs_handle* h, void* stream, const float* weights,
+                    const uint32_t* partition_indices, const float* partition_elements,
+                    const wrs_split_record* records, uint32_t n, wrs_alias_entry* table,
+                    wrs_buffers* b) {
+    if (!h || !weights || !partition_indices || !records || !table)
+        return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    wrs_status s = check_n(b, n);
+    if (s != WRS_OK) return s;
+    if (h->cfg.split_size == 0) return fail(WRS_ERR_INVALID_ARG, "split_size must be >= 1");
+    const SplitRecord* r = reinterpret_cast<const SplitRecord*>(records);
+    uint2* t = reinterpret_cast<uint2*>(table);
+    WRS_CUDA(h->cfg.split_pack_mode == WRS_SPLITPACK_SERIAL_SUBGROUP
+                 ? launch_pack_records_warp(as_stream(stream), weights, partition_indices,
+                                            partition_elements, b->ctrl, &b->ctrl->status, n,
+                                            h->cfg.split_size, r, t)
+                 : launch_pack_records(as_stream(stream), weights, partition_indices,
+                                       partition_elements, b->ctrl, &b->ctrl->status, n,
+                                       h->cfg.split_size, r, t),
+             "pack");
+    return WRS_OK;
+}
+
 wrs_status wrs_alias_sample(const wrs_handle* h, void* stream, const wrs_alias_entry* table,
                             uint32_t n, uint64_t s, uint64_t seed, uint64_t offset,
                             uint32_t* samples) {
@@ -443,6 +494,24 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
     WRS_CUDA(launch_prefix_partition(st, comp, weights, n, b->ctrl, b->part_states, b->cap_tiles,
                                      b->idx, b->prefix, elems, lo),
              "prefix partition");
+    if (h->cfg.split_pack_mode != WRS_SPLITPACK_INLINE) {
+        // SerialSplitPack: the split records, then the pack from them
+        if (!b->records || b->cfg.split_size != h->cfg.split_size)
+            return fail(WRS_ERR_INVALID_ARG,
+                        "buffers were created without split records for this split size");
+        WRS_CUDA(launch_split_records(st, h->cfg.split_residual_f64 != 0,
+                                      h->cfg.split_full_light != 0, b->prefix, lo, b->ctrl, n,
+                                      h->cfg.split_size, b->records),
+                 "split records");
+        WRS_CUDA(h->cfg.split_pack_mode == WRS_SPLITPACK_SERIAL_SUBGROUP
+                     ? launch_pack_records_warp(st, weights, b->idx, elems, b->ctrl,
+                                                &b->ctrl->status, n, h->cfg.split_size,
+                                                b->records, b->table)
+                     : launch_pack_records(st, weights, b->idx, elems, b->ctrl, &b->ctrl->status,
+                                           n, h->cfg.split_size, b->records, b->table),
+                 "pack");
+        return WRS_OK;
+    }
     WRS_CUDA(launch_split_pack(st, h->cfg.split_residual_f64 != 0, h->cfg.split_full_light != 0,
                                weights, b->idx, elems, b->prefix, lo, b->ctrl, &b->ctrl->status, n,
                                h->cfg.split_size, b->table),
@@ -535,6 +604,9 @@ const wrs_alias_entry* wrs_buffers_alias_table(const wrs_buffers* b) {
 }
 const float* wrs_buffers_cmf(const wrs_buffers* b) { return b ? b->cmf : nullptr; }
 const uint32_t* wrs_buffers_guide_table(const wrs_buffers* b) { return b ? b->guide : nullptr; }
+const wrs_split_record* wrs_buffers_split_records(const wrs_buffers* b) {
+    return b ? reinterpret_cast<const wrs_split_record*>(b->records) : nullptr;
+}
 const uint32_t* wrs_buffers_partition_indices(const wrs_buffers* b) { return b ? b->idx : nullptr; }
 const float* wrs_buffers_partition_prefix(const wrs_buffers* b) { return b ? b->prefix : nullptr; }
 const float* wrs_buffers_partition_elements(const wrs_buffers* b) { return b ? b->elems : nullptr; }
@@ -621,6 +693,8 @@ wrs_status check_batch_handle(const wrs_handle* h, const wrs_batch* b) {
     if (!h || !b) return fail(WRS_ERR_INVALID_ARG, "handle or batch is NULL");
     if (h->cfg.method != WRS_METHOD_ALIAS_TABLE)
         return fail(WRS_ERR_NOT_IMPLEMENTED, "batches exist for the alias method only");
+    if (h->cfg.split_pack_mode != WRS_SPLITPACK_INLINE)
+        return fail(WRS_ERR_NOT_IMPLEMENTED, "batches use the inline split-pack");
     if (h->cfg.split_size != b->cfg.split_size ||
         h->cfg.use_partition_elements != b->cfg.use_partition_elements ||
         h->cfg.scan_precision != b->cfg.scan_precision)
@@ -648,6 +722,8 @@ wrs_status wrs_batch_create(const wrs_handle* h, uint32_t max_dists, uint64_t ma
     *out = nullptr;
     if (h->cfg.method != WRS_METHOD_ALIAS_TABLE)
         return fail(WRS_ERR_NOT_IMPLEMENTED, "batches exist for the alias method only");
+    if (h->cfg.split_pack_mode != WRS_SPLITPACK_INLINE)
+        return fail(WRS_ERR_NOT_IMPLEMENTED, "batches use the inline split-pack");
     if (max_dists == 0 || max_dists > (1u << 24))
         return fail(WRS_ERR_INVALID_ARG, "max_dists out of range");
     BatchCaps c;

@@ -123,6 +123,24 @@ cudaError_t launch_prefix_partition(cudaStream_t st, bool comp, const float* w, 
 cudaError_t launch_scan(cudaStream_t st, bool comp, const float* in, uint32_t n, float* out,
                         BuildCtrl* ctrl, ScanState* states, uint32_t cap_tiles, double* partials,
                         uint32_t spin_limit = kSpinLimit);
+// ScalarSplit's record (split/scalar/shader.comp:12-16, std430: 12 bytes)
+struct SplitRecord {
+    uint32_t i, j;
+    float spill;
+};
+static_assert(sizeof(SplitRecord) == 12, "split record layout");
+// serial split-pack: records_for(n, s) = ceil(n / s) records (the last is (lc, hc, 0))
+cudaError_t launch_split_records(cudaStream_t st, bool r64, bool full_light, const float* prefix,
+                                 const float* prefix_lo, const BuildCtrl* ctrl, uint32_t n,
+                                 uint32_t split_size, SplitRecord* records);
+cudaError_t launch_pack_records(cudaStream_t st, const float* w, const uint32_t* idx,
+                                const float* elems, const BuildCtrl* ctrl, uint32_t* status,
+                                uint32_t n, uint32_t split_size, const SplitRecord* records,
+                                uint2* table);
+cudaError_t launch_pack_records_warp(cudaStream_t st, const float* w, const uint32_t* idx,
+                                     const float* elems, const BuildCtrl* ctrl, uint32_t* status,
+                                     uint32_t n, uint32_t split_size, const SplitRecord* records,
+                                     uint2* table);
 cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const float* w,
                               const uint32_t* idx, const float* elems, const float* prefix,
                               const float* prefix_lo, const BuildCtrl* ctrl, uint32_t* status,
@@ -189,6 +207,10 @@ __host__ __device__ inline uint32_t splits_for(uint32_t n, uint32_t split_size) 
 }
 __host__ __device__ inline uint32_t split_blocks_for(uint32_t n, uint32_t split_size) {
     return (splits_for(n, split_size) + kSplitPack - 1) / kSplitPack;
+}
+__host__ __device__ inline uint32_t records_for(uint32_t n, uint32_t split_size) {
+    const uint32_t k = static_cast<uint32_t>((static_cast<uint64_t>(n) + split_size - 1) / split_size);
+    return k ? k : 1u;
 }
 __host__ __device__ inline uint64_t alias_blocks_for(uint64_t s) { return (s + kAliasPerBlock - 1) / kAliasPerBlock; }
 // guiding-table entries of the Cutpoint method (cutpoint/Cutpoint.hpp:72-73)

@@ -29,6 +29,9 @@ RNG_PHILOX4X32_10 = 1
 SCAN_FP32 = 0
 SCAN_COMPENSATED = 1
 SCAN_FLOAT_FLOAT = 2
+SPLITPACK_INLINE = 0
+SPLITPACK_SERIAL = 1
+SPLITPACK_SERIAL_SUBGROUP = 2
 
 DEVICE_TIMEOUT = 1
 DEVICE_NONMONOTONE_SPLIT = 2
@@ -43,7 +46,13 @@ class WRSError(RuntimeError):
 class _Config(C.Structure):
     _fields_ = [(n, C.c_uint32) for n in (
         "method", "split_size", "use_partition_elements", "coop_size", "its_parray", "rng",
-        "scan_precision", "split_residual_f64", "split_full_light", "guiding_entry_size")]
+        "scan_precision", "split_residual_f64", "split_full_light", "guiding_entry_size",
+        "split_pack_mode")]
+
+
+class SplitRecord(C.Structure):
+    """wrs_split_record: {i, j, spill} (the shaders' Split, 12 bytes)."""
+    _fields_ = [("i", C.c_uint32), ("j", C.c_uint32), ("spill", C.c_float)]
 
 
 class ServerConfig(C.Structure):
@@ -157,6 +166,10 @@ def lib() -> C.CDLL:
             "wrs_server_get_stats": (i32, [vp, C.POINTER(ServerStats)]),
             "wrs_server_run_trace": (i32, [vp, C.POINTER(Request), C.POINTER(C.c_double), u32,
                                            C.POINTER(Completion)]),
+            "wrs_split_records_count": (u32, [u32, u32]),
+            "wrs_split": (i32, [vp, vp, vp, vp, u32, vp, vp]),
+            "wrs_pack": (i32, [vp, vp, vp, vp, vp, vp, u32, vp, vp]),
+            "wrs_buffers_split_records": (vp, [vp]),
             "wrs_set_l2_fetch_granularity": (i32, [u32]),
             "wrs_get_l2_fetch_granularity": (i32, [C.POINTER(u32)]),
             "wrs_autotune_alias": (i32, [cfgp, vp, vp, u32, u64, vp, C.POINTER(TuneSpace),
@@ -208,12 +221,13 @@ class WRSConfig:
     split_residual_f64: bool = False
     split_full_light: bool = False
     guiding_entry_size: int = 32
+    split_pack_mode: int = SPLITPACK_INLINE
 
     def c(self) -> _Config:
         return _Config(self.method, self.split_size, int(self.use_partition_elements),
                        self.coop_size, int(self.its_parray), self.rng, self.scan_precision,
                        int(self.split_residual_f64), int(self.split_full_light),
-                       self.guiding_entry_size)
+                       self.guiding_entry_size, self.split_pack_mode)
 
     def split_flags(self) -> int:
         """The oracle's split flags for this configuration."""
@@ -294,6 +308,7 @@ class Internals:
             "alias_table": L.wrs_buffers_alias_table(self.ptr),
             "cmf": L.wrs_buffers_cmf(self.ptr),
             "guide_table": L.wrs_buffers_guide_table(self.ptr),
+            "split_records": L.wrs_buffers_split_records(self.ptr),
             "partition_indices": L.wrs_buffers_partition_indices(self.ptr),
             "partition_prefix": L.wrs_buffers_partition_prefix(self.ptr),
             "partition_elements": L.wrs_buffers_partition_elements(self.ptr),
@@ -359,6 +374,17 @@ class WRS:
         check(lib().wrs_split_pack(self.handle.ptr, _stream_ptr(stream), _dev_ptr(weights),
                                    _dev_ptr(idx), _dev_ptr(prefix), _dev_ptr(elems),
                                    _dev_ptr(prefix_lo), N, _dev_ptr(table), internals.ptr))
+
+    def split(self, stream, prefix, N, records, internals, prefix_lo=None) -> None:
+        """wrs_split: the serial split-pack's ceil(N / split_size) split records."""
+        check(lib().wrs_split(self.handle.ptr, _stream_ptr(stream), _dev_ptr(prefix),
+                              _dev_ptr(prefix_lo), N, _dev_ptr(records), internals.ptr))
+
+    def pack(self, stream, weights, idx, elems, records, N, table, internals) -> None:
+        """wrs_pack: the alias table from split records (scalar or warp strategy)."""
+        check(lib().wrs_pack(self.handle.ptr, _stream_ptr(stream), _dev_ptr(weights),
+                             _dev_ptr(idx), _dev_ptr(elems), _dev_ptr(records), N,
+                             _dev_ptr(table), internals.ptr))
 
     def alias_sample(self, stream, table, N, S, seed, offset, out) -> None:
         check(lib().wrs_alias_sample(self.handle.ptr, _stream_ptr(stream), _dev_ptr(table), N, S,

@@ -16,6 +16,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ENTRY_DTYPE = np.dtype([("p", "<f4"), ("a", "<u4")])
+SPLIT_DTYPE = np.dtype([("i", "<u4"), ("j", "<u4"), ("spill", "<f4")])  # wrs_split_record
 
 RNG_REFERENCE = 0
 RNG_PHILOX4X32_10 = 1
@@ -71,6 +72,8 @@ class Oracle:
                 "wrso_split_pack": (None, [vp, vp, vp, vp, vp, u32, f32, f64, u32, u32, i32, vp,
                                            vp]),
                 "wrso_psa_build": (None, [vp, u32, u32, i32, i32, vp, vp, vp]),
+                "wrso_scalar_split": (None, [vp, vp, u32, u32, f32, f64, u32, i32, vp]),
+                "wrso_scalar_pack": (None, [vp, vp, vp, u32, f32, u32, u32, vp, vp]),
                 "wrso_alias_sample": (None, [vp, u32, u64, u64, u64, u32, u32, i32, vp]),
                 "wrso_its_sample": (None, [vp, u32, u64, u64, u64, u32, u32, i32, i32, vp]),
                 "wrso_cutpoint_guide": (None, [vp, u32, u32, vp]),
@@ -178,6 +181,31 @@ class Oracle:
         if return_splits:
             sp = splits.reshape(K + 1, 3)
             return table, (sp[:, 0].copy(), sp[:, 1].copy(), sp[:, 2].view(np.float32).copy())
+        return table
+
+    def scalar_split(self, prefix, heavy_count, mean, split_size, flags=0, prefix_lo=None,
+                     mean64=0.0):
+        """ScalarSplit's ceil(N / split_size) records as a SPLIT_DTYPE array."""
+        prefix = np.ascontiguousarray(prefix, np.float32)
+        lo = None if prefix_lo is None else np.ascontiguousarray(prefix_lo, np.float32)
+        N = prefix.size
+        K = max((N + split_size - 1) // split_size, 1)
+        rec = np.zeros(K, SPLIT_DTYPE)
+        self.lib.wrso_scalar_split(_ptr(prefix), _ptr(lo), N, heavy_count, np.float32(mean),
+                                   float(mean64), split_size, flags, _ptr(rec))
+        return rec
+
+    def scalar_pack(self, w, idx, heavy_count, mean, split_size, records, elems=None):
+        """ScalarPack from split records (SPLIT_DTYPE)."""
+        w = np.ascontiguousarray(w, np.float32)
+        idx = np.ascontiguousarray(idx, np.uint32)
+        rec = np.ascontiguousarray(records, SPLIT_DTYPE)
+        table = np.zeros(w.size, ENTRY_DTYPE)
+        self.lib.wrso_scalar_pack(_ptr(w), _ptr(idx),
+                                  _ptr(np.ascontiguousarray(elems, np.float32))
+                                  if elems is not None else None,
+                                  heavy_count, np.float32(mean), w.size, split_size, _ptr(rec),
+                                  _ptr(table))
         return table
 
     def psa_build(self, w, split_size=2, nthreads=1, flags=0):

@@ -434,6 +434,68 @@ void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, co
     }
 }
 
+/* split/scalar/shader.comp:72-133 (ScalarSplit, the split half of SerialSplitPack):
+ * K = ceil(N / splitSize) records of {i, j, spill}; record k - 1 for k in [1, K) is computeSplit
+ * at n = ceilMulDiv(N, k, K) = ceil(N * k / K) in 64 bits (shader.comp:63-64), record K - 1 =
+ * (lightCount, heavyCount, 0) (shader.comp:125-129).  Each split is wrso_split (the same
+ * bisection, light cap and precision flags as the inline shader's computeSplit, which this
+ * shader's computeSplit equals).  Guard beyond the shader: heavyCount == 0 or N makes every
+ * record the final one. */
+void wrso_scalar_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_t hc,
+                       float mean, double mean64, uint32_t split_size, int flags,
+                       uint32_t* records) {
+    uint32_t K = (uint32_t)(((uint64_t)N + split_size - 1) / split_size);
+    if (K == 0) K = 1;
+    const uint32_t h = hc < N ? hc : N;
+    for (uint32_t t = 0; t < K; ++t) {
+        uint32_t ri = N - h, rj = h;
+        float rs = 0.0f;
+        if (t + 1 < K && hc != 0 && hc < N) {
+            const uint32_t nk = (uint32_t)(((uint64_t)N * (t + 1) + K - 1) / K);
+            wrso_split(prefix, prefix_lo, N, hc, mean, mean64, nk, flags, &ri, &rj, &rs);
+        }
+        records[3 * t + 0] = ri;
+        records[3 * t + 1] = rj;
+        memcpy(&records[3 * t + 2], &rs, 4);
+    }
+}
+
+/* pack/scalar/float.comp:154-180 (ScalarPack, the pack half of SerialSplitPack): subproblem k in
+ * [0, K) packs [split_k, split_{k+1}) with split_0 = (0, 0, 0) and split_k = record k - 1, by
+ * the same loop as the inline shader (wrso_pack, float.comp:56-152 equals
+ * splitpack/inline/shader.comp:130-223), subproblems in increasing k.  Where FP32 rounding
+ * makes a split step back the shader's invocations write the same entries in no defined order;
+ * here i1 = max(split_{k+1}.i, i0), j1 = max(split_{k+1}.j, j0) and the later k's write stands,
+ * as for the inline split-pack.  Guard: heavyCount == 0 or N gives table[i] = (1, i). */
+void wrso_scalar_pack(const float* w, const uint32_t* idx, const float* elems, uint32_t hc,
+                      float mean, uint32_t N, uint32_t split_size, const uint32_t* records,
+                      wrso_entry* table) {
+    if (N == 0) return;
+    if (hc == 0 || hc >= N) {
+        for (uint32_t i = 0; i < N; ++i) {
+            table[i].p = 1.0f;
+            table[i].a = i;
+        }
+        return;
+    }
+    uint32_t K = (uint32_t)(((uint64_t)N + split_size - 1) / split_size);
+    if (K == 0) K = 1;
+    wrso_pack_ctx c = {w, idx, elems, N, hc, N - hc, mean, table};
+    uint32_t pi = 0, pj = 0;
+    float pspill = 0.0f;
+    for (uint32_t k = 0; k < K; ++k) {
+        const uint32_t ni = records[3 * k + 0], nj = records[3 * k + 1];
+        float nspill;
+        memcpy(&nspill, &records[3 * k + 2], 4);
+        const uint32_t i1 = ni > pi ? ni : pi;
+        const uint32_t j1 = nj > pj ? nj : pj;
+        wrso_pack(&c, pi, i1, pj, j1, pspill);
+        pi = ni;
+        pj = nj;
+        pspill = nspill;
+    }
+}
+
 /* ---- threaded PSA build (timed CPU port) ---------------------------------- */
 
 typedef struct {

@@ -57,6 +57,14 @@ void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, co
                      const float* prefix_lo, uint32_t heavy_count, float mean, double mean64,
                      uint32_t N, uint32_t split_size, int flags, wrso_entry* table,
                      uint32_t* splits /* 3*(K+1) or NULL */);
+/* Serial split-pack: ScalarSplit's ceil(N / split_size) records {i, j, spill} (3 words each)
+ * and ScalarPack from them. */
+void wrso_scalar_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_t heavy_count,
+                       float mean, double mean64, uint32_t split_size, int flags,
+                       uint32_t* records);
+void wrso_scalar_pack(const float* w, const uint32_t* idx, const float* elems, uint32_t heavy_count,
+                      float mean, uint32_t N, uint32_t split_size, const uint32_t* records,
+                      wrso_entry* table);
 /* Full PSA build on the CPU (mean -> partition -> prefix -> split+pack) with nthreads
  * worker threads.  Used as the timed CPU port of the reference path. */
 void wrso_psa_build(const float* w, uint32_t N, uint32_t split_size, int flags, int nthreads,

@@ -54,6 +54,7 @@ def test_config_defaults_and_validation(pkg):
         w.WRSConfig(scan_precision=3),
         w.CutpointConfig(guiding_entry_size=0),
         w.CutpointConfig(coop_size=64),  # the Cutpoint method has no cooperative size
+        w.AliasTableConfig(split_pack_mode=3),  # unknown split-pack alternative
     ]
     for c in bad:
         with pytest.raises(w.WRSError) as e:
@@ -198,3 +199,11 @@ def test_autotune_argument_checks_on_host(pkg):
                                 C.byref(res), None, 0) == 1      # split size 0
     assert L.wrs_autotune_batch(C.byref(alias), None, None, 0, None, C.byref(res), None,
                                 0) == 1                          # no distributions
+
+
+def test_split_records_count(pkg):
+    L = pkg.wrs.lib()
+    assert L.wrs_split_records_count(1000, 7) == 143   # ceil(1000 / 7)
+    assert L.wrs_split_records_count(1024, 32) == 32
+    assert L.wrs_split_records_count(5, 32) == 1
+    assert L.wrs_split_records_count(5, 0) == 0

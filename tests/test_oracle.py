@@ -288,3 +288,51 @@ def test_cutpoint_reference_stream(oracle):
         k = min(int(np.float32(u1) * np.float32(G)), G - 1)
         lo, hi = int(guide[k]), int(guide[k + 1]) if k + 1 < G else N - 1
         assert lo <= s[i] <= hi
+
+
+# ------------------------------------------------------------ serial split-pack ---
+
+@pytest.mark.parametrize("N,s", [(1024, 2), (1000, 7), (65536, 32), (65537, 5)])
+def test_live_serial_split_records_pass_reference_checkers(oracle, reference, N, s):
+    """ScalarSplit's records sit at n_k = ceil(N k / K), the positions the reference's
+    assert_is_split checks, and ScalarPack's table from them passes assert_is_alias_table."""
+    w = reference.generate_weights(1, N)
+    mean = oracle.mean(w)
+    idx, _, hc = oracle.partition(w, mean)
+    ridx, rhc = reference.stable_partition_indices(w, mean)
+    hp = reference.prefix_sum(w[ridx[:rhc]])
+    lp = reference.prefix_sum(w[ridx[rhc:]])
+    prefix = np.concatenate([hp, lp[::-1]])
+    rec = oracle.scalar_split(prefix, hc, mean, s)
+    assert rec.size == -(-N // s)
+    assert (int(rec[-1]["i"]), int(rec[-1]["j"]), float(rec[-1]["spill"])) == (N - hc, hc, 0.0)
+    dsj = rec["j"].copy()
+    dsj[-1] = hc - 1  # the checker's last split (it checks records 0 .. K - 2)
+    assert reference.assert_is_split(rec["i"].copy(), dsj, rec["spill"].copy(), hp, lp, mean,
+                                     1e-2) == (0, 0)
+    table = oracle.scalar_pack(w, idx, hc, mean, s, rec)
+    assert reference.assert_is_alias_table(w, table, oracle.total_mass(w), 1e-2) == (0, 0)
+
+
+@pytest.mark.parametrize("gen", [weights_uniform, weights_zipf, weights_lognormal])
+@pytest.mark.parametrize("s", [2, 8, 64])
+def test_serial_split_pack_equals_inline_when_n_divides(oracle, gen, s):
+    """With N a multiple of the split size both split-packs cut at k * s: the records equal
+    the inline splits and ScalarPack's table equals the inline table bit for bit; otherwise
+    the tables still encode w / mean."""
+    from oracle.oracle import SPLIT_FULL_LIGHT
+    for N in (64 * s, 64 * s + 3):
+        w = gen(N, 5 + s)
+        mean = oracle.mean(w)
+        idx, _, hc = oracle.partition(w, mean)
+        prefix = oracle.partition_prefix_f64(w, mean).astype(np.float32)
+        inline, (si, sj, ss) = oracle.split_pack(w, idx, prefix, hc, mean, s,
+                                                 flags=SPLIT_FULL_LIGHT, return_splits=True)
+        rec = oracle.scalar_split(prefix, hc, mean, s, flags=SPLIT_FULL_LIGHT)
+        table = oracle.scalar_pack(w, idx, hc, mean, s, rec)
+        if N % s == 0:
+            assert np.array_equal(rec["i"], si[1:]) and np.array_equal(rec["j"], sj[1:])
+            assert np.array_equal(rec["spill"].view(np.uint32), ss[1:].view(np.uint32))
+            assert np.array_equal(table.view(np.uint64), inline.view(np.uint64))
+        implied = oracle.alias_to_weights(table)
+        assert np.abs(implied - w / w.astype(np.float64).mean()).max() < 1e-3
