@@ -965,6 +965,16 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
     rec("prefix_partition",
         timed(lambda: wrs.prefix_partition(stream, w, n, idx, prefix, elems, internals, lo)),
         20 * n, n, "weights")
+    # the FP32-carry partition, decoupled lookback against the block-wise (reduce-then-scan)
+    # baseline, which reads the weights twice (24 B / weight against 16)
+    fp32 = W.WRS(dataclasses.replace(wrs.config, scan_precision=W.SCAN_FP32))
+    rec("prefix_partition_fp32",
+        timed(lambda: fp32.prefix_partition(stream, w, n, idx, prefix, elems, internals)),
+        16 * n, n, "weights")
+    rec("prefix_partition_blockwise",
+        timed(lambda: fp32.prefix_partition_blockwise(stream, w, n, idx, prefix, elems,
+                                                      internals)), 16 * n, n, "weights")
+    wrs.prefix_partition(stream, w, n, idx, prefix, elems, internals, lo)  # the FF arrays again
     # read index 4 + element 4 + write entry 8 (split probes assumed L2-resident)
     rec("split_pack",
         timed(lambda: wrs.split_pack(stream, w, idx, prefix, elems, n, table, internals, lo)),
@@ -995,6 +1005,11 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
     its = W.WRS(W.ITSConfig(rng=W.RNG_PHILOX4X32_10, scan_precision=W.SCAN_COMPENSATED))
     cmf = torch.empty(n, dtype=torch.float32, device=w.device)
     rec("scan", timed(lambda: its.prefix_sum(stream, w, n, cmf, internals)), 8 * n, n, "weights")
+    its32 = W.WRS(W.ITSConfig(rng=W.RNG_PHILOX4X32_10))
+    rec("scan_fp32", timed(lambda: its32.prefix_sum(stream, w, n, cmf, internals)), 8 * n, n,
+        "weights")
+    rec("scan_blockwise", timed(lambda: its32.prefix_sum_blockwise(stream, w, n, cmf, internals)),
+        8 * n, n, "weights")
     rec("its_sample", timed(lambda: its.its_sample(stream, cmf, n, s, 99, 0, samples)), 4 * s, s,
         "samples")
     # through the buffers API: the compensated build also makes the guiding table, and

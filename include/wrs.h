@@ -221,6 +221,19 @@ wrs_status wrs_split_pack(const wrs_handle* h, void* stream, const float* weight
                           const uint32_t* partition_indices, const float* partition_prefix,
                           const float* partition_elements, const float* partition_prefix_lo,
                           uint32_t n, wrs_alias_entry* table, wrs_buffers* b);
+/* Block-wise (reduce-then-scan) baselines of the two decoupled-lookback kernels, kept for
+ * comparison as the reference keeps BlockWiseScan (src/device/prefix_sum/block_wise/
+ * BlockWiseScan.hpp:183-215) and BlockWisePrefixPartition (src/device/prefix_partition/
+ * block_wise/BlockWisePrefixPartition.hpp:226-329): every 4096-weight tile is reduced, the tile
+ * reductions are scanned, and every tile is scanned again with its offset (3 launches, the
+ * weights read twice).  FP32 carries (the handle's precision does not apply); the partition's
+ * pivot is the mean held in b (run wrs_total_mass first) and its heavy count lands in b. */
+wrs_status wrs_prefix_sum_blockwise(const wrs_handle* h, void* stream, const float* in,
+                                    uint32_t n, float* out, wrs_buffers* b);
+wrs_status wrs_prefix_partition_blockwise(const wrs_handle* h, void* stream, const float* weights,
+                                          uint32_t n, uint32_t* partition_indices,
+                                          float* partition_prefix, float* partition_elements,
+                                          wrs_buffers* b);
 /* Serial split-pack (SerialSplitPack::run, src/device/wrs/alias/psa/splitpack/serial/
  * SerialSplitPack.hpp:52-93): wrs_split writes the K = wrs_split_records_count(n, split_size)
  * = ceil(n / split_size) records of ScalarSplit (split/scalar/shader.comp:72-133): record k - 1

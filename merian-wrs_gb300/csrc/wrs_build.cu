@@ -368,6 +368,11 @@ struct PartArgs {
     float* prefix;
     float* elems;
     float* prefix_lo;
+    // block-wise baseline: exclusive per-tile offsets (heavy count, heavy sum, light sum)
+    // precomputed by k_bw_part_reduce + k_bw_tiles instead of the lookback
+    const uint32_t* bw_c;
+    const float* bw_h;
+    const float* bw_l;
 };
 
 // One CTA = one tile of 4096 weights.  The tile is loaded with 16-byte coalesced loads and
@@ -382,7 +387,7 @@ struct PartArgs {
 // float-float pair per tile; sums within a tile run in a fixed order.  Every prefix is then a
 // deterministic function of the weights.  FFOUT also writes prefix_lo[], the low word of the
 // prefix as a float-float pair (prefix[] is its high word), with float-float local sums.
-template <bool COMP, bool FFOUT, bool BATCH>
+template <bool COMP, bool FFOUT, bool BATCH, bool BW = false>
 __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partition(PartArgs a,
                                                                                    BatchView bv) {
     // warp totals (phase A), turned into warp-exclusive offsets by warp 0 (phase B)
@@ -403,8 +408,8 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
     float2* const s_lh = reinterpret_cast<float2*>(s_val + kTileThreads);      // lane-exclusive sums
     float2* const s_ll = reinterpret_cast<float2*>(s_val + 3 * kTileThreads);
 
-    PartState* cur;
-    const uint32_t tile = lookback_begin(a.lb, a.states, a.cap_tiles, cur);
+    PartState* cur = nullptr;
+    const uint32_t tile = BW ? blockIdx.x : lookback_begin(a.lb, a.states, a.cap_tiles, cur);
     const float* w = a.w;
     uint32_t n = a.n, first = 0;
     BuildCtrl* ctrl = a.ctrl;
@@ -528,7 +533,11 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
         }
         ff exh{0.f, 0.f}, exl{0.f, 0.f};
         uint32_t exc = 0;
-        if constexpr (COMP) {
+        if constexpr (BW) {
+            exh = {__ldg(a.bw_h + tile), 0.f};
+            exl = {__ldg(a.bw_l + tile), 0.f};
+            exc = __ldg(a.bw_c + tile);
+        } else if constexpr (COMP) {
             const int grid = fx_grid(ctrl->total);
             const PartX agg{fx_from_ff(agg_h, grid), fx_from_ff(agg_l, grid), agg_c};
             PartX ex{0, 0, 0u};
@@ -698,7 +707,7 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
         }
     }
     if (threadIdx.x == 0 && lt == tiles_for(n) - 1u) ctrl->heavy_count = ex_c + s_aggc;
-    lookback_end(a.lb);
+    if constexpr (!BW) lookback_end(a.lb);
 }
 
 template <bool BATCH>
@@ -1390,6 +1399,217 @@ cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const 
                       full_light ? 1u : 0u};
     split_dispatch<false>(st, r64, prefix_lo != nullptr, split_blocks_for(n, split_size), a,
                           BatchView{});
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------
+// block-wise (reduce-then-scan) baselines
+// ---------------------------------------------------------------------------------
+//
+// The reference's BlockWiseScan (src/device/prefix_sum/block_wise/BlockWiseScan.hpp:183-215)
+// and BlockWisePrefixPartition (src/device/prefix_partition/block_wise/
+// BlockWisePrefixPartition.hpp:226-329) are multi-pass baselines against the decoupled
+// lookback: reduce every block, scan the block reductions, then scan every block again with
+// its offset.  Here: k_bw_scan<false> / k_bw_part_reduce write each tile's FP32 aggregates
+// (the same tile and thread order as the decoupled kernels), k_bw_tiles turns them into
+// exclusive offsets in one CTA (fixed order), and k_bw_scan<true> / k_prefix_partition<...,
+// BW> scan each tile again with its offset instead of a lookback.  FP32 carries, as the
+// reference's; 12 B/weight for the scan (the weights are read twice) where the decoupled scan
+// moves 8.
+
+template <bool APPLY>
+__global__ __launch_bounds__(kTileThreads) void k_bw_scan(const float* __restrict__ in, uint32_t n,
+                                                          float* __restrict__ out,
+                                                          float* __restrict__ tile_val) {
+    __shared__ float s_w[kTileWarps];
+    const uint32_t tile = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t tbase = tile * kTileItems;
+    const uint32_t wbase = tbase + warp * kWarpItems;
+    float x[4][4];
+    load_tile(in, n, tile, x);
+    float lex[4], voff[4], run = 0.f;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        const float t = __fadd_rn(__fadd_rn(__fadd_rn(x[v][0], x[v][1]), x[v][2]), x[v][3]);
+        const float inc = warp_incl_f(t, lane);
+        const float e = __shfl_up_sync(0xffffffffu, inc, 1);
+        lex[v] = lane ? e : 0.f;
+        voff[v] = run;
+        run = __fadd_rn(run, __shfl_sync(0xffffffffu, inc, 31));
+    }
+    if (lane == 0) s_w[warp] = run;
+    __syncthreads();
+    if (warp == 0) {
+        const float t = lane < kTileWarps ? s_w[lane] : 0.f;
+        const float inc = warp_incl_f(t, lane);
+        const float e = __shfl_up_sync(0xffffffffu, inc, 1);
+        if (!APPLY && lane == kTileWarps - 1) tile_val[tile] = inc;  // the tile's aggregate
+        __syncwarp();
+        if (lane < kTileWarps) s_w[lane] = lane ? e : 0.f;
+    }
+    if constexpr (!APPLY) return;
+    __syncthreads();
+    const float ex = __ldg(tile_val + tile);  // exclusive offset (k_bw_tiles)
+    const float wex = s_w[warp];
+    const bool full = (static_cast<uint64_t>(tbase) + kTileItems <= n) &&
+                      ((reinterpret_cast<uintptr_t>(out) & 15u) == 0);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        float r = __fadd_rn(__fadd_rn(wex, voff[v]), lex[v]);
+        float y[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            r = __fadd_rn(r, x[v][c]);
+            y[c] = __fadd_rn(ex, r);
+        }
+        const uint32_t e0 = wbase + v * 128 + lane * 4;
+        if (full) {
+            __stcs(reinterpret_cast<float4*>(out + e0), make_float4(y[0], y[1], y[2], y[3]));
+        } else {
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (e0 + c < n) out[e0 + c] = y[c];
+        }
+    }
+}
+
+// Per-tile heavy count, heavy sum and light sum (items above / not above the mean).
+__global__ __launch_bounds__(kTileThreads) void k_bw_part_reduce(const float* __restrict__ w,
+                                                                 uint32_t n,
+                                                                 const BuildCtrl* __restrict__ ctrl,
+                                                                 uint32_t* __restrict__ tc,
+                                                                 float* __restrict__ th,
+                                                                 float* __restrict__ tl) {
+    __shared__ uint32_t s_c[kTileWarps];
+    __shared__ float s_h[kTileWarps], s_l[kTileWarps];
+    const uint32_t tile = blockIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float pivot = ctrl->mean;
+    float x[4][4];
+    load_tile(w, n, tile, x);
+    uint32_t c = 0;
+    float h = 0.f, l = 0.f;
+    const uint32_t wbase = tile * kTileItems + warp * kWarpItems;
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (wbase + v * 128 + lane * 4 + k >= n) continue;
+            if (x[v][k] > pivot) {
+                ++c;
+                h = __fadd_rn(h, x[v][k]);
+            } else {
+                l = __fadd_rn(l, x[v][k]);
+            }
+        }
+    const uint32_t ic = warp_incl_u(c, lane);
+    const float ih = warp_incl_f(h, lane), il = warp_incl_f(l, lane);
+    if (lane == 31) {
+        s_c[warp] = ic;
+        s_h[warp] = ih;
+        s_l[warp] = il;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t cc = warp_incl_u(lane < kTileWarps ? s_c[lane] : 0u, lane);
+        const float hh = warp_incl_f(lane < kTileWarps ? s_h[lane] : 0.f, lane);
+        const float ll = warp_incl_f(lane < kTileWarps ? s_l[lane] : 0.f, lane);
+        if (lane == kTileWarps - 1) {
+            tc[tile] = cc;
+            th[tile] = hh;
+            tl[tile] = ll;
+        }
+    }
+}
+
+// Exclusive scans, in place, of up to three per-tile arrays (any may be null) in one CTA of
+// 1024 threads: thread t sums its chunk of consecutive tiles in order, the chunk totals are
+// scanned across the CTA, then each thread rewrites its chunk as exclusive prefixes.
+constexpr int kBwThreads = 1024;
+
+__global__ __launch_bounds__(kBwThreads) void k_bw_tiles(uint32_t T, uint32_t* __restrict__ c,
+                                                         float* __restrict__ h,
+                                                         float* __restrict__ l) {
+    __shared__ uint32_t s_c[32];
+    __shared__ float s_h[32], s_l[32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t chunk = (T + kBwThreads - 1) / kBwThreads;
+    const uint32_t b0 = min(T, threadIdx.x * chunk), b1 = min(T, b0 + chunk);
+    uint32_t sc = 0;
+    float sh = 0.f, sl = 0.f;
+    for (uint32_t t = b0; t < b1; ++t) {
+        if (c) sc += c[t];
+        if (h) sh = __fadd_rn(sh, h[t]);
+        if (l) sl = __fadd_rn(sl, l[t]);
+    }
+    const uint32_t ic = warp_incl_u(sc, lane);
+    const float ih = warp_incl_f(sh, lane), il = warp_incl_f(sl, lane);
+    if (lane == 31) {
+        s_c[warp] = ic;
+        s_h[warp] = ih;
+        s_l[warp] = il;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t wc = warp_incl_u(s_c[lane], lane);
+        const float wh = warp_incl_f(s_h[lane], lane), wl = warp_incl_f(s_l[lane], lane);
+        const uint32_t ec = __shfl_up_sync(0xffffffffu, wc, 1);
+        const float eh = __shfl_up_sync(0xffffffffu, wh, 1);
+        const float el = __shfl_up_sync(0xffffffffu, wl, 1);
+        __syncwarp();
+        s_c[lane] = lane ? ec : 0u;
+        s_h[lane] = lane ? eh : 0.f;
+        s_l[lane] = lane ? el : 0.f;
+    }
+    __syncthreads();
+    // exclusive start of this thread's chunk: the warp's offset plus the lanes before it
+    const float eh = __shfl_up_sync(0xffffffffu, ih, 1), el = __shfl_up_sync(0xffffffffu, il, 1);
+    uint32_t rc = s_c[warp] + (ic - sc);
+    float rh = __fadd_rn(s_h[warp], lane ? eh : 0.f);
+    float rl = __fadd_rn(s_l[warp], lane ? el : 0.f);
+    for (uint32_t t = b0; t < b1; ++t) {
+        if (c) {
+            const uint32_t v = c[t];
+            c[t] = rc;
+            rc += v;
+        }
+        if (h) {
+            const float v = h[t];
+            h[t] = rh;
+            rh = __fadd_rn(rh, v);
+        }
+        if (l) {
+            const float v = l[t];
+            l[t] = rl;
+            rl = __fadd_rn(rl, v);
+        }
+    }
+}
+
+cudaError_t launch_prefix_sum_blockwise(cudaStream_t st, const float* in, uint32_t n, float* out,
+                                        float* tile_scratch) {
+    const uint32_t T = tiles_for(n);
+    k_bw_scan<false><<<T, kTileThreads, 0, st>>>(in, n, out, tile_scratch);
+    k_bw_tiles<<<1, kBwThreads, 0, st>>>(T, nullptr, tile_scratch, nullptr);
+    k_bw_scan<true><<<T, kTileThreads, 0, st>>>(in, n, out, tile_scratch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prefix_partition_blockwise(cudaStream_t st, const float* w, uint32_t n,
+                                              BuildCtrl* ctrl, uint32_t* tile_scratch,
+                                              uint32_t* idx_out, float* prefix_out,
+                                              float* elems_out) {
+    const uint32_t T = tiles_for(n);
+    uint32_t* tc = tile_scratch;
+    float* th = reinterpret_cast<float*>(tile_scratch + T);
+    float* tl = reinterpret_cast<float*>(tile_scratch + 2 * static_cast<size_t>(T));
+    k_bw_part_reduce<<<T, kTileThreads, 0, st>>>(w, n, ctrl, tc, th, tl);
+    k_bw_tiles<<<1, kBwThreads, 0, st>>>(T, tc, th, tl);
+    const PartArgs a{w,       n,        ctrl,     nullptr,  nullptr,   0u,
+                     0u,      &ctrl->status, idx_out, prefix_out, elems_out, nullptr,
+                     tc,      th,       tl};
+    k_prefix_partition<false, false, false, true><<<T, kTileThreads, 0, st>>>(a, BatchView{});
     return cudaGetLastError();
 }
 

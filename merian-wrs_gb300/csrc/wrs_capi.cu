@@ -49,6 +49,7 @@ struct wrs_buffers {
     uint32_t* guide = nullptr;
     ItsCell* cells = nullptr;
     uint32_t* coarse = nullptr;  // scratch of the guiding-table / cell construction
+    uint32_t* tile_scratch = nullptr;  // block-wise baselines: 3 words per tile
 };
 
 namespace {
@@ -77,7 +78,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct Layout {
     size_t ctrl, partials, part_states, scan_states, idx, prefix, elems, prefix_lo, table, records,
-        cmf, guide, cells, coarse, total;
+        cmf, guide, cells, coarse, tile_scratch, total;
 };
 
 Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
@@ -95,6 +96,7 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
     L.part_states = alias ? take(sizeof(PartState) * 2 * static_cast<size_t>(cap_tiles)) : 0;
     L.scan_states = take(sizeof(ScanState) * 2 * static_cast<size_t>(cap_tiles));
     const size_t zero_end = off;  // everything above starts zeroed
+    L.tile_scratch = take(3 * sizeof(uint32_t) * static_cast<size_t>(cap_tiles));
     (void)zero_end;
     if (alias) {
         L.idx = take(sizeof(uint32_t) * static_cast<size_t>(max_n));
@@ -241,6 +243,7 @@ wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers**
     const bool alias = h->cfg.method == WRS_METHOD_ALIAS_TABLE;
     b->part_states = alias ? reinterpret_cast<PartState*>(p + L.part_states) : nullptr;
     b->scan_states = reinterpret_cast<ScanState*>(p + L.scan_states);
+    b->tile_scratch = reinterpret_cast<uint32_t*>(p + L.tile_scratch);
     if (alias) {
         b->idx = reinterpret_cast<uint32_t*>(p + L.idx);
         b->prefix = reinterpret_cast<float*>(p + L.prefix);
@@ -362,6 +365,32 @@ wrs_status wrs_split_pack(const wrs_handle* h, void* stream, const float* weight
                                &b->ctrl->status, n, h->cfg.split_size,
                                reinterpret_cast<uint2*>(table)),
              "split pack");
+    return WRS_OK;
+}
+
+wrs_status wrs_prefix_sum_blockwise(const wrs_handle* h, void* stream, const float* in,
+                                    uint32_t n, float* out, wrs_buffers* b) {
+    if (!h || !in || !out) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    wrs_status s = check_n(b, n);
+    if (s != WRS_OK) return s;
+    WRS_CUDA(launch_prefix_sum_blockwise(as_stream(stream), in, n, out,
+                                         reinterpret_cast<float*>(b->tile_scratch)),
+             "block-wise prefix sum");
+    return WRS_OK;
+}
+
+wrs_status wrs_prefix_partition_blockwise(const wrs_handle* h, void* stream, const float* weights,
+                                          uint32_t n, uint32_t* partition_indices,
+                                          float* partition_prefix, float* partition_elements,
+                                          wrs_buffers* b) {
+    if (!h || !weights || !partition_indices || !partition_prefix)
+        return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+    wrs_status s = check_n(b, n);
+    if (s != WRS_OK) return s;
+    WRS_CUDA(launch_prefix_partition_blockwise(as_stream(stream), weights, n, b->ctrl,
+                                               b->tile_scratch, partition_indices,
+                                               partition_prefix, partition_elements),
+             "block-wise prefix partition");
     return WRS_OK;
 }
 

@@ -123,6 +123,14 @@ cudaError_t launch_prefix_partition(cudaStream_t st, bool comp, const float* w, 
 cudaError_t launch_scan(cudaStream_t st, bool comp, const float* in, uint32_t n, float* out,
                         BuildCtrl* ctrl, ScanState* states, uint32_t cap_tiles, double* partials,
                         uint32_t spin_limit = kSpinLimit);
+// block-wise (reduce-then-scan) baselines; tile_scratch: 1 (scan) or 3 (partition) words per
+// tile
+cudaError_t launch_prefix_sum_blockwise(cudaStream_t st, const float* in, uint32_t n, float* out,
+                                        float* tile_scratch);
+cudaError_t launch_prefix_partition_blockwise(cudaStream_t st, const float* w, uint32_t n,
+                                              BuildCtrl* ctrl, uint32_t* tile_scratch,
+                                              uint32_t* idx_out, float* prefix_out,
+                                              float* elems_out);
 // ScalarSplit's record (split/scalar/shader.comp:12-16, std430: 12 bytes)
 struct SplitRecord {
     uint32_t i, j;

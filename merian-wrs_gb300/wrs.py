@@ -166,6 +166,8 @@ def lib() -> C.CDLL:
             "wrs_server_get_stats": (i32, [vp, C.POINTER(ServerStats)]),
             "wrs_server_run_trace": (i32, [vp, C.POINTER(Request), C.POINTER(C.c_double), u32,
                                            C.POINTER(Completion)]),
+            "wrs_prefix_sum_blockwise": (i32, [vp, vp, vp, u32, vp, vp]),
+            "wrs_prefix_partition_blockwise": (i32, [vp, vp, vp, u32, vp, vp, vp, vp]),
             "wrs_split_records_count": (u32, [u32, u32]),
             "wrs_split": (i32, [vp, vp, vp, vp, u32, vp, vp]),
             "wrs_pack": (i32, [vp, vp, vp, vp, vp, vp, u32, vp, vp]),
@@ -374,6 +376,19 @@ class WRS:
         check(lib().wrs_split_pack(self.handle.ptr, _stream_ptr(stream), _dev_ptr(weights),
                                    _dev_ptr(idx), _dev_ptr(prefix), _dev_ptr(elems),
                                    _dev_ptr(prefix_lo), N, _dev_ptr(table), internals.ptr))
+
+    def prefix_sum_blockwise(self, stream, inp, N, out, internals) -> None:
+        """wrs_prefix_sum_blockwise: the reduce-then-scan baseline (FP32 carries)."""
+        check(lib().wrs_prefix_sum_blockwise(self.handle.ptr, _stream_ptr(stream), _dev_ptr(inp),
+                                             N, _dev_ptr(out), internals.ptr))
+
+    def prefix_partition_blockwise(self, stream, weights, N, idx, prefix, elems,
+                                   internals) -> None:
+        """wrs_prefix_partition_blockwise: the reduce-then-scan baseline (FP32 carries)."""
+        check(lib().wrs_prefix_partition_blockwise(self.handle.ptr, _stream_ptr(stream),
+                                                   _dev_ptr(weights), N, _dev_ptr(idx),
+                                                   _dev_ptr(prefix), _dev_ptr(elems),
+                                                   internals.ptr))
 
     def split(self, stream, prefix, N, records, internals, prefix_lo=None) -> None:
         """wrs_split: the serial split-pack's ceil(N / split_size) split records."""
