@@ -607,6 +607,8 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
         }
     }
     __syncthreads();  // the lane offsets are read; the staging area is free
+    // float-float: the low words of the first round's sums wait here for the second round
+    float lo_keep[16];
     {
         uint32_t hc = hc0;
         ff rh = rh0, rl = rl0;
@@ -617,6 +619,7 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 const uint32_t local = tloc + 4 * j + c;
+                lo_keep[4 * j + c] = 0.f;
                 if (local < m) {
                     const float xv = yv[c];
                     uint32_t slot;
@@ -625,7 +628,9 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
                         slot = hc++;
                         if constexpr (FFOUT) {
                             rh = ff_add_f(rh, xv);
-                            hi = carry_add<true>(ex_h, rh).hi;
+                            const ff v = carry_add<true>(ex_h, rh);
+                            hi = v.hi;
+                            lo_keep[4 * j + c] = v.lo;
                         } else {
                             rh32 = __fadd_rn(rh32, xv);
                             hi = carry_apply<COMP>(ex_h, rh32);
@@ -634,7 +639,9 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
                         slot = kTileItems - 1u - (local - hc);
                         if constexpr (FFOUT) {
                             rl = ff_add_f(rl, xv);
-                            hi = carry_add<true>(ex_l, rl).hi;
+                            const ff v = carry_add<true>(ex_l, rl);
+                            hi = v.hi;
+                            lo_keep[4 * j + c] = v.lo;
                         } else {
                             rl32 = __fadd_rn(rl32, xv);
                             hi = carry_apply<COMP>(ex_l, rl32);
@@ -674,10 +681,9 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
         if (elems_out) elems_out[pos] = s_xf[park_slot(local >> 2) * 4 + (local & 3)];
     }
     if constexpr (FFOUT) {
-        // second round for the low words: the same running sums, staged again
+        // second round for the low words, kept in registers by the first round
         __syncthreads();
         uint32_t hc = hc0;
-        ff rh = rh0, rl = rl0;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const float4 q = s_x[park_slot(warp * 128 + lane * 4 + j)];
@@ -686,14 +692,8 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
             for (int c = 0; c < 4; ++c) {
                 const uint32_t local = tloc + 4 * j + c;
                 if (local < m) {
-                    const float xv = yv[c];
-                    if (xv > pivot) {
-                        rh = ff_add_f(rh, xv);
-                        s_val[stage_idx(hc++)] = carry_add<true>(ex_h, rh).lo;
-                    } else {
-                        rl = ff_add_f(rl, xv);
-                        s_val[stage_idx(kTileItems - 1u - (local - hc))] = carry_add<true>(ex_l, rl).lo;
-                    }
+                    const uint32_t slot = yv[c] > pivot ? hc++ : kTileItems - 1u - (local - hc);
+                    s_val[stage_idx(slot)] = lo_keep[4 * j + c];
                 }
             }
         }
