@@ -1106,18 +1106,22 @@ __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, 
 // compute_split for kSplitPerThread splits at once: the bisections advance in lockstep so the
 // probes of all of them are in flight together (the search is latency-bound); each split
 // follows exactly compute_split's probe sequence and arithmetic.
+//
+// (a0, b0): the bisection state after the levels every split of the CTA decides alike (see
+// split_descent); (0, hc - 1) starts from the top.
 template <bool R64, bool FF, int V>
 __device__ __forceinline__ void compute_splits(const PackIn& c, const uint32_t (&nsplit)[V],
                                                const bool (&on)[V], uint32_t (&io)[V],
-                                               uint32_t (&jo)[V], float (&spill)[V]) {
+                                               uint32_t (&jo)[V], float (&spill)[V], int a0,
+                                               int b0) {
     int a[V], b[V];
     float target[V];
     ff tff[V];
     const uint32_t lcm1 = c.lcap;
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-        a[v] = 0;
-        b[v] = on[v] ? static_cast<int>(c.hc) - 1 : -1;
+        a[v] = a0;
+        b[v] = on[v] ? b0 : -1;
         target[v] = __fmul_rn(c.mean, __uint2float_rn(nsplit[v]));
         tff[v] = FF ? ff_target(c.mean, c.mean_lo, nsplit[v]) : ff{0.f, 0.f};
     }
@@ -1196,6 +1200,52 @@ __device__ __forceinline__ void compute_splits(const PackIn& c, const uint32_t (
         }
         io[v] = i;
         jo[v] = j;
+    }
+}
+
+// The top of the bisections of one CTA's splits, shared.  Every split of a CTA starts from
+// (a, b) = (0, hc - 1) and probes the same j while its decisions agree with the others'.  For a
+// fixed j the probed difference f(n) = heavy(j) + light(n - j) - mean * n does not increase
+// with n in exact arithmetic (one more light item adds at most the mean), and the stored
+// prefixes are non-decreasing up to a few ulps; so where the CTA's first split n0 and last
+// split n1 both evaluate f beyond a margin M of 64 ulps of the larger of their
+// (heavy + light + target) on the same side, every split n0 <= n <= n1 has |f(n)| > M - (a
+// few ulps) on that side, which its own FP32 evaluation (error below 2 ulps of its, smaller,
+// heavy + light + target) and float-float evaluation decide alike.  split_descent walks the
+// levels the two end splits decide alike with that margin and stops at the first other one;
+// starting every split of the CTA from the state it returns skips those levels without
+// changing any split (the probe sequence below it is the shader's).
+template <bool FF>
+__device__ void split_descent(const PackIn& c, uint32_t n0, uint32_t n1, int& a, int& b) {
+    a = 0;
+    b = static_cast<int>(c.hc) - 1;
+    const uint32_t lcap = c.lcap;
+    const uint32_t ns[2] = {n0, n1};
+    float t[2];
+#pragma unroll
+    for (int e = 0; e < 2; ++e)
+        t[e] = FF ? ff_target(c.mean, c.mean_lo, ns[e]).hi : __fmul_rn(c.mean, __uint2float_rn(ns[e]));
+    while (a <= b) {
+        const uint32_t j = static_cast<uint32_t>(a + ((b - a) >> 1));
+        float d[2], mag[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const uint32_t i = j > ns[e] ? lcap : min(ns[e] - j, lcap);
+            const float h = j == 0 ? 0.f : __ldg(c.prefix + j - 1);
+            const float l = i == 0 ? 0.f : __ldg(c.prefix + c.n - i);
+            const float sum = __fadd_rn(l, h);
+            d[e] = __fsub_rn(sum, t[e]);
+            mag[e] = __fadd_rn(sum, t[e]);
+        }
+        const float m = __fmul_rn(3.814697265625e-06f, fmaxf(mag[0], mag[1]));  // 64 * 2^-24
+        int dec[2];
+#pragma unroll
+        for (int e = 0; e < 2; ++e) dec[e] = d[e] < -m ? 1 : (d[e] > m ? -1 : 0);
+        if (dec[0] == 0 || dec[0] != dec[1]) break;
+        if (dec[0] > 0)
+            a = static_cast<int>(j) + 1;
+        else
+            b = static_cast<int>(j) - 1;
     }
 }
 
@@ -1279,7 +1329,29 @@ struct SplitArgs {
     uint32_t split_size;
     uint32_t full_light;
     SplitRecord* records;  // serial split-pack: the split records (split k = records[k - 1])
+    int2* descent;         // per CTA: the shared top of its bisections (k_split_descent) or null
 };
+
+// One thread per split-pack CTA: the shared descent of its splits (k_split_pack's slots
+// 1 .. kSplitSlots - 1 of the CTA, the look-ahead slots included).
+template <bool FF>
+__global__ __launch_bounds__(256) void k_split_descent(SplitArgs a) {
+    const uint32_t blk = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = a.n;
+    const uint32_t K = splits_for(n, a.split_size);
+    if (blk >= split_blocks_for(n, a.split_size)) return;
+    const uint32_t hc = a.ctrl->heavy_count;
+    int2 st = make_int2(0, static_cast<int>(hc) - 1);
+    const uint32_t k0 = max(1u, blk * kSplitPack);
+    const uint32_t k1 = min(blk * kSplitPack + kSplitSlots - 1u, K - 1u);
+    if (hc != 0u && hc < n && k0 <= k1) {
+        const PackIn c{a.w,    a.idx, a.elems, a.prefix, a.prefix_lo, n, hc, n - hc,
+                       a.full_light ? n - hc : n - hc - 1u, a.ctrl->mean, a.ctrl->mean_lo};
+        split_descent<FF>(c, k0 * a.split_size, k1 * a.split_size, st.x, st.y);
+    }
+    a.descent[blk] = st;
+}
+
 
 // Slot t of CTA b (t < kSplitSlots; thread t % kSplitThreads holds slots t and t + 512) holds
 // split k = b*kSplitPack + t (k in [0, K]) and packs subproblem k = [split_k, split_{k+1})
@@ -1350,7 +1422,9 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, Batch
             sp[v] = r.spill;
         }
     } else {
-        compute_splits<R64, FF, kSplitPerThread>(c, nsplit, on, si, sj, sp);
+        int2 d0 = make_int2(0, static_cast<int>(hc) - 1);
+        if (!BATCH && a.descent) d0 = a.descent[blk];
+        compute_splits<R64, FF, kSplitPerThread>(c, nsplit, on, si, sj, sp, d0.x, d0.y);
     }
 #pragma unroll
     for (int v = 0; v < kSplitPerThread; ++v) {
@@ -1393,12 +1467,18 @@ static void split_dispatch(cudaStream_t st, bool r64, bool ff, uint32_t grid, co
 cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const float* w,
                               const uint32_t* idx, const float* elems, const float* prefix,
                               const float* prefix_lo, const BuildCtrl* ctrl, uint32_t* status,
-                              uint32_t n, uint32_t split_size, uint2* table) {
+                              uint32_t n, uint32_t split_size, uint2* table, int2* descent) {
     const SplitArgs a{w,      n,         ctrl,   table,      idx,
                       elems,  prefix,    prefix_lo, status,  split_size,
-                      full_light ? 1u : 0u};
-    split_dispatch<false>(st, r64, prefix_lo != nullptr, split_blocks_for(n, split_size), a,
-                          BatchView{});
+                      full_light ? 1u : 0u, nullptr, descent};
+    const uint32_t blocks = split_blocks_for(n, split_size);
+    if (descent) {
+        if (prefix_lo)
+            k_split_descent<true><<<(blocks + 255u) / 256u, 256, 0, st>>>(a);
+        else
+            k_split_descent<false><<<(blocks + 255u) / 256u, 256, 0, st>>>(a);
+    }
+    split_dispatch<false>(st, r64, prefix_lo != nullptr, blocks, a, BatchView{});
     return cudaGetLastError();
 }
 

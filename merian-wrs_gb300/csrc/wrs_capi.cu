@@ -50,6 +50,7 @@ struct wrs_buffers {
     ItsCell* cells = nullptr;
     uint32_t* coarse = nullptr;  // scratch of the guiding-table / cell construction
     uint32_t* tile_scratch = nullptr;  // block-wise baselines: 3 words per tile
+    int2* descent = nullptr;           // split-pack: shared bisection tops per CTA
 };
 
 namespace {
@@ -78,7 +79,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct Layout {
     size_t ctrl, partials, part_states, scan_states, idx, prefix, elems, prefix_lo, table, records,
-        cmf, guide, cells, coarse, tile_scratch, total;
+        cmf, guide, cells, coarse, tile_scratch, descent, total;
 };
 
 Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
@@ -106,6 +107,7 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
                           ? take(sizeof(float) * static_cast<size_t>(max_n))
                           : 0;
         L.table = take(sizeof(uint2) * static_cast<size_t>(max_n));
+        L.descent = take(sizeof(int2) * static_cast<size_t>(descent_entries(max_n)));
         L.records = cfg.split_pack_mode != WRS_SPLITPACK_INLINE
                         ? take(sizeof(SplitRecord) * records_for(max_n, cfg.split_size))
                         : 0;
@@ -252,6 +254,7 @@ wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers**
                            ? reinterpret_cast<float*>(p + L.prefix_lo)
                            : nullptr;
         b->table = reinterpret_cast<uint2*>(p + L.table);
+        b->descent = reinterpret_cast<int2*>(p + L.descent);
         b->records = L.records ? reinterpret_cast<SplitRecord*>(p + L.records) : nullptr;
     } else {
         b->cmf = reinterpret_cast<float*>(p + L.cmf);
@@ -363,7 +366,7 @@ wrs_status wrs_split_pack(const wrs_handle* h, void* stream, const float* weight
                                h->cfg.split_full_light != 0, weights, partition_indices,
                                partition_elements, partition_prefix, partition_prefix_lo, b->ctrl,
                                &b->ctrl->status, n, h->cfg.split_size,
-                               reinterpret_cast<uint2*>(table)),
+                               reinterpret_cast<uint2*>(table), b->descent),
              "split pack");
     return WRS_OK;
 }
@@ -543,7 +546,7 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
     }
     WRS_CUDA(launch_split_pack(st, h->cfg.split_residual_f64 != 0, h->cfg.split_full_light != 0,
                                weights, b->idx, elems, b->prefix, lo, b->ctrl, &b->ctrl->status, n,
-                               h->cfg.split_size, b->table),
+                               h->cfg.split_size, b->table, b->descent),
              "split pack");
     return WRS_OK;
 }

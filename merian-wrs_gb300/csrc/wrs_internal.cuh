@@ -149,10 +149,14 @@ cudaError_t launch_pack_records_warp(cudaStream_t st, const float* w, const uint
                                      const float* elems, const BuildCtrl* ctrl, uint32_t* status,
                                      uint32_t n, uint32_t split_size, const SplitRecord* records,
                                      uint2* table);
+// descent: scratch of descent_entries(n) int2 (or null: every bisection starts at the top)
+__host__ __device__ inline uint32_t descent_entries(uint32_t max_n) {
+    return max_n / kSplitPack + 2u;  // split blocks at split size 1, and more
+}
 cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const float* w,
                               const uint32_t* idx, const float* elems, const float* prefix,
                               const float* prefix_lo, const BuildCtrl* ctrl, uint32_t* status,
-                              uint32_t n, uint32_t split_size, uint2* table);
+                              uint32_t n, uint32_t split_size, uint2* table, int2* descent);
 cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, const uint2* table,
                                 uint32_t n, uint64_t s, uint64_t seed, uint64_t offset,
                                 uint32_t* out);
