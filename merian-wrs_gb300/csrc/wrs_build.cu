@@ -1037,11 +1037,6 @@ __device__ __forceinline__ ff ff_target(float m, float ml, uint32_t n) {
     return fast_two_sum(s.hi, lo);
 }
 
-__device__ __forceinline__ float elem_at(const PackIn& c, uint32_t pos) {
-    if (c.elems) return __ldg(c.elems + pos);
-    const uint32_t widx = __ldg(c.idx + pos);
-    return widx < c.n ? __ldg(c.w + widx) : 0.f;
-}
 
 // splitpack/inline/shader.comp:81-114: bisection over the number of heavy items with the
 // shader's probe sequence (a = 0, b = heavyCount - 1, j = (a + b) / 2) and its FP32
@@ -1275,12 +1270,39 @@ __device__ __forceinline__ bool covered_later(const LaterSplits& L, uint32_t ite
     return false;
 }
 
-__device__ void pack(const PackIn& c, uint2* __restrict__ table, uint32_t i0, uint32_t i1,
-                     uint32_t j0, uint32_t j1, float spill, const LaterSplits* later) {
+// The partition items a CTA's subproblems walk, staged in shared memory by one coalesced pass
+// (the walks themselves read one item per step at positions that differ from thread to
+// thread): heavy positions [hlo, hlo + hcnt) at s[0, hcnt), light ranks [llo, llo + lcnt)
+// (partition position n - 1 - rank) at s[hcnt, hcnt + lcnt), each as (original index, weight
+// bits).  Items outside the windows (a split stepping back, a window larger than kPackWin)
+// are read from global memory; the values are the same.
+constexpr uint32_t kPackWin = 6144;
+struct PackWin {
+    const uint2* s;
+    uint32_t hlo, hcnt, llo, lcnt;
+};
+
+__device__ __forceinline__ uint2 item_global(const PackIn& c, uint32_t pos) {
+    const uint32_t widx = __ldg(c.idx + pos);
+    // widx < n holds for any partition this library wrote; the guard keeps a corrupt one
+    // (e.g. after a lookback wait gave up) from reading out of bounds
+    const float wt = c.elems ? __ldg(c.elems + pos) : (widx < c.n ? __ldg(c.w + widx) : 0.f);
+    return make_uint2(widx, __float_as_uint(wt));
+}
+__device__ __forceinline__ uint2 heavy_item(const PackIn& c, const PackWin& win, uint32_t pos) {
+    return pos - win.hlo < win.hcnt ? win.s[pos - win.hlo] : item_global(c, pos);
+}
+__device__ __forceinline__ uint2 light_item(const PackIn& c, const PackWin& win, uint32_t rank) {
+    return rank - win.llo < win.lcnt ? win.s[win.hcnt + rank - win.llo]
+                                     : item_global(c, c.n - 1u - rank);
+}
+
+__device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ table, uint32_t i0,
+                     uint32_t i1, uint32_t j0, uint32_t j1, float spill,
+                     const LaterSplits* later) {
     uint32_t i = i0, j = j0;
     float wv = spill;
-    if (wv == 0.0f) wv = elem_at(c, j);
-    const uint32_t last_light = c.n - 1u;
+    if (wv == 0.0f) wv = __uint_as_float(heavy_item(c, win, j).y);
     while (i < i1 || j < j1) {
         bool heavy_step;
         if (j == j1 || j == c.hc)
@@ -1289,12 +1311,10 @@ __device__ void pack(const PackIn& c, uint2* __restrict__ table, uint32_t i0, ui
             heavy_step = true;
         else
             heavy_step = wv <= c.mean;
-        const uint32_t h = __ldg(c.idx + j);
-        const uint32_t pos = heavy_step ? j + 1u : last_light - i;
-        const uint32_t widx = __ldg(c.idx + pos);
-        // widx < n holds for any partition this library wrote; the guards keep a corrupt
-        // one (e.g. after a lookback wait gave up) from reading or writing out of bounds
-        const float weight = c.elems ? __ldg(c.elems + pos) : (widx < c.n ? __ldg(c.w + widx) : 0.f);
+        const uint32_t h = heavy_item(c, win, j).x;
+        const uint2 it = heavy_step ? heavy_item(c, win, j + 1u) : light_item(c, win, i);
+        const uint32_t widx = it.x;
+        const float weight = __uint_as_float(it.y);
         float p;
         uint32_t tidx, al;
         bool owned = true;
@@ -1330,6 +1350,7 @@ struct SplitArgs {
     uint32_t full_light;
     SplitRecord* records;  // serial split-pack: the split records (split k = records[k - 1])
     int2* descent;         // per CTA: the shared top of its bisections (k_split_descent) or null
+    uint32_t stage;        // nonzero: stage the CTA's items in shared memory (kPackWin of them)
 };
 
 // One thread per split-pack CTA: the shared descent of its splits (k_split_pack's slots
@@ -1434,6 +1455,26 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, Batch
         s_spill[slot] = sp[v];
     }
     __syncthreads();
+    // stage the items of this CTA's subproblems [split_kb, split_{kb + npack}) when the launch
+    // gave the shared memory for it (the serial pack at small split sizes: measured faster
+    // there; the inline kernel's bisections lose more to the smaller L1 than its walks gain)
+    extern __shared__ uint2 s_items[];
+    PackWin win{s_items, 0u, 0u, 0u, 0u};
+    if (a.stage) {
+        const uint32_t kb = blk * kSplitPack;
+        const uint32_t npack = min(static_cast<uint32_t>(kSplitPack), K - kb);
+        win.s = s_items;
+        win.hlo = s_j[0];
+        const uint32_t hhi = min(s_j[npack] + 1u, hc);
+        win.hcnt = min(hhi > win.hlo ? hhi - win.hlo : 0u, kPackWin);
+        win.llo = s_i[0];
+        const uint32_t lhi = s_i[npack];
+        win.lcnt = min(lhi > win.llo ? lhi - win.llo : 0u, kPackWin - win.hcnt);
+        for (uint32_t q = threadIdx.x; q < win.hcnt + win.lcnt; q += blockDim.x)
+            s_items[q] = item_global(c, q < win.hcnt ? win.hlo + q
+                                                     : n - 1u - (win.llo + (q - win.hcnt)));
+    }
+    __syncthreads();
 #pragma unroll 1
     for (int v = 0; v < kSplitPerThread; ++v) {
         const int t = threadIdx.x + v * kSplitThreads;
@@ -1449,19 +1490,39 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, Batch
             (s_i[t + kSplitLook + 1] < i1 || s_j[t + kSplitLook + 1] < j1))
             atomicOr(a.status, kStatusNonMonotone);
         const LaterSplits later{s_i, s_j, t, count};
-        pack(c, table, si[v], i1, sj[v], j1, sp[v], clean ? nullptr : &later);
+        pack(c, win, table, si[v], i1, sj[v], j1, sp[v], clean ? nullptr : &later);
     }
+}
+
+// the staging window is dynamic shared memory above the 48 KB static limit
+constexpr size_t kPackWinBytes = kPackWin * sizeof(uint2);
+
+template <bool R64, bool FF, bool BATCH, bool RECORDS>
+static void launch_split_kernel(cudaStream_t st, uint32_t grid, const SplitArgs& a,
+                                const BatchView& bv) {
+    if (!a.stage) {
+        k_split_pack<R64, FF, BATCH, RECORDS><<<grid, kSplitThreads, 0, st>>>(a, bv);
+        return;
+    }
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_split_pack<R64, FF, BATCH, RECORDS>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kPackWinBytes));
+        attr = true;
+    }
+    k_split_pack<R64, FF, BATCH, RECORDS><<<grid, kSplitThreads, kPackWinBytes, st>>>(a, bv);
 }
 
 template <bool BATCH>
 static void split_dispatch(cudaStream_t st, bool r64, bool ff, uint32_t grid, const SplitArgs& a,
                            const BatchView& bv) {
     if (ff)
-        k_split_pack<true, true, BATCH><<<grid, kSplitThreads, 0, st>>>(a, bv);
+        launch_split_kernel<true, true, BATCH, false>(st, grid, a, bv);
     else if (r64)
-        k_split_pack<true, false, BATCH><<<grid, kSplitThreads, 0, st>>>(a, bv);
+        launch_split_kernel<true, false, BATCH, false>(st, grid, a, bv);
     else
-        k_split_pack<false, false, BATCH><<<grid, kSplitThreads, 0, st>>>(a, bv);
+        launch_split_kernel<false, false, BATCH, false>(st, grid, a, bv);
 }
 
 cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const float* w,
@@ -1743,10 +1804,13 @@ cudaError_t launch_pack_records(cudaStream_t st, const float* w, const uint32_t*
                                 const float* elems, const BuildCtrl* ctrl, uint32_t* status,
                                 uint32_t n, uint32_t split_size, const SplitRecord* records,
                                 uint2* table) {
+    // the CTA's items fit the staging window up to split size kPackWin / kSplitPack (12)
+    const uint32_t stage = split_size * kSplitPack <= kPackWin ? 1u : 0u;
     const SplitArgs a{w,       n,       ctrl,   table,      idx, elems,
-                      nullptr, nullptr, status, split_size, 0u,  const_cast<SplitRecord*>(records)};
+                      nullptr, nullptr, status, split_size, 0u,  const_cast<SplitRecord*>(records),
+                      nullptr, stage};
     const uint32_t blocks = (records_for(n, split_size) + kSplitPack - 1) / kSplitPack;
-    k_split_pack<false, false, false, true><<<blocks, kSplitThreads, 0, st>>>(a, BatchView{});
+    launch_split_kernel<false, false, false, true>(st, blocks, a, BatchView{});
     return cudaGetLastError();
 }
 
