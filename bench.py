@@ -63,6 +63,15 @@ E2E_CHUNKS = 8
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "alias_sample_n26_s28.md")
 
 
+def headline_config(n: int, s: int, world: int) -> dict:
+    """The headline configuration, the same for both arms."""
+    return {"workload": WORKLOAD, "N": n, "S": s, "split_size": SPLIT_SIZE,
+            "rng": "philox4x32-10", "precision": "float-float partition prefix",
+            "split": "float-float residual, light cap fixed",
+            "l2": "inputs larger than L2 (256 MB weights, 512 MB table, 1 GB samples)",
+            "parallelism": f"replicas x{world}"}
+
+
 def parse_args():
     p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     p.add_argument("--gpus", type=int, default=1)
@@ -228,8 +237,7 @@ def run_reference(args) -> None:
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "N": n, "S": s, "split_size": SPLIT_SIZE,
-                   "l2": "inputs larger than L2"},
+        "config": headline_config(n, s, args.gpus),
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": nthreads, "kind": kind,
                          "sample": f"per step: full PSA build of N=2^{args.log2n} + "
                                    f"{s_sample} alias samples timed, sampling extrapolated to "
@@ -470,12 +478,7 @@ def main() -> None:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "N": n, "S": s, "split_size": SPLIT_SIZE,
-                   "rng": "philox4x32-10", "precision": "float-float partition prefix",
-                   "split": "float-float residual, light cap fixed",
-                   "l2": "inputs larger than L2 (256 MB weights, 512 MB table, 1 GB samples)",
-                   "l2_fetch_granularity": tune["l2_fetch"],
-                   "parallelism": f"replicas x{world}"},
+        "config": headline_config(n, s, world),
         "autotune": {"l2_fetch": tune["l2_fetch"], "trials": tune["trials"],
                      "method": "wrs_autotune_alias over L2 fetch granularity 32/64/128 B at "
                                f"split size {SPLIT_SIZE} (CUDA events, 1 warm-up + 2 timed "
