@@ -498,7 +498,7 @@ def main() -> None:
         "build_ms_mean": statistics.mean(build_ms),
         "sample_ms_mean": statistics.mean(sample_ms),
         "clocks": clk,
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": 5 * args.steps,
         "device_status": {"timeout": bool(dev_status & W.DEVICE_TIMEOUT),
                           "split_overlap_beyond_window": bool(dev_status & W.DEVICE_NONMONOTONE_SPLIT)},
     }
@@ -579,7 +579,7 @@ def cpu_batch_baseline(items, total_s: int, what: str, reuse=None, seed: int = 6
 
 def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
     """The batched configuration: all 4096 distributions built and sampled by one CUDA graph
-    (wrs_batch_build + wrs_batch_sample: 4 launches), against 4096 per-call wrs_build +
+    (wrs_batch_build + wrs_batch_sample: 5 launches), against 4096 per-call wrs_build +
     wrs_sample pairs on the same stream, same inputs and seeds.  Both arms' samples are
     compared bit for bit and their per-distribution RMSE reported."""
     import numpy as np
@@ -676,7 +676,7 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
         "per_call_samples_per_s": total_s / (per_call_ms / 1e3),
         "builds_per_s": D / (batched_ms / 1e3),
         "speedup_vs_per_call": per_call_ms / batched_ms,
-        "graph_launches": 4, "per_call_launches": 4 * D,
+        "graph_launches": 5, "per_call_launches": 5 * D,
         "samples_bitwise_equal": identical,
         "rmse_mean": statistics.mean(rmse), "rmse_max": max(rmse),
         "per_call_driver": "Python loop over the C ABI (wrs_build + wrs_sample_at per "

@@ -296,7 +296,7 @@ const double* wrs_buffers_mean64(const wrs_buffers* b);
 
 /* ---- batches ------------------------------------------------------------------------
  * Many independent distributions of any sizes, built and sampled with one launch per
- * stage for the whole batch (3 build launches, 1 sampling launch), e.g. captured once into
+ * stage for the whole batch (4 build launches, 1 sampling launch), e.g. captured once into
  * a CUDA graph and replayed.  No counterpart in the reference, whose WRS::build and
  * WRS::sample (src/device/wrs/WRS.hpp:121-168) handle one distribution per call.  Each
  * distribution's table and samples are bit-for-bit those of wrs_build + wrs_sample on the
@@ -332,7 +332,7 @@ void wrs_batch_destroy(wrs_batch* b);
 wrs_status wrs_batch_set(wrs_batch* b, void* stream, const wrs_dist_desc* descs,
                          uint32_t count);
 uint32_t wrs_batch_count(const wrs_batch* b);
-/* Builds the table of every distribution with weights: 3 launches.  No host
+/* Builds the table of every distribution with weights: 4 launches.  No host
  * synchronisation and no allocation, so the call can be captured into a CUDA graph. */
 wrs_status wrs_batch_build(const wrs_handle* h, void* stream, wrs_batch* b);
 /* Samples every distribution with samples: 1 launch; capturable like wrs_batch_build. */

@@ -1355,22 +1355,39 @@ struct SplitArgs {
 
 // One thread per split-pack CTA: the shared descent of its splits (k_split_pack's slots
 // 1 .. kSplitSlots - 1 of the CTA, the look-ahead slots included).
-template <bool FF>
-__global__ __launch_bounds__(256) void k_split_descent(SplitArgs a) {
-    const uint32_t blk = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = a.n;
+// (BATCH: one thread per split-pack CTA of the whole batch, each of its distribution)
+template <bool FF, bool BATCH>
+__global__ __launch_bounds__(256) void k_split_descent(SplitArgs a, BatchView bv) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;  // the split-pack CTA
+    uint32_t blk = g, n = a.n;
+    const BuildCtrl* ctrl = a.ctrl;
+    const float* prefix = a.prefix;
+    const float* prefix_lo = a.prefix_lo;
+    int2* out = a.descent;
+    if constexpr (BATCH) {
+        if (g >= bv.split_blocks) return;
+        const uint32_t d = __ldg(bv.split_map + g);
+        const DistDesc* D = bv.dist + d;
+        n = D->n;
+        blk = g - D->split0;
+        ctrl = bv.dctrl + d;
+        prefix += D->base;
+        if (prefix_lo) prefix_lo += D->base;
+        out = bv.descent;
+    } else {
+        if (g >= split_blocks_for(n, a.split_size)) return;
+    }
     const uint32_t K = splits_for(n, a.split_size);
-    if (blk >= split_blocks_for(n, a.split_size)) return;
-    const uint32_t hc = a.ctrl->heavy_count;
+    const uint32_t hc = ctrl->heavy_count;
     int2 st = make_int2(0, static_cast<int>(hc) - 1);
     const uint32_t k0 = max(1u, blk * kSplitPack);
     const uint32_t k1 = min(blk * kSplitPack + kSplitSlots - 1u, K - 1u);
     if (hc != 0u && hc < n && k0 <= k1) {
-        const PackIn c{a.w,    a.idx, a.elems, a.prefix, a.prefix_lo, n, hc, n - hc,
-                       a.full_light ? n - hc : n - hc - 1u, a.ctrl->mean, a.ctrl->mean_lo};
+        const PackIn c{nullptr, nullptr, nullptr, prefix, prefix_lo, n, hc, n - hc,
+                       a.full_light ? n - hc : n - hc - 1u, ctrl->mean, ctrl->mean_lo};
         split_descent<FF>(c, k0 * a.split_size, k1 * a.split_size, st.x, st.y);
     }
-    a.descent[blk] = st;
+    out[g] = st;
 }
 
 
@@ -1444,7 +1461,8 @@ __global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, Batch
         }
     } else {
         int2 d0 = make_int2(0, static_cast<int>(hc) - 1);
-        if (!BATCH && a.descent) d0 = a.descent[blk];
+        const int2* desc = BATCH ? bv.descent : a.descent;
+        if (desc) d0 = desc[BATCH ? blockIdx.x : blk];
         compute_splits<R64, FF, kSplitPerThread>(c, nsplit, on, si, sj, sp, d0.x, d0.y);
     }
 #pragma unroll
@@ -1535,9 +1553,9 @@ cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const 
     const uint32_t blocks = split_blocks_for(n, split_size);
     if (descent) {
         if (prefix_lo)
-            k_split_descent<true><<<(blocks + 255u) / 256u, 256, 0, st>>>(a);
+            k_split_descent<true, false><<<(blocks + 255u) / 256u, 256, 0, st>>>(a, BatchView{});
         else
-            k_split_descent<false><<<(blocks + 255u) / 256u, 256, 0, st>>>(a);
+            k_split_descent<false, false><<<(blocks + 255u) / 256u, 256, 0, st>>>(a, BatchView{});
     }
     split_dispatch<false>(st, r64, prefix_lo != nullptr, blocks, a, BatchView{});
     return cudaGetLastError();
@@ -2025,7 +2043,8 @@ cudaError_t launch_batch_maps(cudaStream_t st, const DistDesc* dist, uint32_t co
 }
 
 // total mass -> prefix-partition -> split+pack over every distribution of the batch that
-// has weights: three launches, whatever the number and sizes of the distributions.
+// has weights: four launches (the split descent included), whatever the number and sizes of
+// the distributions.
 cudaError_t launch_batch_build(cudaStream_t st, uint32_t precision, bool r64, const BatchView& b) {
     if (b.tiles == 0) return cudaSuccess;
     k_total_mass<true><<<b.tiles, kTileThreads, 0, st>>>(nullptr, 0u, b.partials, nullptr, b);
@@ -2034,6 +2053,13 @@ cudaError_t launch_batch_build(cudaStream_t st, uint32_t precision, bool r64, co
     part_dispatch<true>(st, precision, b.tiles, pa, b);
     const SplitArgs sa{nullptr, 0u,       nullptr,     nullptr,  b.idx,        b.elems,
                        b.prefix, b.prefix_lo, b.status, b.split_size, b.full_light};
+    if (b.descent && b.split_blocks) {
+        const uint32_t g = (b.split_blocks + 255u) / 256u;
+        if (precision == 2)
+            k_split_descent<true, true><<<g, 256, 0, st>>>(sa, b);
+        else
+            k_split_descent<false, true><<<g, 256, 0, st>>>(sa, b);
+    }
     split_dispatch<true>(st, r64, precision == 2, b.split_blocks, sa, b);
     return cudaGetLastError();
 }

@@ -691,7 +691,8 @@ bool batch_caps(const wrs_config& cfg, uint32_t max_dists, uint64_t max_weights,
 }
 
 struct BatchLayout {
-    size_t bctrl, dctrl, states, dist, partials, tile_map, split_map, sample_map, idx, prefix,
+    size_t bctrl, dctrl, states, dist, partials, tile_map, split_map, descent, sample_map, idx,
+        prefix,
         elems, prefix_lo, zero_end, total;
 };
 
@@ -712,6 +713,7 @@ BatchLayout batch_layout(const wrs_config& cfg, uint32_t max_dists, uint64_t max
     L.partials = take(sizeof(double) * static_cast<size_t>(c.tiles));
     L.tile_map = take(sizeof(uint32_t) * static_cast<size_t>(c.tiles));
     L.split_map = take(sizeof(uint32_t) * static_cast<size_t>(c.split));
+    L.descent = take(sizeof(int2) * static_cast<size_t>(c.split));
     L.sample_map = take(sizeof(uint32_t) * static_cast<size_t>(c.sample));
     L.idx = take(sizeof(uint32_t) * max_weights);
     L.prefix = take(sizeof(float) * max_weights);
@@ -794,6 +796,7 @@ wrs_status wrs_batch_create(const wrs_handle* h, uint32_t max_dists, uint64_t ma
     v.dist = reinterpret_cast<const DistDesc*>(p + L.dist);
     v.tile_map = reinterpret_cast<const uint32_t*>(p + L.tile_map);
     v.split_map = reinterpret_cast<const uint32_t*>(p + L.split_map);
+    v.descent = reinterpret_cast<int2*>(p + L.descent);
     v.sample_map = reinterpret_cast<const uint32_t*>(p + L.sample_map);
     v.dctrl = reinterpret_cast<BuildCtrl*>(p + L.dctrl);
     v.lb = &b->bctrl->part;

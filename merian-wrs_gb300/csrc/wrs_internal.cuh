@@ -109,6 +109,7 @@ struct BatchView {
     uint32_t tiles, split_blocks, sample_blocks;  // grid sizes of the three launches
     uint32_t split_size;
     uint32_t full_light;
+    int2* descent;               // per split-pack CTA: the shared top of its bisections
 };
 
 // ---- launchers (defined in wrs_build.cu / wrs_sample.cu) -------------------------
