@@ -1543,15 +1543,19 @@ static void split_dispatch(cudaStream_t st, bool r64, bool ff, uint32_t grid, co
         launch_split_kernel<false, false, BATCH, false>(st, grid, a, bv);
 }
 
+constexpr uint32_t kDescentMinBlocks = 512;
+
 cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const float* w,
                               const uint32_t* idx, const float* elems, const float* prefix,
                               const float* prefix_lo, const BuildCtrl* ctrl, uint32_t* status,
                               uint32_t n, uint32_t split_size, uint2* table, int2* descent) {
     const SplitArgs a{w,      n,         ctrl,   table,      idx,
                       elems,  prefix,    prefix_lo, status,  split_size,
-                      full_light ? 1u : 0u, nullptr, descent};
+                      full_light ? 1u : 0u, nullptr,
+                      split_blocks_for(n, split_size) >= kDescentMinBlocks ? descent : nullptr};
     const uint32_t blocks = split_blocks_for(n, split_size);
-    if (descent) {
+    // the extra launch pays off once there are several waves of split-pack CTAs
+    if (descent && blocks >= kDescentMinBlocks) {
         if (prefix_lo)
             k_split_descent<true, false><<<(blocks + 255u) / 256u, 256, 0, st>>>(a, BatchView{});
         else
