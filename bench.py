@@ -63,6 +63,17 @@ E2E_CHUNKS = 8
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "alias_sample_n26_s28.md")
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest x over the ranks of the job (the job's time is its slowest replica's); x
+    itself without a process group."""
+    if dist is None or not dist.is_initialized():
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def headline_config(n: int, s: int, world: int) -> dict:
     """The headline configuration, the same for both arms."""
     return {"workload": WORKLOAD, "N": n, "S": s, "split_size": SPLIT_SIZE,
@@ -357,10 +368,7 @@ def main() -> None:
     elapsed_ms = e_start.elapsed_time(e_end)
     build_ms = [e[0].elapsed_time(e[1]) for e in evs]
     sample_ms = [e[1].elapsed_time(e[2]) for e in evs]
-    if dist is not None:
-        t = torch.tensor([elapsed_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, dist, dev)
     value = world * args.steps * s / (elapsed_ms / 1e3)
     dev_status |= internals.status()
     assert not dev_status & W.DEVICE_TIMEOUT, "a lookback wait gave up in the timed region"
@@ -439,12 +447,7 @@ def main() -> None:
         stream.wait_stream(ostream)  # the last samples are in host memory
         t1.record(stream)
         torch.cuda.synchronize()
-        ms = t0.elapsed_time(t1)
-        if dist is not None:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(t0.elapsed_time(t1), dist, dev)
 
     e2e_ms = e2e_time(e2e_step)
     e2e_value = world * args.steps * s / (e2e_ms / 1e3)
