@@ -510,7 +510,9 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_cells(
     const float v[kCellParts] = {__uint_as_float(q0.z), __uint_as_float(q0.w),
                                  __uint_as_float(q1.x), __uint_as_float(q1.y),
                                  __uint_as_float(q1.z), __uint_as_float(q1.w)};
-    if (settled && !above(v[kCellParts - 1])) {
+    // (y >= x holds for every non-decreasing CMF; the test keeps weights outside the
+    // contract -- NaN, negative -- from producing an index outside [0, N))
+    if (settled && y >= x && !above(v[kCellParts - 1])) {
         // the first part whose last value is >= T (the values are non-decreasing)
         uint32_t part = 0;
 #pragma unroll
