@@ -121,7 +121,7 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
         else if (G && cfg.scan_precision != WRS_SCAN_FP32)
             L.cells = take(sizeof(ItsCell) * G);
         if (G && cfg.scan_precision != WRS_SCAN_FP32)
-            L.coarse = take(sizeof(uint32_t) * coarse_entries(G));
+            L.coarse = take(sizeof(uint32_t) * (coarse_entries(G) + group_entries(G)));
     }
     L.total = off;
     return L;

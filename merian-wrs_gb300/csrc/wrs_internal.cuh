@@ -168,12 +168,14 @@ cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool
 cudaError_t launch_cutpoint_guide(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
                                   uint32_t* guide);
 // the same table for an exactly non-decreasing CMF (galloping searches)
-// (coarse: scratch of coarse_entries(G) words: every kCoarseStride-th entry, bracketing the
-// searches of the others)
+// (coarse: scratch of coarse_entries(G) + group_entries(G) words: every kCoarseStride-th
+// entry, then every 32nd, bracketing the searches of the others)
 constexpr uint32_t kCoarseStride = 1024;
 __host__ __device__ inline uint32_t coarse_entries(uint32_t G) {
     return (G + kCoarseStride - 1) / kCoarseStride + 1;
 }
+// starts of the groups of 32 cells (the third pass's brackets), after the coarse ones
+__host__ __device__ inline uint32_t group_entries(uint32_t G) { return (G + 31u) / 32u + 1u; }
 cudaError_t launch_guide_monotone(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
                                   uint32_t* coarse, uint32_t* guide);
 // ITS on a non-decreasing CMF through cell blocks: cell k of G equal-mass cells (the Cutpoint

@@ -406,11 +406,14 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_tree(const float*
 // Results equal the bisection's (k_its_sample_tree's).
 
 // Starts x_k = lower bound of c_k = fl(step * k) (clamped to N - 1) of the equal-mass cells of
-// a non-decreasing CMF, in two passes.  k_cell_coarse bisects the whole CMF for every
-// kCoarseStride-th start (coarse[j] = x_{j * kCoarseStride}, coarse[ceil(G / stride)] = N - 1);
-// then each cell's start lies in [coarse[j], coarse[j + 1]] (c_k is non-decreasing in k) and
-// one thread per cell bisects only that bracket.  Consecutive cells' threads share the top of
-// their searches and finish within a few hundred bytes of each other, in L1.
+// a non-decreasing CMF, in three passes, each bracketing the next (c_k is non-decreasing in k,
+// so x_k is too).  k_cell_coarse bisects the whole CMF for every kCoarseStride-th start;
+// k_cell_groups bisects, inside those brackets, for the first start of every group of 32
+// cells; then one warp per group finds its 32 starts in the group's bracket [x_{32g},
+// x_{32(g+1)}]: where that holds at most 128 values, the lanes load them with one coalesced
+// pass and each start is the bracket's start plus the number of values below its threshold,
+// found by a bisection over the values held in the warp's registers (shuffles, no dependent
+// loads); wider brackets are bisected in memory.
 __device__ __forceinline__ float cell_step(const float* __restrict__ cmf, uint32_t n, uint32_t G) {
     return __fdiv_rn(__ldg(cmf + n - 1u), __uint2float_rn(G));
 }
@@ -436,19 +439,80 @@ __device__ __forceinline__ uint32_t cell_start(const float* __restrict__ cmf, ui
                   __fmul_rn(cell_step(cmf, n, G), __uint2float_rn(k)));
 }
 
+// group[g] = x_{32 g} (N - 1 past the last cell), g <= ceil(G / 32)
+__global__ __launch_bounds__(kSampleThreads) void k_cell_groups(const float* __restrict__ cmf,
+                                                                uint32_t n, uint32_t G,
+                                                                const uint32_t* __restrict__ coarse,
+                                                                uint32_t* __restrict__ group) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= group_entries(G)) return;
+    const uint64_t k = static_cast<uint64_t>(g) * 32u;
+    group[g] = k < G ? cell_start(cmf, n, G, coarse, static_cast<uint32_t>(k)) : n - 1u;
+}
+
+// The start of cell k = 32 g + lane (all lanes of the warp call it; k >= G returns N - 1), and
+// the end of the group's bracket in hi.
+__device__ __forceinline__ uint32_t cell_start_warp(const float* __restrict__ cmf, uint32_t n,
+                                                    uint32_t G, const uint32_t* __restrict__ group,
+                                                    uint32_t g, uint32_t& hi) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lo = __ldg(group + g);
+    hi = __ldg(group + g + 1u);
+    const uint32_t k = g * 32u + lane;
+    const float t = k < G ? __fmul_rn(cell_step(cmf, n, G), __uint2float_rn(k))
+                          : __int_as_float(0x7f800000);
+    uint32_t x;
+    if (hi >= lo && hi - lo < 128u) {
+        // values lo .. lo + 127, 4 consecutive per lane (past hi or N: +inf, never below t)
+        float v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t pos = lo + 4u * lane + q;
+            v[q] = pos <= hi && pos < n ? __ldg(cmf + pos) : __int_as_float(0x7f800000);
+        }
+        // the values are non-decreasing across the lanes: find the first lane whose last
+        // value is >= t (a bisection over the lanes' maxima, fixed trip count so that every
+        // lane takes part in every shuffle), then count inside its 4 values
+        uint32_t a = 0, b = 32;
+#pragma unroll
+        for (int it = 0; it < 6; ++it) {
+            const uint32_t mid = (a + b) >> 1;
+            const float m = __shfl_sync(0xffffffffu, v[3], min(mid, 31u));
+            if (a < b) {
+                if (m < t)
+                    a = mid + 1u;
+                else
+                    b = mid;
+            }
+        }
+        const uint32_t c = min(a, 31u);
+        uint32_t in = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) in += __shfl_sync(0xffffffffu, v[q], c) < t ? 1u : 0u;
+        const uint32_t cnt = a < 32u ? 4u * a + in : 128u;
+        x = min(lo + cnt, hi);
+    } else {
+        x = k < G ? bisect(cmf, lo, hi > lo ? hi : lo, t) : n - 1u;
+    }
+    return k < G ? x : n - 1u;
+}
+
 __device__ __forceinline__ uint32_t cell_part(uint32_t x, uint32_t y) {
     return (y - x + kCellParts) / kCellParts;  // ceil((y - x + 1) / kCellParts)
 }
 
 __global__ __launch_bounds__(kSampleThreads) void k_its_cells(const float* __restrict__ cmf,
                                                               uint32_t n, uint32_t G,
-                                                              const uint32_t* __restrict__ coarse,
+                                                              const uint32_t* __restrict__ group,
                                                               ItsCell* __restrict__ cells) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;  // whole warps are launched
-    const uint32_t x = k < G ? cell_start(cmf, n, G, coarse, k) : n - 1u;
-    // the end of a cell is the next cell's start: the next lane's, except for the last lane
+    const uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // whole warps
+    if (g * 32u >= G) return;
+    uint32_t hi;
+    const uint32_t x = cell_start_warp(cmf, n, G, group, g, hi);
+    const uint32_t k = g * 32u + (threadIdx.x & 31u);
+    // the end of a cell is the next cell's start: the next lane's, or the next group's
     uint32_t y = __shfl_down_sync(0xffffffffu, x, 1);
-    if ((threadIdx.x & 31u) == 31u) y = k + 1u < G ? cell_start(cmf, n, G, coarse, k + 1u) : n - 1u;
+    if ((threadIdx.x & 31u) == 31u) y = hi;
     if (k >= G) return;
     if (k + 1u >= G) y = n - 1u;
     const uint32_t d = cell_part(x, y);
@@ -544,26 +608,38 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_cells(
 // search gives the same index, so the bracketed searches of cell_start apply.
 __global__ __launch_bounds__(kSampleThreads) void k_guide_monotone(const float* __restrict__ cmf,
                                                                    uint32_t n, uint32_t G,
-                                                                   const uint32_t* __restrict__ coarse,
+                                                                   const uint32_t* __restrict__ group,
                                                                    uint32_t* __restrict__ guide) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < G) guide[k] = cell_start(cmf, n, G, coarse, k);
+    const uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // whole warps
+    if (g * 32u >= G) return;
+    uint32_t hi;
+    const uint32_t x = cell_start_warp(cmf, n, G, group, g, hi);
+    const uint32_t k = g * 32u + (threadIdx.x & 31u);
+    if (k < G) guide[k] = x;
 }
 
-static cudaError_t launch_cell_coarse(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
-                                      uint32_t* coarse) {
-    const uint32_t m = coarse_entries(G);
+// the first two passes: coarse starts, then group starts (scratch: coarse_entries(G) +
+// group_entries(G) words); returns the group array
+static uint32_t* launch_cell_brackets(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
+                                      uint32_t* scratch) {
+    const uint32_t m = coarse_entries(G), ng = group_entries(G);
+    uint32_t* group = scratch + m;
     k_cell_coarse<<<(m + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(cmf, n, G,
-                                                                                        coarse);
-    return cudaGetLastError();
+                                                                                        scratch);
+    k_cell_groups<<<(ng + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(
+        cmf, n, G, scratch, group);
+    return group;
+}
+
+static uint32_t warp_blocks(uint32_t G) {
+    const uint64_t threads = (static_cast<uint64_t>(G) + 31u) / 32u * 32u;
+    return static_cast<uint32_t>((threads + kSampleThreads - 1) / kSampleThreads);
 }
 
 cudaError_t launch_its_cells(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
                              uint32_t* coarse, ItsCell* cells) {
-    const cudaError_t e = launch_cell_coarse(st, cmf, n, G, coarse);
-    if (e != cudaSuccess) return e;
-    k_its_cells<<<(G + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(cmf, n, G,
-                                                                                      coarse, cells);
+    uint32_t* group = launch_cell_brackets(st, cmf, n, G, coarse);
+    k_its_cells<<<warp_blocks(G), kSampleThreads, 0, st>>>(cmf, n, G, group, cells);
     return cudaGetLastError();
 }
 
@@ -641,10 +717,8 @@ cudaError_t launch_cutpoint_guide(cudaStream_t st, const float* cmf, uint32_t n,
 
 cudaError_t launch_guide_monotone(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
                                   uint32_t* coarse, uint32_t* guide) {
-    const cudaError_t e = launch_cell_coarse(st, cmf, n, G, coarse);
-    if (e != cudaSuccess) return e;
-    k_guide_monotone<<<(G + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(
-        cmf, n, G, coarse, guide);
+    uint32_t* group = launch_cell_brackets(st, cmf, n, G, coarse);
+    k_guide_monotone<<<warp_blocks(G), kSampleThreads, 0, st>>>(cmf, n, G, group, guide);
     return cudaGetLastError();
 }
 
