@@ -1018,6 +1018,14 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
         8 * n, n, "weights")
     rec("its_sample", timed(lambda: its.its_sample(stream, cmf, n, s, 99, 0, samples)), 4 * s, s,
         "samples")
+    # FP32 ITS through the buffers API: the build also stores the probe tree's levels 12 .. 19
+    # and the bisection reads them from there (the same samples as its_sample on that CMF)
+    its32_bufs = W.WRSBuffers(w, samples, W.Internals(its32.handle, n))
+    rec("its_build_fp32", timed(lambda: its32.build(stream, its32_bufs, n)), 8 * n, n,
+        "weights")
+    rec("its_sample_stored_levels",
+        timed(lambda: its32.sample(stream, its32_bufs, n, s, seed=99)), 4 * s, s, "samples")
+    del its32_bufs
     # through the buffers API: the compensated build also makes the guiding table, and
     # sampling runs the guided search (same samples as the bisection)
     its_bufs = W.WRSBuffers(w, samples, W.Internals(its.handle, n))

@@ -168,7 +168,10 @@ wrs_status wrs_config_init(wrs_config* cfg, uint32_t method);
 wrs_status wrs_create(const wrs_config* cfg, wrs_handle** out);
 void wrs_destroy(wrs_handle* h);
 
-/* Internals for distributions of up to max_n weights (one cudaMalloc). */
+/* Internals for distributions of up to max_n weights (one cudaMalloc).  For ITS on the FP32
+ * CMF above 2^16 weights they include the bisection's stored probe-tree blocks (at most ~2/7
+ * of the CMF's bytes), which wrs_build writes and wrs_sample reads for the n built last; the
+ * primitive wrs_its_sample probes the CMF alone (same samples). */
 size_t wrs_buffers_bytes(const wrs_handle* h, uint32_t max_n);
 wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers** out);
 void wrs_buffers_destroy(wrs_buffers* b);

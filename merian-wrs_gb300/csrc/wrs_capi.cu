@@ -6,7 +6,8 @@
 //   alias build : k_total_mass -> k_prefix_partition -> k_split_pack
 //                 (PSA::run, src/device/wrs/alias/psa/PSA.hpp:170-237)
 //   ITS build   : k_scan (ITS::build, src/device/wrs/its/ITS.hpp:90-108), then in the
-//                 compensated precisions k_its_cells (the cell blocks k_its_sample_cells reads)
+//                 compensated precisions k_its_cells (the cell blocks k_its_sample_cells reads),
+//                 otherwise k_its_tree (the bisection's probe-tree block levels)
 //   Cutpoint    : k_scan -> k_cutpoint_guide, or k_guide_monotone on the compensated CMF
 //                 (Cutpoint::build, src/device/wrs/cutpoint/Cutpoint.hpp:108-138)
 //   sample      : k_alias_sample | k_its_sample (k_its_sample_cells) | k_cutpoint_sample
@@ -48,6 +49,8 @@ struct wrs_buffers {
     float* cmf = nullptr;
     uint32_t* guide = nullptr;
     ItsCell* cells = nullptr;
+    TreeBlock* tree = nullptr;   // ITS bisection: the probe tree's stored block levels
+    uint32_t tree_n = 0;         // the n the last build stored them for (0: none)
     uint32_t* coarse = nullptr;  // scratch of the guiding-table / cell construction
     uint32_t* tile_scratch = nullptr;  // block-wise baselines: 3 words per tile
     int2* descent = nullptr;           // split-pack: shared bisection tops per CTA
@@ -79,8 +82,17 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct Layout {
     size_t ctrl, partials, part_states, scan_states, idx, prefix, elems, prefix_lo, table, records,
-        cmf, guide, cells, coarse, tile_scratch, descent, total;
+        cmf, guide, cells, tree, coarse, tile_scratch, descent, total;
 };
+
+// ITS bisects the whole CMF with the non-cooperative sampler, and its CMF is deep enough for
+// stored block levels below the probe tree's shared-memory ones: the build stores them
+// (k_its_tree)
+bool its_tree_levels(const wrs_config& cfg, uint32_t n) {
+    const bool cells = cfg.guiding_entry_size != 0 && cfg.scan_precision != WRS_SCAN_FP32;
+    return cfg.method == WRS_METHOD_ITS && cfg.coop_size == 0 && !cells &&
+           its_tree_block_levels(n) > 0;
+}
 
 Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
     const uint32_t cap_tiles = tiles_for(max_n) + 1;
@@ -122,6 +134,9 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
             L.cells = take(sizeof(ItsCell) * G);
         if (G && cfg.scan_precision != WRS_SCAN_FP32)
             L.coarse = take(sizeof(uint32_t) * (coarse_entries(G) + group_entries(G)));
+        // ITS bisecting the whole CMF (FP32, or no cells): the probe tree's deeper levels
+        if (its_tree_levels(cfg, max_n))
+            L.tree = take(sizeof(TreeBlock) * its_tree_blocks(its_tree_block_levels(max_n)));
     }
     L.total = off;
     return L;
@@ -260,6 +275,7 @@ wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers**
         b->cmf = reinterpret_cast<float*>(p + L.cmf);
         b->guide = L.guide ? reinterpret_cast<uint32_t*>(p + L.guide) : nullptr;
         b->cells = L.cells ? reinterpret_cast<ItsCell*>(p + L.cells) : nullptr;
+        b->tree = L.tree ? reinterpret_cast<TreeBlock*>(p + L.tree) : nullptr;
         b->coarse = L.coarse ? reinterpret_cast<uint32_t*>(p + L.coarse) : nullptr;
     }
     e = cudaMemset(b->base, 0, zeroed_bytes(h->cfg, max_n));
@@ -514,6 +530,12 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
                      "guiding table");
         else if (its_guided(h))
             WRS_CUDA(launch_its_cells(st, b->cmf, n, G, b->coarse, b->cells), "ITS cells");
+        b->tree_n = 0;
+        if (b->tree && its_tree_levels(h->cfg, n)) {
+            WRS_CUDA(launch_its_tree(st, b->cmf, n, its_tree_block_levels(n), b->tree),
+                     "ITS probe tree");
+            b->tree_n = n;
+        }
         return WRS_OK;
     }
     if (h->cfg.use_partition_elements && !b->elems)
@@ -567,6 +589,14 @@ wrs_status wrs_sample_at(const wrs_handle* h, void* stream, const wrs_buffers* b
             WRS_CUDA(launch_its_sample_cells(as_stream(stream), h->cfg.rng, b->cmf, n, b->cells,
                                              guide_entries(n, h->cfg.guiding_entry_size), s,
                                              seed, offset, samples),
+                     "its sample");
+            return WRS_OK;
+        }
+        if (b->tree && b->tree_n == n && its_tree_levels(h->cfg, n) && s) {
+            // the bisection with the probe tree's block levels read from the build's copy
+            if (!samples) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+            WRS_CUDA(launch_its_sample(as_stream(stream), h->cfg.rng, 0, false, b->cmf, n, s, seed,
+                                       offset, samples, b->tree, its_tree_block_levels(n)),
                      "its sample");
             return WRS_OK;
         }

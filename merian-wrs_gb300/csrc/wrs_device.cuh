@@ -370,6 +370,13 @@ __device__ __forceinline__ void ld_u32x8_policy(const uint32_t* p, uint64_t pol,
                    "=r"(b.w)
                  : "l"(p), "l"(pol));
 }
+// 32 bytes in one request without an L2 policy; p 32-byte aligned
+__device__ __forceinline__ void ld_u32x8(const uint32_t* p, uint4& a, uint4& b) {
+    asm volatile("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z),
+                   "=r"(b.w)
+                 : "l"(p));
+}
 __device__ __forceinline__ uint4 ld_u32x4_policy(const uint32_t* p, uint64_t pol) {
     uint4 v;
     asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"

@@ -161,9 +161,43 @@ cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const 
 cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, const uint2* table,
                                 uint32_t n, uint64_t s, uint64_t seed, uint64_t offset,
                                 uint32_t* out);
+// The non-cooperative ITS sampler's bisection probes one implicit binary tree (node k, root
+// 1: the range left by the decisions spelled by the bits of k below its leading one).  Its
+// top kTreeTop levels sit in each CTA's shared memory; the build can store the next
+// kTreeBlockLevels * B levels as blocks of three levels -- a node and its 6 descendants, 7
+// probe values (slot 7 unused) in one 32-byte sector -- so that one random read resolves
+// three levels.  Block level b holds the blocks rooted at the 2^(kTreeTop + 3b) nodes of tree
+// level kTreeTop + 3b, after the blocks of the levels above it.
+constexpr uint32_t kTreeTop = 12;
+constexpr uint32_t kTreeBlockLevels = 3;
+struct alignas(32) TreeBlock {
+    float v[8];
+};
+static_assert(sizeof(TreeBlock) == 32, "one probe-tree block is one 32-byte sector");
+// levels of the bisection of n values: ceil(log2 n)
+__host__ __device__ inline uint32_t its_tree_depth(uint32_t n) {
+    uint32_t t = 0;
+    while (t < 32u && (1ull << t) < n) ++t;
+    return t;
+}
+// block levels stored for n values: after them the bisection's range holds at most 16 values
+// (a 64-byte stretch of the CMF), and the blocks take at most ~2/7 of the CMF's bytes
+__host__ __device__ inline uint32_t its_tree_block_levels(uint32_t n) {
+    const uint32_t t = its_tree_depth(n);
+    return t >= kTreeTop + 5u ? (t - kTreeTop - 2u) / kTreeBlockLevels : 0u;
+}
+// blocks in the first B block levels
+__host__ __device__ inline size_t its_tree_blocks(uint32_t B) {
+    size_t s = 0;
+    for (uint32_t b = 0; b < B; ++b) s += size_t(1) << (kTreeTop + kTreeBlockLevels * b);
+    return s;
+}
+cudaError_t launch_its_tree(cudaStream_t st, const float* cmf, uint32_t n, uint32_t B,
+                            TreeBlock* blocks);
 cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool parray,
-                              const float* cmf, uint32_t n, uint64_t s, uint64_t seed,
-                              uint64_t offset, uint32_t* out);
+                              const float* cmf, uint32_t n, uint64_t S, uint64_t seed,
+                              uint64_t offset, uint32_t* out, const TreeBlock* blocks = nullptr,
+                              uint32_t B = 0);
 
 cudaError_t launch_cutpoint_guide(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
                                   uint32_t* guide);

@@ -293,11 +293,60 @@ __device__ __forceinline__ void tree_range(uint32_t k, uint32_t last, uint32_t& 
     }
 }
 
+static_assert(kItsTreeLevels == static_cast<int>(kTreeTop), "shared levels above the blocks");
+
+// One thread per stored block (TreeBlock): the range of its root node, then the ranges of the
+// root's 6 descendants and the probe values of the 7 nodes (0 for a node whose range is one
+// index: no search reaches it with a probe).  Slot 7 holds the root's range [x, x + len - 1]
+// as x | (len - floor(n / 2^level)) << 31: the ranges of one tree level are floor(n / 2^level)
+// or one more long (the left half of a range takes the odd index), and x < 2^31.
+__global__ __launch_bounds__(kSampleThreads) void k_its_tree(const float* __restrict__ cmf,
+                                                             uint32_t n, uint32_t B,
+                                                             TreeBlock* __restrict__ blocks) {
+    const size_t gb = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (gb >= its_tree_blocks(B)) return;
+    uint32_t level = kTreeTop;
+    size_t off = 0;
+    while (gb >= off + (size_t(1) << level)) {
+        off += size_t(1) << level;
+        level += kTreeBlockLevels;
+    }
+    uint32_t xs[8], ys[8];
+    tree_range((1u << level) + static_cast<uint32_t>(gb - off), n - 1u, xs[1], ys[1]);
+    float v[8];
+#pragma unroll
+    for (int j = 1; j < 8; ++j) {
+        const bool live = xs[j] < ys[j];
+        const uint32_t mid = xs[j] + ((ys[j] - xs[j]) >> 1);
+        v[j - 1] = live ? __ldg(cmf + mid) : 0.0f;
+        if (j < 4) {
+            // children: a finished range leaves finished ones
+            xs[2 * j] = xs[j];
+            ys[2 * j] = live ? mid : xs[j];
+            xs[2 * j + 1] = live ? mid + 1 : xs[j];
+            ys[2 * j + 1] = live ? ys[j] : xs[j];
+        }
+    }
+    v[7] = __uint_as_float(xs[1] | ((ys[1] - xs[1] + 1u - (n >> level)) << 31));
+    float4* dst = reinterpret_cast<float4*>(blocks + gb);
+    dst[0] = make_float4(v[0], v[1], v[2], v[3]);
+    dst[1] = make_float4(v[4], v[5], v[6], v[7]);
+}
+
+// With stored blocks (B > 0, so n > 2^16) no range ends above the tail: the ranges of tree
+// level l hold at least floor(n / 2^l) >= 4 indices for every l below the last block level's
+// bottom.  The shared and all but the last block levels then only follow the node (its probe
+// value is the tree's); the last block's slot 7 gives the range of its root, and the searches
+// track their ranges from there.  A decision is one comparison: "T > c" (the exact target's
+// tie rule folded into the FP32 target: T_hi + a positive remainder is > c exactly when the
+// next float above T_hi is > c).
 template <uint32_t RNG>
 __global__ __launch_bounds__(kSampleThreads) void k_its_sample_tree(const float* __restrict__ cmf,
                                                                     uint32_t n, uint64_t S,
                                                                     uint64_t seed, uint64_t offset,
-                                                                    uint32_t* __restrict__ out) {
+                                                                    uint32_t* __restrict__ out,
+                                                                    const TreeBlock* __restrict__ blocks,
+                                                                    uint32_t B) {
     __shared__ float s_tree[kItsTreeNodes];
     const uint32_t last = n - 1u;
     for (uint32_t k = threadIdx.x + 1; k < kItsTreeNodes; k += blockDim.x) {
@@ -309,16 +358,14 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_tree(const float*
     const float total = __ldg(cmf + last);
     for (uint64_t grp = blockIdx.x; grp * kItsGroup < S; grp += gridDim.x) {
         const uint64_t s0 = grp * kItsGroup + threadIdx.x;
-        float t_hi[kItsPerThread];
-        int t_sgn[kItsPerThread];
+        float t[kItsPerThread];  // a search goes right at probe c exactly when t > c
         uint32_t x[kItsPerThread], y[kItsPerThread], node[kItsPerThread];
         if constexpr (RNG == RNG_REF) {
             const uint32_t seed32 = static_cast<uint32_t>(seed);
 #pragma unroll
             for (int v = 0; v < kItsPerThread; ++v) {
                 const uint32_t g = static_cast<uint32_t>(offset + s0 + v * kSampleThreads);
-                t_hi[v] = search_range_u(cmf, 0, last, unit_ref(wang_hash((seed32 ^ 0xA9EC5C80u) + g)));
-                t_sgn[v] = 0;
+                t[v] = search_range_u(cmf, 0, last, unit_ref(wang_hash((seed32 ^ 0xA9EC5C80u) + g)));
             }
         } else {
             uint2 ks[10];
@@ -328,31 +375,92 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_tree(const float*
                 const uint64_t g = offset + s0 + v * kSampleThreads;
                 const uint4 r = philox4x32_10(
                     make_uint4(static_cast<uint32_t>(g), static_cast<uint32_t>(g >> 32), 0u, 0u), ks);
-                exact_target(r.x, total, t_hi[v], t_sgn[v]);
+                float t_hi;
+                int t_sgn;
+                exact_target(r.x, total, t_hi, t_sgn);
+                // t_hi >= 0: the next float above is one bit pattern up (+inf above the largest)
+                t[v] = t_sgn > 0 ? __uint_as_float(__float_as_uint(t_hi) + 1u) : t_hi;
             }
         }
+        if (B > 0) {
 #pragma unroll
-        for (int v = 0; v < kItsPerThread; ++v) {
-            x[v] = 0;
-            y[v] = s0 + v * kSampleThreads < S ? last : 0u;
-            node[v] = 1;
-        }
-        // levels held in shared memory
+            for (int v = 0; v < kItsPerThread; ++v) node[v] = 1;
+#pragma unroll
+            for (int l = 0; l < kItsTreeLevels; ++l)
+#pragma unroll
+                for (int v = 0; v < kItsPerThread; ++v)
+                    node[v] = 2 * node[v] + (t[v] > s_tree[node[v]] ? 1u : 0u);
+            const TreeBlock* level_blocks = blocks;
+            uint32_t level = kTreeTop;
 #pragma unroll 1
-        for (int l = 0; l < kItsTreeLevels; ++l) {
+            for (uint32_t bl = 0; bl < B; ++bl, level += kTreeBlockLevels) {
+                const uint32_t first = 1u << level;  // the level's first node
+                uint4 lo[kItsPerThread], hi[kItsPerThread];
+#pragma unroll
+                for (int v = 0; v < kItsPerThread; ++v)
+                    ld_u32x8(reinterpret_cast<const uint32_t*>(level_blocks + (node[v] - first)),
+                             lo[v], hi[v]);
+                level_blocks += first;
+                if (bl + 1 < B) {
+#pragma unroll
+                    for (int v = 0; v < kItsPerThread; ++v) {
+                        const uint32_t r0 = t[v] > __uint_as_float(lo[v].x) ? 1u : 0u;
+                        const uint32_t r1 =
+                            t[v] > __uint_as_float(r0 ? lo[v].z : lo[v].y) ? 1u : 0u;
+                        const uint32_t c2 = r0 ? (r1 ? hi[v].z : hi[v].y) : (r1 ? hi[v].x : lo[v].w);
+                        const uint32_t r2 = t[v] > __uint_as_float(c2) ? 1u : 0u;
+                        node[v] = 8 * node[v] + 4 * r0 + 2 * r1 + r2;
+                    }
+                } else {
+                    const uint32_t floor_len = n >> level;
+#pragma unroll
+                    for (int v = 0; v < kItsPerThread; ++v) {
+                        x[v] = hi[v].w & 0x7fffffffu;
+                        y[v] = x[v] + floor_len + (hi[v].w >> 31) - 1u;
+                        uint32_t mid = x[v] + ((y[v] - x[v]) >> 1);
+                        const uint32_t r0 = t[v] > __uint_as_float(lo[v].x) ? 1u : 0u;
+                        x[v] = r0 ? mid + 1 : x[v];
+                        y[v] = r0 ? y[v] : mid;
+                        mid = x[v] + ((y[v] - x[v]) >> 1);
+                        const uint32_t r1 =
+                            t[v] > __uint_as_float(r0 ? lo[v].z : lo[v].y) ? 1u : 0u;
+                        x[v] = r1 ? mid + 1 : x[v];
+                        y[v] = r1 ? y[v] : mid;
+                        mid = x[v] + ((y[v] - x[v]) >> 1);
+                        const uint32_t c2 = r0 ? (r1 ? hi[v].z : hi[v].y) : (r1 ? hi[v].x : lo[v].w);
+                        const uint32_t r2 = t[v] > __uint_as_float(c2) ? 1u : 0u;
+                        x[v] = r2 ? mid + 1 : x[v];
+                        y[v] = r2 ? y[v] : mid;
+                        // the tail reads stay inside the CMF whatever the block holds
+                        y[v] = min(y[v], last);
+                        x[v] = min(x[v], y[v]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < kItsPerThread; ++v)
+                if (s0 + v * kSampleThreads >= S) y[v] = x[v];  // past the end: no tail loads
+        } else {
+            // the shared levels with ranges (short CMFs end inside them)
 #pragma unroll
             for (int v = 0; v < kItsPerThread; ++v) {
-                if (x[v] < y[v]) {
-                    const uint32_t mid = x[v] + ((y[v] - x[v]) >> 1);
-                    const float c = s_tree[node[v]];
-                    const bool right = RNG == RNG_REF ? t_hi[v] > c
-                                                      : (t_hi[v] > c || (t_hi[v] == c && t_sgn[v] > 0));
-                    if (right) {
-                        x[v] = mid + 1;
-                        node[v] = 2 * node[v] + 1;
-                    } else {
-                        y[v] = mid;
-                        node[v] = 2 * node[v];
+                x[v] = 0;
+                y[v] = s0 + v * kSampleThreads < S ? last : 0u;
+                node[v] = 1;
+            }
+#pragma unroll 1
+            for (int l = 0; l < kItsTreeLevels; ++l) {
+#pragma unroll
+                for (int v = 0; v < kItsPerThread; ++v) {
+                    if (x[v] < y[v]) {
+                        const uint32_t mid = x[v] + ((y[v] - x[v]) >> 1);
+                        if (t[v] > s_tree[node[v]]) {
+                            x[v] = mid + 1;
+                            node[v] = 2 * node[v] + 1;
+                        } else {
+                            y[v] = mid;
+                            node[v] = 2 * node[v];
+                        }
                     }
                 }
             }
@@ -371,10 +479,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_tree(const float*
             for (int v = 0; v < kItsPerThread; ++v) {
                 if (x[v] < y[v]) {
                     const uint32_t mid = x[v] + ((y[v] - x[v]) >> 1);
-                    const bool right = RNG == RNG_REF
-                                           ? t_hi[v] > c[v]
-                                           : (t_hi[v] > c[v] || (t_hi[v] == c[v] && t_sgn[v] > 0));
-                    if (right)
+                    if (t[v] > c[v])
                         x[v] = mid + 1;
                     else
                         y[v] = mid;
@@ -770,9 +875,20 @@ cudaError_t launch_batch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t co
     return cudaGetLastError();
 }
 
+cudaError_t launch_its_tree(cudaStream_t st, const float* cmf, uint32_t n, uint32_t B,
+                            TreeBlock* blocks) {
+    const size_t count = its_tree_blocks(B);
+    if (count == 0) return cudaSuccess;
+    const size_t grid = (count + kSampleThreads - 1) / kSampleThreads;
+    if (grid > 0x7fffffffull) return cudaErrorInvalidValue;
+    k_its_tree<<<static_cast<unsigned>(grid), kSampleThreads, 0, st>>>(cmf, n, B, blocks);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool parray,
                               const float* cmf, uint32_t n, uint64_t S, uint64_t seed,
-                              uint64_t offset, uint32_t* out) {
+                              uint64_t offset, uint32_t* out, const TreeBlock* tree,
+                              uint32_t B) {
     const uint64_t blocks = (S + kSampleThreads - 1) / kSampleThreads;
     if (blocks == 0) return cudaSuccess;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
@@ -781,9 +897,11 @@ cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool
         const uint64_t groups = (S + kItsGroup - 1) / kItsGroup;
         const unsigned tb = static_cast<unsigned>(groups < kItsMaxBlocks ? groups : kItsMaxBlocks);
         if (rng == RNG_REF)
-            k_its_sample_tree<RNG_REF><<<tb, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, out);
+            k_its_sample_tree<RNG_REF><<<tb, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, out,
+                                                                      tree, B);
         else
-            k_its_sample_tree<RNG_PHILOX><<<tb, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, out);
+            k_its_sample_tree<RNG_PHILOX><<<tb, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset,
+                                                                         out, tree, B);
     } else if (parray) {
         k_its_sample<RNG_REF, 2><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
     } else {

@@ -374,6 +374,38 @@ def test_its_sample_edge_sizes(pkg, cuda, oracle, N, rng):
     assert np.array_equal(got, ref)
 
 
+@pytest.mark.parametrize("rng", [RNG_REFERENCE, RNG_PHILOX4X32_10])
+def test_its_stored_tree_blocks(pkg, cuda, oracle, rng):
+    """The FP32 build stores the bisection's probe-tree levels below the shared-memory ones as
+    blocks of three levels: samples through the buffers equal those of the primitive that
+    probes the CMF itself at 2^22 + 3 (3 block levels), 2^19 + 1 (2) and 2^16 + 1 (1), the
+    same buffers rebuilt for each smaller size; the last equals the oracle."""
+    import torch
+    W = pkg.wrs
+    cfg = pkg.ITSConfig(rng=rng)
+    wrs = W.WRS(cfg)
+    sizes = ((1 << 22) + 3, (1 << 19) + 1, (1 << 16) + 1)
+    bufs = W.WRSBuffers.allocate(sizes[0], 1, cfg, handle=wrs.handle)
+    S = (1 << 21) + 9
+    small = sizes[-1]
+    for N in sizes:
+        w = weights_lognormal(N, N)
+        bufs.weights[:N].copy_(h2d(w))
+        wrs.build(None, bufs, N)
+        out = torch.empty(S, dtype=torch.int32, device="cuda")
+        bufs.samples = out
+        wrs.sample(None, bufs, N, S, 31, offset=4)
+        plain = torch.empty(S, dtype=torch.int32, device="cuda")
+        cmf = bufs.internals.views()["cmf"]
+        wrs.its_sample(None, cmf, N, S, 31, 4, plain)
+        torch.cuda.synchronize()
+        assert bufs.internals.status() == 0
+        assert torch.equal(out, plain)
+    got = t2h(out, np.uint32)
+    ref = oracle.its_sample(d2h(cmf, small, np.float32), S, 31, rng=rng, offset=4, nthreads=8)
+    assert np.array_equal(got, ref)
+
+
 # ------------------------------------------------------------------- cutpoint ---
 
 @pytest.mark.parametrize("N,entry", [(1, 32), (5, 1), (1000, 32), (4097, 128), (300001, 32),
