@@ -101,6 +101,8 @@ def parse_args():
                    help="skip the plain small configuration (N = 65,536)")
     p.add_argument("--no-precision", action="store_true",
                    help="skip the precision study (N = 2^28, S = 2^30)")
+    p.add_argument("--batched-only", action="store_true",
+                   help="only run the batched configuration and print its object (profiling)")
     p.add_argument("--probe-gather", action="store_true",
                    help="only measure the random-gather rate per load width and exit")
     return p.parse_args()
@@ -320,6 +322,11 @@ def main() -> None:
     wrs = W.WRS(cfg)
     stream = torch.cuda.current_stream()
     dev = torch.device("cuda", local)
+    if args.batched_only:
+        print(json.dumps({"batched": batched_leg(W, cfg, dev, stream, max(3, args.steps // 2),
+                                                 max(3, args.warmup),
+                                                 cpu=not args.no_cpu_baseline)}))
+        return
     weights = [make_weights(d, n, SEEDS[d] + 1000 * rank, dev) for d in range(3)]
     internals = W.Internals(wrs.handle, n)
     samples = torch.empty(s, dtype=torch.int32, device=dev)
@@ -511,7 +518,7 @@ def main() -> None:
                                            stream, pk["hbm_gbs"], args)
     if not args.no_batched:
         line["batched"] = batched_leg(W, cfg, dev, stream, max(3, args.steps // 2),
-                                      max(3, args.warmup))
+                                      max(3, args.warmup), cpu=not args.no_cpu_baseline)
     if not args.no_served:
         line["served"] = served_leg(W, cfg, dev)
     if not args.no_small:
@@ -580,7 +587,7 @@ def cpu_batch_baseline(items, total_s: int, what: str, reuse=None, seed: int = 6
                        if reuse is not None else "")}
 
 
-def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
+def batched_leg(W, cfg, dev, stream, steps: int, warmup: int, cpu: bool = True) -> dict:
     """The batched configuration: all 4096 distributions built and sampled by one CUDA graph
     (wrs_batch_build + wrs_batch_sample: 5 launches), against 4096 per-call wrs_build +
     wrs_sample pairs on the same stream, same inputs and seeds.  Both arms' samples are
@@ -625,6 +632,18 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
     e1.record(stream)
     torch.cuda.synchronize()
     batched_ms = e0.elapsed_time(e1) / steps
+    assert batch.status() == 0
+    # the graph's two halves timed apart (the 4 build launches, the sampling launch)
+    stages = {}
+    for name, fn in (("build_ms", lambda: batch.build(stream)),
+                     ("sample_ms", lambda: batch.sample(stream))):
+        fn()
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        stages[name] = e0.elapsed_time(e1) / steps
     assert batch.status() == 0
 
     # per call: one buffers object sized for the largest distribution, reused
@@ -674,7 +693,7 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
                      "method": "wrs_autotune_batch: L2 fetch granularity 32/64/128 B at split "
                                f"size {SPLIT_SIZE}, then split sizes 4-32 at the best L2 value "
                                "(CUDA events, 1 warm-up + 2 timed batch build+sample each)"},
-        "graph_ms": batched_ms, "per_call_ms": per_call_ms,
+        "graph_ms": batched_ms, "stages": stages, "per_call_ms": per_call_ms,
         "samples_per_s": total_s / (batched_ms / 1e3),
         "per_call_samples_per_s": total_s / (per_call_ms / 1e3),
         "builds_per_s": D / (batched_ms / 1e3),
@@ -686,7 +705,8 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int) -> dict:
                            "distribution), one reused buffers object",
         "cpu_baseline": cpu_batch_baseline(
             [(w[int(w_off[d]):int(w_off[d]) + int(sizes[d])], int(counts[d]), seeds[d])
-             for d in range(D)], total_s, "distributions", split_size=cfg.split_size),
+             for d in range(D)], total_s, "distributions", split_size=cfg.split_size)
+        if cpu else None,
     }
 
 
