@@ -386,7 +386,9 @@ struct PartArgs {
 // along the lookback exactly in fixed point (fx_*) and the carry is rounded once to a
 // float-float pair per tile; sums within a tile run in a fixed order.  Every prefix is then a
 // deterministic function of the weights.  FFOUT also writes prefix_lo[], the low word of the
-// prefix as a float-float pair (prefix[] is its high word), with float-float local sums.
+// prefix as a float-float pair (prefix[] is its high word): float-float local sums give the
+// carried prefix before each thread's first item, and the thread adds its items to that in
+// float-float.
 template <bool COMP, bool FFOUT, bool BATCH, bool BW = false>
 __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partition(PartArgs a,
                                                                                    BatchView bv) {
@@ -599,8 +601,10 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
     {
         const float2 lh = s_lh[threadIdx.x], ll = s_ll[threadIdx.x];
         if constexpr (FFOUT) {
-            rh0 = carry_add<true>(s_fh[warp], ff{lh.x, lh.y});
-            rl0 = carry_add<true>(s_fl[warp], ff{ll.x, ll.y});
+            // the carried prefix before the thread's first item; the items are then added
+            // to it one by one in float-float
+            rh0 = carry_add<true>(ex_h, carry_add<true>(s_fh[warp], ff{lh.x, lh.y}));
+            rl0 = carry_add<true>(ex_l, carry_add<true>(s_fl[warp], ff{ll.x, ll.y}));
         } else {
             rh32 = __fadd_rn(s_wh[warp], lh.x);
             rl32 = __fadd_rn(s_wl[warp], ll.x);
@@ -628,9 +632,8 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
                         slot = hc++;
                         if constexpr (FFOUT) {
                             rh = ff_add_f(rh, xv);
-                            const ff v = carry_add<true>(ex_h, rh);
-                            hi = v.hi;
-                            lo_keep[4 * j + c] = v.lo;
+                            hi = rh.hi;
+                            lo_keep[4 * j + c] = rh.lo;
                         } else {
                             rh32 = __fadd_rn(rh32, xv);
                             hi = carry_apply<COMP>(ex_h, rh32);
@@ -639,9 +642,8 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
                         slot = kTileItems - 1u - (local - hc);
                         if constexpr (FFOUT) {
                             rl = ff_add_f(rl, xv);
-                            const ff v = carry_add<true>(ex_l, rl);
-                            hi = v.hi;
-                            lo_keep[4 * j + c] = v.lo;
+                            hi = rl.hi;
+                            lo_keep[4 * j + c] = rl.lo;
                         } else {
                             rl32 = __fadd_rn(rl32, xv);
                             hi = carry_apply<COMP>(ex_l, rl32);
