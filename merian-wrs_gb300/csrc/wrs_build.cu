@@ -1304,7 +1304,14 @@ __device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ ta
                      const LaterSplits* later) {
     uint32_t i = i0, j = j0;
     float wv = spill;
-    if (wv == 0.0f) wv = __uint_as_float(heavy_item(c, win, j).y);
+    // h: the original index of heavy item j, the current heavy; a heavy step moves it to
+    // item j + 1, whose index that step has just read
+    uint32_t h = 0;
+    if (wv == 0.0f || i < i1 || j < j1) {
+        const uint2 first = heavy_item(c, win, j);
+        h = first.x;
+        if (wv == 0.0f) wv = __uint_as_float(first.y);
+    }
     while (i < i1 || j < j1) {
         bool heavy_step;
         if (j == j1 || j == c.hc)
@@ -1313,7 +1320,6 @@ __device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ ta
             heavy_step = true;
         else
             heavy_step = wv <= c.mean;
-        const uint32_t h = heavy_item(c, win, j).x;
         const uint2 it = heavy_step ? heavy_item(c, win, j + 1u) : light_item(c, win, i);
         const uint32_t widx = it.x;
         const float weight = __uint_as_float(it.y);
@@ -1326,6 +1332,7 @@ __device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ ta
             tidx = h;
             if (later) owned = !covered_later(*later, j, false);
             ++j;
+            h = widx;
         } else {
             p = __fdiv_rn(weight, c.mean);
             al = h;
