@@ -1849,7 +1849,9 @@ cudaError_t launch_pack_records(cudaStream_t st, const float* w, const uint32_t*
 // the subproblem's heavy and light items 32 at a time (coalesced; without partition elements
 // the 32 weight gathers are in flight together), the walk runs in lockstep with every item
 // fetched from its lane by a shuffle, and each lane keeps one table entry of every 32 steps,
-// written together.  Decisions and arithmetic are the scalar pack's operation for operation,
+// written together (the serial loop carries only the residual and the decisions; each lane
+// divides its entry's numerator by the mean when the group is written, so the warp issues
+// one division per 32 steps).  Decisions and arithmetic are the scalar pack's operation for operation,
 // so the table is bit-identical to launch_pack_records'.  (The reference's subgroup shader
 // updates the residual as w + (weight - mean) and keeps a zero spill; here one arithmetic
 // serves both strategies.)  Ownership: a later subproblem within kWarpLook overrides, as in
@@ -1949,9 +1951,14 @@ __global__ __launch_bounds__(256) void k_pack_records_warp(SplitArgs a) {
     uint32_t i = i0, j = j0;
     float wv = spill;
     if (wv == 0.0f) wv = __shfl_sync(0xffffffffu, hw, 0);  // elem(j0): lane 0 of the heavy chunk
-    // pending entries: lane e holds step e of the current group of 32
+    // the current heavy item's original index (lane 0 of the heavy chunk); a heavy step moves
+    // it to item j + 1, whose index that step fetches
+    uint32_t h = __shfl_sync(0xffffffffu, hidx, 0);
+    // pending entries: lane e holds step e of the current group of 32 -- the numerator of its
+    // p (divided by the mean when the group is written, one division per lane), its alias,
+    // its table index and its partition position
     uint32_t e_out = 0u, e_a = 0u, e_pos = 0u;
-    float e_p = 0.0f;
+    float e_num = 0.0f;
     bool e_light = false;
     uint32_t pend = 0;
     while (i < i1 || j < j1) {
@@ -1966,7 +1973,6 @@ __global__ __launch_bounds__(256) void k_pack_records_warp(SplitArgs a) {
             hb = j;
             load_heavy();
         }
-        const uint32_t h = __shfl_sync(0xffffffffu, hidx, j - hb);
         uint32_t widx;
         float weight;
         if (heavy_step) {
@@ -1981,35 +1987,31 @@ __global__ __launch_bounds__(256) void k_pack_records_warp(SplitArgs a) {
             weight = __shfl_sync(0xffffffffu, lw, i - lb);
         }
         if (lane == pend) {
-            if (heavy_step) {
-                e_p = __fdiv_rn(wv, mean);
-                e_a = widx;
-                e_out = h;
-                e_pos = j;
-                e_light = false;
-            } else {
-                e_p = __fdiv_rn(weight, mean);
-                e_a = h;
-                e_out = widx;
-                e_pos = i;
-                e_light = true;
-            }
+            e_num = heavy_step ? wv : weight;
+            e_a = heavy_step ? widx : h;
+            e_out = heavy_step ? h : widx;
+            e_pos = heavy_step ? j : i;
+            e_light = !heavy_step;
         }
-        if (heavy_step)
+        if (heavy_step) {
             ++j;
-        else
+            h = widx;
+        } else {
             ++i;
+        }
         wv = __fsub_rn(__fadd_rn(wv, weight), mean);
         if (++pend == 32u) {
             // whole warp: the shuffles of the ownership test need every lane
             const bool owned = clean || !covered_later_warp(li, lj, count, e_pos, e_light);
-            if (owned && e_out < n) table[e_out] = make_uint2(__float_as_uint(e_p), e_a);
+            if (owned && e_out < n)
+                table[e_out] = make_uint2(__float_as_uint(__fdiv_rn(e_num, mean)), e_a);
             pend = 0;
         }
     }
     // the last, partial group
     const bool owned = clean || !covered_later_warp(li, lj, count, e_pos, e_light);
-    if (lane < pend && owned && e_out < n) table[e_out] = make_uint2(__float_as_uint(e_p), e_a);
+    if (lane < pend && owned && e_out < n)
+        table[e_out] = make_uint2(__float_as_uint(__fdiv_rn(e_num, mean)), e_a);
 }
 
 cudaError_t launch_pack_records_warp(cudaStream_t st, const float* w, const uint32_t* idx,
