@@ -63,3 +63,28 @@ def test_max_size_build_and_sample(pkg, cuda, method):
     p = w.double() / st["total"]
     ideal = math.sqrt(float((p * (1.0 - p)).sum()) / (S * N))
     assert abs(st["rmse"] / ideal - 1.0) < 0.02, (st["rmse"], ideal)
+
+
+@pytest.mark.parametrize("rng", ["reference", "philox"])
+def test_max_size_its_fp32_stored_tree(pkg, cuda, rng):
+    """FP32 ITS at N = 2^30 + 7: the build stores 5 block levels of the bisection's probe tree
+    (tree levels 12 .. 26, 613 MB); 2^27 samples through the buffers equal those of the
+    primitive that probes the CMF alone (same probe sequence), all in range."""
+    import torch
+    W = pkg.wrs
+    cfg = pkg.ITSConfig(rng=W.RNG_PHILOX4X32_10 if rng == "philox" else W.RNG_REFERENCE)
+    w = _weights(13)
+    S = 1 << 27
+    samples = torch.empty(S, dtype=torch.int32, device="cuda")
+    wrs = W.WRS(cfg)
+    internals = W.Internals(wrs.handle, N)
+    bufs = W.WRSBuffers(w, samples, internals)
+    wrs.build(None, bufs, N)
+    wrs.sample(None, bufs, N, S, seed=99, offset=1 << 33)
+    plain = torch.empty_like(samples)
+    wrs.its_sample(None, internals.views()["cmf"], N, S, 99, 1 << 33, plain)
+    torch.cuda.synchronize()
+    assert internals.status() == 0
+    assert torch.equal(samples, plain)
+    assert int(samples.min()) >= 0
+    assert int(samples.max()) < N
