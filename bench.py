@@ -34,6 +34,7 @@ import argparse
 import dataclasses
 import importlib
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -1052,6 +1053,17 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
     rec("its_build", timed(lambda: its.build(stream, its_bufs, n)), 8 * n, n, "weights")
     rec("its_sample_cells", timed(lambda: its.sample(stream, its_bufs, n, s, seed=99)), 4 * s,
         s, "samples")
+    # the ITS sector model: the 4-byte output plus one 32-byte sector per bisection level
+    # whose probes fall outside L2, ceil(log2(4 N / L2 bytes)) levels; the cell-block search
+    # reads one random 32-byte block instead
+    l2 = getattr(torch.cuda.get_device_properties(w.device), "L2_cache_size", 126 << 20)
+    outside = max(0, math.ceil(math.log2(4 * n / l2)))
+    for name, b in (("its_sample", 4 + 32 * outside),
+                    ("its_sample_stored_levels", 4 + 32 * outside),
+                    ("its_sample_cells", 4 + 32)):
+        sec = out[name]["ms"] / 1e3
+        out[name]["sector_model"] = {"bytes_per_sample": b, "levels_outside_l2": outside,
+                                     "GB/s": b * s / sec / 1e9, "frac": b * s / sec / 1e9 / peak}
     # guiding-table granularity of the guided search: build (scan + table) and sampling time
     sweep = {}
     for entry in (2, 3, 4, 6, 8):
