@@ -4,7 +4,8 @@
 //   k_prefix_partition  fused heavy/light stable partition + heavy and light inclusive
 //                       prefix sums + heavyCount, single pass with decoupled lookback
 //                                                          (src/device/prefix_partition/decoupled/shader.comp)
-//   k_scan              inclusive FP32 scan, single pass    (src/device/prefix_sum/decoupled/shader.comp)
+//   k_scan_bulk         inclusive FP32 scan, single pass, tiles brought in by bulk copies
+//                                                          (src/device/prefix_sum/decoupled/shader.comp)
 //   k_scan_exact        the compensated form: exact fixed-point carries, correctly rounded
 //                       outputs (after k_total_mass, which sets the grid)
 //   k_split_pack        PSA split search + pack, one thread per split
@@ -767,28 +768,82 @@ __device__ ff scan_lookback(const ScanState* st, uint32_t tile, uint32_t* status
         [](ff a, ff b) { return carry_add<COMP>(a, b); });
 }
 
-template <bool COMP>
-__global__ __launch_bounds__(kTileThreads) void k_scan(const float* __restrict__ in, uint32_t n,
-                                                       float* __restrict__ out,
-                                                       BuildCtrl* __restrict__ ctrl,
-                                                       ScanState* __restrict__ states,
-                                                       uint32_t cap_tiles, uint32_t spin_limit) {
+// The FP32-carry scan with its tile brought in by one bulk copy.  Thread 0 takes the tile's
+// ticket and at once issues a cp.async.bulk (the TMA unit) of the whole tile, kScanBulkV * 4 KB,
+// into shared memory, completing on an mbarrier; the threads then read it from there.  With
+// no registers held by loads in flight, a CTA covers kScanBulkV * 1024 items and more CTAs fit
+// on an SM than with register tiles, so more of HBM's latency is covered while tiles wait in
+// the lookback.  Per tile: each thread sums its float4s, warp scans give lane and warp offsets,
+// warp 0 publishes the tile aggregate and runs the lookback, and every element is the FP32
+// carry plus its running sum (thread (warp w, lane l) holds the items w*V*128 + v*128 + 4l + c,
+// v < V, c < 4).  A tile that is not whole, or an input
+// that is not 16-byte aligned, is read with plain loads.  The scan states are indexed by these
+// tiles (fewer than the 4096-item tiles the state buffer is sized for).
+template <bool COMP, int V>
+__global__ __launch_bounds__(kTileThreads) void k_scan_bulk(const float* __restrict__ in,
+                                                            uint32_t n, float* __restrict__ out,
+                                                            BuildCtrl* __restrict__ ctrl,
+                                                            ScanState* __restrict__ states,
+                                                            uint32_t cap_tiles,
+                                                            uint32_t spin_limit) {
+    constexpr uint32_t kItems = kTileThreads * 4u * V;  // per tile
+    constexpr uint32_t kWarpSpan = 128u * V;             // per warp
+    extern __shared__ __align__(128) float s_tile[];     // kItems floats
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ uint32_t s_tile_id, s_epoch;
     __shared__ float s_w[kTileWarps];
     __shared__ ff s_ex;
-    ScanState* cur;
-    const uint32_t tile = lookback_begin(&ctrl->scan, states, cap_tiles, cur);
+    LbCtrl* lb = &ctrl->scan;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t tbase = tile * kTileItems;
-    const uint32_t wbase = tbase + warp * kWarpItems;
-    const bool full = (static_cast<uint64_t>(tbase) + kTileItems <= n) &&
-                      ((reinterpret_cast<uintptr_t>(in) & 15u) == 0) &&
-                      ((reinterpret_cast<uintptr_t>(out) & 15u) == 0);
-    float x[4][4];
-    load_tile(in, n, tile, x);
-    float lex[4], voff[4], run = 0.f;
+    const bool aligned_in = (reinterpret_cast<uintptr_t>(in) & 15u) == 0;
+    if (threadIdx.x == 0) {
+        const uint32_t t = atomicAdd(&lb->ticket, 1u);
+        s_tile_id = t;
+        s_epoch = ld_relaxed_u32(&lb->epoch);
+        if (aligned_in && static_cast<uint64_t>(t) * kItems + kItems <= n) {
+            mbar_init(&s_bar, 1u);
+            mbar_init_fence();
+            mbar_arrive_expect_tx(&s_bar, kItems * 4u);
+            bulk_load_smem(s_tile, in + static_cast<size_t>(t) * kItems, kItems * 4u, &s_bar);
+        }
+    }
+    __syncthreads();
+    const uint32_t tile = s_tile_id, epoch = s_epoch;
+    ScanState* cur = states + static_cast<size_t>(epoch & 1u) * cap_tiles;
+    {
+        // the other half of the states is the next launch's: clear this launch's share
+        ScanState* other = states + static_cast<size_t>((epoch + 1u) & 1u) * cap_tiles;
+        constexpr int kWords = sizeof(ScanState) / 16;
+        for (uint32_t t = tile; t < cap_tiles; t += gridDim.x)
+            if (threadIdx.x < kWords)
+                reinterpret_cast<ulonglong2*>(other + t)[threadIdx.x] = make_ulonglong2(0ull, 0ull);
+    }
+    const uint64_t tbase = static_cast<uint64_t>(tile) * kItems;
+    const bool whole = aligned_in && tbase + kItems <= n;
+    bool landed = true;
+    if (whole) {
+        landed = mbar_wait_bounded(&s_bar, 0u, spin_limit);
+    } else {
+        for (uint32_t e = threadIdx.x; e < kItems; e += kTileThreads)
+            s_tile[e] = tbase + e < n ? __ldg(in + tbase + e) : 0.0f;
+    }
+    if (__syncthreads_or(!landed)) {
+        // the copy did not land in time: report it, wait (bounded) once more for it to end
+        // before the CTA's shared memory goes, and leave the tile unpublished (its
+        // successors' lookbacks give up in turn)
+        if (threadIdx.x == 0) {
+            atomicOr(&ctrl->status, kStatusTimeout);
+            mbar_wait_bounded(&s_bar, 0u, spin_limit);
+        }
+        lookback_end(lb);
+        return;
+    }
+    const float4* q = reinterpret_cast<const float4*>(s_tile + warp * kWarpSpan);
+    float lex[V], voff[V], run = 0.f;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-        float t = __fadd_rn(__fadd_rn(__fadd_rn(x[v][0], x[v][1]), x[v][2]), x[v][3]);
+    for (int v = 0; v < V; ++v) {
+        const float4 e4 = q[v * 32 + lane];
+        float t = __fadd_rn(__fadd_rn(__fadd_rn(e4.x, e4.y), e4.z), e4.w);
         float inc = warp_incl_f(t, lane);
         float e = __shfl_up_sync(0xffffffffu, inc, 1);
         lex[v] = lane ? e : 0.f;
@@ -805,29 +860,33 @@ __global__ __launch_bounds__(kTileThreads) void k_scan(const float* __restrict__
         __syncwarp();
         if (lane < kTileWarps) s_w[lane] = lane ? e : 0.f;
         ff ex{0.f, 0.f};
-        unsigned long long* q = reinterpret_cast<unsigned long long*>(cur + tile);
+        unsigned long long* st = reinterpret_cast<unsigned long long*>(cur + tile);
         if (tile == 0) {
-            if (lane == 0) st_relaxed_v2(q, pack_ff(agg), pack_ff(agg));
+            if (lane == 0) st_relaxed_v2(st, pack_ff(agg), pack_ff(agg));
         } else {
-            if (lane == 0) st_relaxed(q, pack_ff(agg));
+            if (lane == 0) st_relaxed(st, pack_ff(agg));
             ex = scan_lookback<COMP>(cur, tile, &ctrl->status, spin_limit);
-            if (lane == 0) st_relaxed(q + 1, pack_ff(carry_add<COMP>(ex, agg)));
+            if (lane == 0) st_relaxed(st + 1, pack_ff(carry_add<COMP>(ex, agg)));
         }
         if (lane == 0) s_ex = ex;
     }
     __syncthreads();
     const ff ex = s_ex;
     const float wex = s_w[warp];
+    const uint64_t wbase = tbase + warp * kWarpSpan;
+    const bool full = whole && (reinterpret_cast<uintptr_t>(out) & 15u) == 0;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
+    for (int v = 0; v < V; ++v) {
+        const float4 e4 = q[v * 32 + lane];
+        const float xv[4] = {e4.x, e4.y, e4.z, e4.w};
         float r = __fadd_rn(__fadd_rn(wex, voff[v]), lex[v]);
         float y[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-            r = __fadd_rn(r, x[v][c]);
+            r = __fadd_rn(r, xv[c]);
             y[c] = carry_apply<COMP>(ex, r);
         }
-        const uint32_t e0 = wbase + v * 128 + lane * 4;
+        const uint64_t e0 = wbase + v * 128 + lane * 4;
         if (full) {
             __stcs(reinterpret_cast<float4*>(out + e0), make_float4(y[0], y[1], y[2], y[3]));
         } else {
@@ -836,8 +895,9 @@ __global__ __launch_bounds__(kTileThreads) void k_scan(const float* __restrict__
                 if (e0 + c < n) out[e0 + c] = y[c];
         }
     }
-    lookback_end(&ctrl->scan);
+    lookback_end(lb);
 }
+constexpr int kScanBulkV = 8;  // 8192 items (32 KB) per tile
 
 // Compensated scan with exact carries (the ITS / Cutpoint CMF).  Thread t of warp w holds the
 // 16 consecutive items [w*512 + 16t, +16) (re-read from the parked tile) and runs an FP32
@@ -993,7 +1053,10 @@ cudaError_t launch_scan(cudaStream_t st, bool comp, const float* in, uint32_t n,
         if (e != cudaSuccess) return e;
         k_scan_exact<<<tiles, kTileThreads, 0, st>>>(in, n, out, ctrl, states, cap_tiles, spin_limit);
     } else {
-        k_scan<false><<<tiles, kTileThreads, 0, st>>>(in, n, out, ctrl, states, cap_tiles, spin_limit);
+        constexpr uint32_t items = kTileThreads * 4u * kScanBulkV;
+        const uint32_t bulk_tiles = static_cast<uint32_t>((static_cast<uint64_t>(n) + items - 1) / items);
+        k_scan_bulk<false, kScanBulkV><<<bulk_tiles, kTileThreads, items * sizeof(float), st>>>(
+            in, n, out, ctrl, states, cap_tiles, spin_limit);
     }
     return cudaGetLastError();
 }

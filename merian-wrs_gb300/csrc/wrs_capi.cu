@@ -5,10 +5,11 @@
 // caller-owned weights and samples) in a single device allocation.  Launch sequences:
 //   alias build : k_total_mass -> k_prefix_partition -> k_split_pack
 //                 (PSA::run, src/device/wrs/alias/psa/PSA.hpp:170-237)
-//   ITS build   : k_scan (ITS::build, src/device/wrs/its/ITS.hpp:90-108), then in the
-//                 compensated precisions k_its_cells (the cell blocks k_its_sample_cells reads),
-//                 otherwise k_its_tree (the bisection's probe-tree block levels)
-//   Cutpoint    : k_scan -> k_cutpoint_guide, or k_guide_monotone on the compensated CMF
+//   ITS build   : k_scan_bulk, or k_total_mass -> k_scan_exact in the compensated precisions
+//                 (ITS::build, src/device/wrs/its/ITS.hpp:90-108), then in the compensated
+//                 precisions k_its_cells (the cell blocks k_its_sample_cells reads), otherwise
+//                 k_its_tree (the bisection's probe-tree block levels)
+//   Cutpoint    : the same scan -> k_cutpoint_guide, or k_guide_monotone on the compensated CMF
 //                 (Cutpoint::build, src/device/wrs/cutpoint/Cutpoint.hpp:108-138)
 //   sample      : k_alias_sample | k_its_sample (k_its_sample_cells) | k_cutpoint_sample
 //                 (WRS::sample, src/device/wrs/WRS.hpp:145-168)
