@@ -1594,13 +1594,11 @@ static void launch_split_kernel(cudaStream_t st, uint32_t grid, const SplitArgs&
         k_split_pack<R64, FF, BATCH, RECORDS><<<grid, kSplitThreads, 0, st>>>(a, bv);
         return;
     }
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_split_pack<R64, FF, BATCH, RECORDS>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(kPackWinBytes));
-        attr = true;
-    }
+    // the attribute belongs to the current device's context: set it for every launch (a
+    // host-side call; a failure shows as the launch's error)
+    cudaFuncSetAttribute(k_split_pack<R64, FF, BATCH, RECORDS>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(kPackWinBytes));
     k_split_pack<R64, FF, BATCH, RECORDS><<<grid, kSplitThreads, kPackWinBytes, st>>>(a, bv);
 }
 
