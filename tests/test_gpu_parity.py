@@ -261,6 +261,27 @@ def test_scan_precision(pkg, cuda, oracle, N, comp):
     assert err.max() <= (1e-6 if comp else 1e-4), err.max()
 
 
+@pytest.mark.parametrize("N", [8191, 8192, 8193, 3 * 8192 + 5])
+@pytest.mark.parametrize("comp", [False, True])
+@pytest.mark.parametrize("shift_in,shift_out", [(0, 0), (1, 0), (0, 1), (3, 2)])
+def test_scan_tiles_and_unaligned_views(pkg, cuda, oracle, N, comp, shift_in, shift_out):
+    """The scan primitive around its tile size (8192 weights per bulk-copied tile in FP32
+    mode) and on views whose pointers are not 16-byte aligned (input read with plain loads,
+    output written element by element): within the precision's bound of the FP64 prefix."""
+    W = pkg.wrs
+    w = weights_lognormal(N + shift_in, N)
+    wrs = W.WRS(pkg.ITSConfig(scan_precision=1 if comp else 0))
+    internals = W.Internals(wrs.handle, N)
+    dw = h2d(w)
+    out = empty(N + shift_out)
+    wrs.prefix_sum(None, dw[shift_in:], N, out[shift_out:], internals)
+    assert internals.status() == 0
+    got = t2h(out, np.float32)[shift_out:].astype(np.float64)
+    ref = oracle.prefix_f64(w[shift_in:])
+    err = np.abs(got - ref) / np.maximum(ref, 1e-30)
+    assert err.max() <= (1e-6 if comp else 1e-4), err.max()
+
+
 @pytest.mark.parametrize("N", [4097, (1 << 22) + 5])
 def test_compensated_cmf_is_exactly_monotone(pkg, cuda, oracle, N):
     """The compensated CMF is non-decreasing, equal across every zero weight (also at thread
