@@ -21,6 +21,7 @@
 #include <list>
 #include <map>
 #include <new>
+#include <set>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -38,49 +39,63 @@ double now_s() {
 
 constexpr uint64_t kArenaUnit = 256;
 
-// First-fit allocator over [0, size) with coalescing of free neighbours.
+// Best-fit allocator over [0, size) with coalescing of free neighbours.  The free blocks are
+// indexed twice -- by offset (to merge a released block with its neighbours) and by (size,
+// offset) (the smallest block that fits, the lowest such offset first) -- so an allocation, a
+// release and each retry of the eviction loop cost O(log free blocks), however many tables are
+// resident.
 class Arena {
   public:
     void reset(uint64_t size) {
-        free_.clear();
-        if (size) free_[0] = size;
+        by_off_.clear();
+        by_size_.clear();
+        if (size) insert(0, size);
         used_ = 0;
     }
     bool alloc(uint64_t bytes, uint64_t& off) {
         bytes = (bytes + kArenaUnit - 1) / kArenaUnit * kArenaUnit;
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second >= bytes) {
-                off = it->first;
-                const uint64_t rest = it->second - bytes;
-                free_.erase(it);
-                if (rest) free_[off + bytes] = rest;
-                used_ += bytes;
-                return true;
-            }
-        }
-        return false;
+        const auto it = by_size_.lower_bound({bytes, 0});
+        if (it == by_size_.end()) return false;
+        const uint64_t size = it->first;
+        off = it->second;
+        erase(off, size);
+        if (size > bytes) insert(off + bytes, size - bytes);
+        used_ += bytes;
+        return true;
     }
     void release(uint64_t off, uint64_t bytes) {
         bytes = (bytes + kArenaUnit - 1) / kArenaUnit * kArenaUnit;
         used_ -= bytes;
-        auto next = free_.lower_bound(off);
-        if (next != free_.end() && off + bytes == next->first) {
+        auto next = by_off_.lower_bound(off);
+        if (next != by_off_.end() && off + bytes == next->first) {
             bytes += next->second;
-            next = free_.erase(next);
+            by_size_.erase({next->second, next->first});
+            next = by_off_.erase(next);
         }
-        if (next != free_.begin()) {
-            auto prev = std::prev(next);
+        if (next != by_off_.begin()) {
+            const auto prev = std::prev(next);
             if (prev->first + prev->second == off) {
-                prev->second += bytes;
-                return;
+                off = prev->first;
+                bytes += prev->second;
+                by_size_.erase({prev->second, prev->first});
+                by_off_.erase(prev);
             }
         }
-        free_[off] = bytes;
+        insert(off, bytes);
     }
     uint64_t used() const { return used_; }
 
   private:
-    std::map<uint64_t, uint64_t> free_;
+    void insert(uint64_t off, uint64_t size) {
+        by_off_[off] = size;
+        by_size_.insert({size, off});
+    }
+    void erase(uint64_t off, uint64_t size) {
+        by_off_.erase(off);
+        by_size_.erase({size, off});
+    }
+    std::map<uint64_t, uint64_t> by_off_;                 // offset -> size
+    std::set<std::pair<uint64_t, uint64_t>> by_size_;     // (size, offset)
     uint64_t used_ = 0;
 };
 
