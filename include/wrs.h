@@ -290,6 +290,12 @@ wrs_status wrs_prefix_sum_noalloc(void* stream, const float* in, uint32_t n, flo
 wrs_status wrs_test_prefix_sum_stalled(const wrs_handle* h, void* stream, const float* in,
                                        uint32_t n, float* out, wrs_buffers* b,
                                        uint32_t spin_limit);
+/* Test hook for the server's table arena (host only, no device work): `iterations` random
+ * allocations and releases of up to 4 MiB in a 1 GiB arena, checked against a shadow map
+ * (no two live blocks overlap, the used byte count matches, everything released coalesces
+ * back into one block).  Returns 0 when every check held, else the number of the first
+ * check that failed. */
+int wrs_test_arena(uint64_t seed, uint32_t iterations);
 /* Host helper: upload the FP32 mean, the FP64 mean (total / N, used by the float-float
  * mode's split targets) and the heavy count into b, for driving wrs_split_pack directly. */
 wrs_status wrs_buffers_set_partition_info(wrs_buffers* b, void* stream, float mean,

@@ -21,6 +21,7 @@
 #include <list>
 #include <map>
 #include <new>
+#include <random>
 #include <set>
 #include <string>
 #include <thread>
@@ -496,3 +497,37 @@ wrs_status wrs_server_run_trace(wrs_server* s, const wrs_request* reqs, const do
 }
 
 }  // extern "C"
+
+int wrs_test_arena(uint64_t seed, uint32_t iterations) {
+    constexpr uint64_t kSize = 1ull << 30;
+    Arena ar;
+    ar.reset(kSize);
+    std::mt19937_64 rng(seed);
+    std::map<uint64_t, uint64_t> live;  // offset -> rounded bytes
+    uint64_t used = 0;
+    for (uint32_t it = 0; it < iterations; ++it) {
+        if (live.empty() || rng() % 3u) {
+            const uint64_t bytes = 1u + rng() % (4ull << 20);
+            uint64_t off = 0;
+            if (!ar.alloc(bytes, off)) continue;
+            const uint64_t rb = (bytes + kArenaUnit - 1) / kArenaUnit * kArenaUnit;
+            if (off % kArenaUnit || off + rb > kSize) return 1;
+            const auto nx = live.lower_bound(off);
+            if (nx != live.end() && nx->first < off + rb) return 2;
+            if (nx != live.begin() && std::prev(nx)->first + std::prev(nx)->second > off) return 3;
+            live[off] = rb;
+            used += rb;
+        } else {
+            auto victim = live.begin();
+            std::advance(victim, static_cast<long>(rng() % live.size()));
+            ar.release(victim->first, victim->second);
+            used -= victim->second;
+            live.erase(victim);
+        }
+        if (ar.used() != used) return 4;
+    }
+    for (const auto& kv : live) ar.release(kv.first, kv.second);
+    uint64_t off = 1;
+    if (!ar.alloc(kSize, off) || off != 0) return 5;
+    return 0;
+}

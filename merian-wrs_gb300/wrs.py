@@ -144,6 +144,7 @@ def lib() -> C.CDLL:
             "wrs_buffers_set_partition_info": (i32, [vp, vp, f32, C.c_double, u32]),
             "wrs_buffers_mean64": (vp, [vp]),
             "wrs_test_prefix_sum_stalled": (i32, [vp, vp, vp, u32, vp, vp, u32]),
+            "wrs_test_arena": (i32, [u64, u32]),
             "wrs_prefix_sum_noalloc": (i32, [vp, vp, u32, vp, u32, vp]),
             "wrs_batch_bytes": (sz, [vp, u32, u64, u64]),
             "wrs_batch_create": (i32, [vp, u32, u64, u64, C.POINTER(vp)]),

@@ -146,6 +146,15 @@ def test_server_argument_checks_on_host(pkg):
     assert L.wrs_server_pending(None) == 0
 
 
+def test_server_table_arena(pkg):
+    """The server's table arena (best fit over free blocks indexed by offset and by size):
+    random allocations and releases never overlap, the byte count matches, and everything
+    released coalesces back into one block -- host code, no device."""
+    L = pkg.wrs.lib()
+    for seed in (1, 2, 3):
+        assert L.wrs_test_arena(seed, 100000) == 0
+
+
 def test_served_workload_shape(pkg):
     """The served request stream: Poisson arrivals at the stated rate, N and S in range,
     about 30% of requests reuse an earlier table id, and a reused id keeps its n and its
