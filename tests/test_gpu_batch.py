@@ -88,6 +88,7 @@ def test_batch_matches_per_call(pkg, cuda, name):
     h = W.Handle(cfg)
     batch = W.Batch(h, 64, sum(SIZES), sum(counts))
     batch.set(None, case.descs())
+    assert batch.count() == len(SIZES)
     batch.build(None)
     batch.sample(None)
     assert batch.status() == 0
@@ -144,6 +145,7 @@ def test_batch_sample_only_and_build_only(pkg, cuda):
     descs[0] = (None, case.tables[0], case.out[0], sizes[0], counts[0], 99)
     descs[1] = (case.dw[1], case.tables[1], None, sizes[1], 0, 12)
     batch.set(None, descs[:2])
+    assert batch.count() == 2
     batch.build(None)
     batch.sample(None)
     assert batch.status() == 0
