@@ -1059,14 +1059,23 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
         8 * n, n, "weights")
     rec("its_sample", timed(lambda: its.its_sample(stream, cmf, n, s, 99, 0, samples)), 4 * s, s,
         "samples")
-    # FP32 ITS through the buffers API: the build also stores the probe tree's levels 12 .. 19
-    # and the bisection reads them from there (the same samples as its_sample on that CMF)
-    its32_bufs = W.WRSBuffers(w, samples, W.Internals(its32.handle, n))
-    rec("its_build_fp32", timed(lambda: its32.build(stream, its32_bufs, n)), 8 * n, n,
+    # FP32 ITS through the buffers API (the same samples as its_sample on that CMF): with cell
+    # size 0 the build stores the probe tree as blocks and the tree sampler reads them; with
+    # the default cell size 4 the build also makes the cells and marks those the FP32 CMF's
+    # decreases can reach, the cell search serves the others and the marked ones bisect
+    tree32 = W.WRS(W.ITSConfig(rng=W.RNG_PHILOX4X32_10, guiding_entry_size=0))
+    bufs32 = W.WRSBuffers(w, samples, W.Internals(tree32.handle, n))
+    rec("its_build_fp32", timed(lambda: tree32.build(stream, bufs32, n)), 8 * n, n,
         "weights")
     rec("its_sample_stored_levels",
-        timed(lambda: its32.sample(stream, its32_bufs, n, s, seed=99)), 4 * s, s, "samples")
-    del its32_bufs
+        timed(lambda: tree32.sample(stream, bufs32, n, s, seed=99)), 4 * s, s, "samples")
+    del bufs32
+    bufs32 = W.WRSBuffers(w, samples, W.Internals(its32.handle, n))
+    rec("its_build_fp32_cells", timed(lambda: its32.build(stream, bufs32, n)), 8 * n, n,
+        "weights")
+    rec("its_sample_fp32_cells", timed(lambda: its32.sample(stream, bufs32, n, s, seed=99)),
+        4 * s, s, "samples")
+    del bufs32
     # through the buffers API: the compensated build also makes the guiding table, and
     # sampling runs the guided search (same samples as the bisection)
     its_bufs = W.WRSBuffers(w, samples, W.Internals(its.handle, n))
@@ -1080,6 +1089,7 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
     outside = max(0, math.ceil(math.log2(4 * n / l2)))
     for name, b in (("its_sample", 4 + 32 * outside),
                     ("its_sample_stored_levels", 4 + 32 * outside),
+                    ("its_sample_fp32_cells", 4 + 32),
                     ("its_sample_cells", 4 + 32)):
         sec = out[name]["ms"] / 1e3
         out[name]["sector_model"] = {"bytes_per_sample": b, "levels_outside_l2": outside,

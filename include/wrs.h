@@ -128,13 +128,15 @@ typedef struct wrs_config {
                                         light bucket extra mass; 0 = reference behaviour */
     uint32_t guiding_entry_size;     /* Cutpoint: CutpointConfig::guidingEntrySize, weights per
                                         guiding-table entry (table size ceil(N / this));
-                                        default 32.  ITS in the compensated precisions with
-                                        coop 0: the CMF is cut into as many equal-mass cells,
-                                        each stored as a 32-byte block (its first index and 7
-                                        CMF values), and each sample reads the block of its
-                                        cell instead of bisecting the whole CMF (indices
-                                        unchanged, the CMF being exactly non-decreasing);
-                                        0 = no cells, every search bisects; default 4 */
+                                        default 32.  ITS with coop 0: the CMF is cut into as
+                                        many equal-mass cells, each stored as a 32-byte block
+                                        (its index range and 6 CMF values), and each sample
+                                        reads the block of its cell instead of bisecting the
+                                        whole CMF, with the same index: the compensated CMF is
+                                        exactly non-decreasing; on an FP32 CMF the build marks
+                                        the cells whose targets can meet a decrease of the CMF,
+                                        and those samples bisect.  Default 4 for ITS; 0 = no
+                                        cells (the bisection through the stored probe tree) */
     uint32_t split_pack_mode;        /* wrs_split_pack_mode: PSAConfig's splitPack alternative;
                                         default WRS_SPLITPACK_INLINE */
 } wrs_config;

@@ -90,8 +90,10 @@ struct Layout {
 // stored block levels below the probe tree's shared-memory ones: the build stores them
 // (k_its_tree)
 bool its_tree_levels(const wrs_config& cfg, uint32_t n) {
-    const bool cells = cfg.guiding_entry_size != 0 && cfg.scan_precision != WRS_SCAN_FP32;
-    return cfg.method == WRS_METHOD_ITS && cfg.coop_size == 0 && !cells &&
+    // the compensated CMF's cells serve every sample; an FP32 CMF's cells send the marked ones
+    // to the bisection through the blocks
+    const bool cells_alone = cfg.guiding_entry_size != 0 && cfg.scan_precision != WRS_SCAN_FP32;
+    return cfg.method == WRS_METHOD_ITS && cfg.coop_size == 0 && !cells_alone &&
            its_tree_block_levels(n) > 0;
 }
 
@@ -126,18 +128,19 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
                         : 0;
     } else {
         L.cmf = take(sizeof(float) * static_cast<size_t>(max_n));
-        // Cutpoint: its guiding table; ITS: the cell blocks that steer sampling on the
-        // compensated (exactly non-decreasing) CMF (none with guiding_entry_size 0)
+        // Cutpoint: its guiding table; ITS: the cell blocks that steer sampling (none with
+        // guiding_entry_size 0) and their construction scratch
         const uint32_t G = cfg.guiding_entry_size ? guide_entries(max_n, cfg.guiding_entry_size) : 0;
-        if (cfg.method == WRS_METHOD_CUTPOINT)
+        const bool its = cfg.method == WRS_METHOD_ITS;
+        if (!its)
             L.guide = take(sizeof(uint32_t) * G);
-        else if (G && cfg.scan_precision != WRS_SCAN_FP32)
+        else if (G)
             L.cells = take(sizeof(ItsCell) * G);
-        if (G && cfg.scan_precision != WRS_SCAN_FP32)
+        if (G && (its || cfg.scan_precision != WRS_SCAN_FP32))
             L.coarse = take(sizeof(uint32_t) * (coarse_entries(G) + group_entries(G)));
         // ITS bisecting the whole CMF (FP32, or no cells): the probe tree's deeper levels
         if (its_tree_levels(cfg, max_n))
-            L.tree = take(sizeof(TreeBlock) * its_tree_blocks(its_tree_block_levels(max_n)));
+            L.tree = take(sizeof(TreeBlock) * its_tree_blocks(its_tree_stored_levels(max_n)));
     }
     L.total = off;
     return L;
@@ -332,7 +335,7 @@ static bool compensated(const wrs_handle* h) {
 // ITS sampling steered by a guiding table: the compensated CMF is exactly non-decreasing, so
 // any lower-bound search returns the bisection's index
 static bool its_guided(const wrs_handle* h) {
-    return h->cfg.method == WRS_METHOD_ITS && compensated(h) && h->cfg.coop_size == 0 &&
+    return h->cfg.method == WRS_METHOD_ITS && h->cfg.coop_size == 0 &&
            h->cfg.guiding_entry_size != 0;
 }
 // the guiding table / cell blocks the handle will use exist in b and have its size
@@ -340,11 +343,11 @@ static wrs_status check_tables(const wrs_handle* h, const wrs_buffers* b) {
     if ((h->cfg.method == WRS_METHOD_CUTPOINT || its_guided(h)) &&
         b->cfg.guiding_entry_size != h->cfg.guiding_entry_size)
         return fail(WRS_ERR_INVALID_ARG, "buffers were created for another guiding_entry_size");
-    if ((its_guided(h) && !b->cells) ||
-        ((h->cfg.method == WRS_METHOD_CUTPOINT || its_guided(h)) && compensated(h) && !b->coarse))
+    if ((its_guided(h) && (!b->cells || !b->coarse)) ||
+        (h->cfg.method == WRS_METHOD_CUTPOINT && compensated(h) && !b->coarse))
         return fail(WRS_ERR_INVALID_ARG,
-                    "buffers were created for the FP32 precision (no cells or construction "
-                    "scratch for the compensated CMF)");
+                    "buffers were created without the cell blocks or the construction scratch "
+                    "this handle's search uses");
     return WRS_OK;
 }
 
@@ -529,11 +532,18 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
             WRS_CUDA(comp ? launch_guide_monotone(st, b->cmf, n, G, b->coarse, b->guide)
                           : launch_cutpoint_guide(st, b->cmf, n, G, b->guide),
                      "guiding table");
-        else if (its_guided(h))
+        else if (its_guided(h)) {
             WRS_CUDA(launch_its_cells(st, b->cmf, n, G, b->coarse, b->cells), "ITS cells");
+            // an FP32 CMF need not be monotone: mark the cells the search cannot serve
+            if (!comp)
+                WRS_CUDA(launch_its_marks(st, b->cmf, n, G, b->cells,
+                                          reinterpret_cast<float*>(b->tile_scratch),
+                                          b->tile_scratch + 2u * b->cap_tiles),
+                         "ITS cell marks");
+        }
         b->tree_n = 0;
         if (b->tree && its_tree_levels(h->cfg, n)) {
-            WRS_CUDA(launch_its_tree(st, b->cmf, n, its_tree_block_levels(n), b->tree),
+            WRS_CUDA(launch_its_tree(st, b->cmf, n, its_tree_stored_levels(n), b->tree),
                      "ITS probe tree");
             b->tree_n = n;
         }
@@ -584,12 +594,15 @@ wrs_status wrs_sample_at(const wrs_handle* h, void* stream, const wrs_buffers* b
     if ((st = check_tables(h, b)) != WRS_OK) return st;
     if (h->cfg.method == WRS_METHOD_ITS) {
         if (its_guided(h) && s) {
-            // the compensated CMF is non-decreasing: the cell-block search returns the
-            // bisection's index (see k_its_sample_cells)
+            // the cell-block search returns the bisection's index: for every target on the
+            // compensated (non-decreasing) CMF, for the unmarked cells' targets on an FP32 one;
+            // the marked cells bisect, through the stored probe tree when the build made it
             if (!samples) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+            const bool tree = !compensated(h) && b->tree && b->tree_n == n;
             WRS_CUDA(launch_its_sample_cells(as_stream(stream), h->cfg.rng, b->cmf, n, b->cells,
                                              guide_entries(n, h->cfg.guiding_entry_size), s,
-                                             seed, offset, samples),
+                                             seed, offset, samples, tree ? b->tree : nullptr,
+                                             tree ? its_tree_stored_levels(n) : 0u),
                      "its sample");
             return WRS_OK;
         }
@@ -597,7 +610,8 @@ wrs_status wrs_sample_at(const wrs_handle* h, void* stream, const wrs_buffers* b
             // the bisection with the probe tree's block levels read from the build's copy
             if (!samples) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
             WRS_CUDA(launch_its_sample(as_stream(stream), h->cfg.rng, 0, false, b->cmf, n, s, seed,
-                                       offset, samples, b->tree, its_tree_block_levels(n)),
+                                       offset, samples, b->tree + kTopBlocks,
+                                       its_tree_block_levels(n)),
                      "its sample");
             return WRS_OK;
         }

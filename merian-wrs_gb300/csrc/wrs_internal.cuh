@@ -162,14 +162,16 @@ cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, co
                                 uint32_t n, uint64_t s, uint64_t seed, uint64_t offset,
                                 uint32_t* out);
 // The non-cooperative ITS sampler's bisection probes one implicit binary tree (node k, root
-// 1: the range left by the decisions spelled by the bits of k below its leading one).  Its
-// top kTreeTop levels sit in each CTA's shared memory; the build can store the next
-// kTreeBlockLevels * B levels as blocks of three levels -- a node and its 6 descendants, 7
-// probe values (slot 7 unused) in one 32-byte sector -- so that one random read resolves
-// three levels.  Block level b holds the blocks rooted at the 2^(kTreeTop + 3b) nodes of tree
-// level kTreeTop + 3b, after the blocks of the levels above it.
+// 1: the range left by the decisions spelled by the bits of k below its leading one).  The
+// build stores the tree's levels as blocks of three levels -- a node and its 6 descendants, 7
+// probe values (slot 7: the node's range start) in one 32-byte sector -- so that one random
+// read resolves three levels.  Block level b holds the 8^b blocks rooted at the nodes of tree
+// level 3b, after the blocks of the levels above it.  The tree sampler keeps the top kTreeTop
+// levels in each CTA's shared memory and reads the B block levels below them; a bisection
+// outside that kernel (the cell search's fallback) reads all B + kTopBlockLevels of them.
 constexpr uint32_t kTreeTop = 12;
 constexpr uint32_t kTreeBlockLevels = 3;
+constexpr uint32_t kTopBlockLevels = kTreeTop / kTreeBlockLevels;  // tree levels 0 .. 11
 struct alignas(32) TreeBlock {
     float v[8];
 };
@@ -180,19 +182,28 @@ __host__ __device__ inline uint32_t its_tree_depth(uint32_t n) {
     while (t < 32u && (1ull << t) < n) ++t;
     return t;
 }
-// block levels stored for n values: after them the bisection's range holds at most 16 values
-// (a 64-byte stretch of the CMF), and the blocks take at most ~2/7 of the CMF's bytes
+// block levels below the shared ones stored for n values (B): after them the bisection's range
+// holds at most 16 values (a 64-byte stretch of the CMF), and all blocks take at most ~2/7 of
+// the CMF's bytes
 __host__ __device__ inline uint32_t its_tree_block_levels(uint32_t n) {
     const uint32_t t = its_tree_depth(n);
     return t >= kTreeTop + 5u ? (t - kTreeTop - 2u) / kTreeBlockLevels : 0u;
 }
-// blocks in the first B block levels
-__host__ __device__ inline size_t its_tree_blocks(uint32_t B) {
+// block levels stored in all (the top ones too), 0 when none below the shared levels
+__host__ __device__ inline uint32_t its_tree_stored_levels(uint32_t n) {
+    const uint32_t B = its_tree_block_levels(n);
+    return B ? B + kTopBlockLevels : 0u;
+}
+// blocks in the first L block levels (from the root)
+__host__ __device__ constexpr size_t its_tree_blocks(uint32_t L) {
     size_t s = 0;
-    for (uint32_t b = 0; b < B; ++b) s += size_t(1) << (kTreeTop + kTreeBlockLevels * b);
+    for (uint32_t b = 0; b < L; ++b) s += size_t(1) << (kTreeBlockLevels * b);
     return s;
 }
-cudaError_t launch_its_tree(cudaStream_t st, const float* cmf, uint32_t n, uint32_t B,
+// blocks of the levels the shared memory holds (1 + 8 + 64 + 512)
+constexpr size_t kTopBlocks = 585;
+// stores the first L block levels (its_tree_stored_levels(n)) of the CMF's probe tree
+cudaError_t launch_its_tree(cudaStream_t st, const float* cmf, uint32_t n, uint32_t L,
                             TreeBlock* blocks);
 cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool parray,
                               const float* cmf, uint32_t n, uint64_t S, uint64_t seed,
@@ -225,7 +236,12 @@ cudaError_t launch_its_cells(cudaStream_t st, const float* cmf, uint32_t n, uint
                              uint32_t* coarse, ItsCell* cells);
 cudaError_t launch_its_sample_cells(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
                                     const ItsCell* cells, uint32_t G, uint64_t S, uint64_t seed,
-                                    uint64_t offset, uint32_t* out);
+                                    uint64_t offset, uint32_t* out,
+                                    const TreeBlock* blocks = nullptr, uint32_t L = 0);
+// FP32 CMF: marks the cells the cell search cannot serve (bit 31 of y), after launch_its_cells;
+// tile_scratch: 2 * tiles_for(n) floats; bad: a device word (set when every cell is marked)
+cudaError_t launch_its_marks(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
+                             ItsCell* cells, float* tile_scratch, uint32_t* bad);
 cudaError_t launch_cutpoint_sample(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
                                    const uint32_t* guide, uint32_t G, uint64_t S, uint64_t seed,
                                    uint64_t offset, uint32_t* out);

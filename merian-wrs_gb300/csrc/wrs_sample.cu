@@ -301,11 +301,12 @@ static_assert(kItsTreeLevels == static_cast<int>(kTreeTop), "shared levels above
 // as x | (len - floor(n / 2^level)) << 31: the ranges of one tree level are floor(n / 2^level)
 // or one more long (the left half of a range takes the odd index), and x < 2^31.
 __global__ __launch_bounds__(kSampleThreads) void k_its_tree(const float* __restrict__ cmf,
-                                                             uint32_t n, uint32_t B,
+                                                             uint32_t n, uint32_t L,
                                                              TreeBlock* __restrict__ blocks) {
+    static_assert(its_tree_blocks(kTopBlockLevels) == kTopBlocks, "top block count");
     const size_t gb = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (gb >= its_tree_blocks(B)) return;
-    uint32_t level = kTreeTop;
+    if (gb >= its_tree_blocks(L)) return;
+    uint32_t level = 0;
     size_t off = 0;
     while (gb >= off + (size_t(1) << level)) {
         off += size_t(1) << level;
@@ -631,6 +632,216 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_cells(const float* __res
                         __float_as_uint(v[5]));
 }
 
+// ---- cells on an FP32 CMF: cells whose targets can meet an inversion ------------------
+//
+// On a CMF that is not monotone every lower-bound search still returns the bisection's index
+// for a target t that lies in no inversion interval (cmf[j], cmf[i]] (i < j, cmf[j] < cmf[i]):
+// then every value below t comes before every value >= t.  For each i the union of its
+// intervals is (S(i + 1), cmf[i]] with S the suffix minimum, so a pass over the CMF marks the
+// cells whose target range meets one (bit 31 of the cell's y; n < 2^31), and the cells whose
+// start x does not have cmf[x - 1] < c_k; a CMF with a value that is not finite or is negative
+// marks every cell.  The cell search serves the unmarked cells and the bisection the others.
+constexpr uint32_t kCellUnsafe = 0x80000000u;
+constexpr uint32_t kMarkSpan = 64;  // an interval over more cells marks the whole CMF unsafe
+
+// the largest k < G with c_k = fl(step * k) < t (0 if none): the cell of targets just above t
+__device__ __forceinline__ uint32_t cell_below(float t, float step, uint32_t G) {
+    uint32_t lo = 0, hi = G - 1u;  // c_0 = 0
+    while (lo < hi) {
+        const uint32_t mid = lo + ((hi - lo + 1u) >> 1);
+        if (__fmul_rn(step, __uint2float_rn(mid)) < t)
+            lo = mid;
+        else
+            hi = mid - 1u;
+    }
+    return lo;
+}
+
+// per 4096-value tile of the CMF: its minimum; any value that is NaN, infinite or negative
+// raises `bad`
+__global__ __launch_bounds__(kSampleThreads) void k_cmf_tile_min(const float* __restrict__ cmf,
+                                                                 uint32_t n,
+                                                                 float* __restrict__ tile_min,
+                                                                 uint32_t* __restrict__ bad) {
+    __shared__ float s_m[kSampleThreads / 32];
+    const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kTileItems;
+    float m = INFINITY;
+    bool b = false;
+    for (uint32_t e = threadIdx.x; e < kTileItems; e += blockDim.x) {
+        if (base + e < n) {
+            const float v = __ldg(cmf + base + e);
+            b = b || !(v >= 0.0f && v <= 3.402823466e38f);
+            m = fminf(m, v);
+        }
+    }
+    if (__syncthreads_or(b) && threadIdx.x == 0) atomicOr(bad, 1u);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, d));
+    if ((threadIdx.x & 31u) == 0) s_m[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < static_cast<int>(kSampleThreads / 32); ++w) m = fminf(m, s_m[w]);
+        tile_min[blockIdx.x] = fminf(m, s_m[0]);
+    }
+}
+
+// suffix minima of the tile minima (one CTA, chunks of 1024 from the end)
+__global__ __launch_bounds__(1024) void k_tile_suffix_min(const float* __restrict__ tile_min,
+                                                          uint32_t tiles,
+                                                          float* __restrict__ suf) {
+    __shared__ float s_w[32];
+    __shared__ float s_carry;
+    if (threadIdx.x == 0) s_carry = INFINITY;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int64_t end = tiles; end > 0; end -= 1024) {
+        // thread j holds tile end - 1 - j (reversed, so an inclusive prefix min is a suffix min)
+        const int64_t t = end - 1 - static_cast<int64_t>(threadIdx.x);
+        float v = t >= 0 ? tile_min[t] : INFINITY;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const float o = __shfl_up_sync(0xffffffffu, v, d);
+            if (lane >= d) v = fminf(v, o);
+        }
+        if (lane == 31) s_w[warp] = v;
+        __syncthreads();
+        if (warp == 0) {
+            float u = s_w[lane];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const float o = __shfl_up_sync(0xffffffffu, u, d);
+                if (lane >= d) u = fminf(u, o);
+            }
+            s_w[lane] = u;  // inclusive over warps 0 .. lane
+        }
+        __syncthreads();
+        const float carry = s_carry;
+        const float r = fminf(fminf(v, warp ? s_w[warp - 1] : INFINITY), carry);
+        if (t >= 0) suf[t] = r;
+        __syncthreads();
+        if (threadIdx.x == 1023) s_carry = r;
+        __syncthreads();
+    }
+}
+
+// marks the cells k in [cell_below(lo+), cell_below(hi)] for the interval (lo, hi]; an interval
+// over more than kMarkSpan cells raises `bad` instead
+__device__ __forceinline__ void mark_interval(float lo, float hi, float step, uint32_t G,
+                                              ItsCell* __restrict__ cells,
+                                              uint32_t* __restrict__ bad) {
+    const uint32_t a = cell_below(__uint_as_float(__float_as_uint(lo) + 1u), step, G);
+    const uint32_t b = cell_below(hi, step, G);
+    if (b >= a && b - a >= kMarkSpan) {
+        atomicOr(bad, 1u);
+        return;
+    }
+    for (uint32_t k = a; k <= b; ++k) atomicOr(&cells[k].y, kCellUnsafe);
+}
+
+// one CTA per 4096-value tile, 16 consecutive values per thread: S(i + 1) from the thread's own
+// later values, the later threads' and the later tiles' minima; every i with S(i + 1) < cmf[i]
+// marks the cells of (S(i + 1), cmf[i]].  Skipped when `bad` is set (every cell is marked then).
+__global__ __launch_bounds__(kSampleThreads) void k_cmf_mark(const float* __restrict__ cmf,
+                                                             uint32_t n, uint32_t G,
+                                                             const float* __restrict__ suf,
+                                                             uint32_t tiles,
+                                                             ItsCell* __restrict__ cells,
+                                                             uint32_t* __restrict__ bad) {
+    __shared__ float s_w[kSampleThreads / 32];
+    // one decision for the whole CTA (other CTAs may raise `bad` meanwhile)
+    if (__syncthreads_or(*reinterpret_cast<volatile uint32_t*>(bad) != 0u)) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kTileItems + threadIdx.x * 16u;
+    float v[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) v[c] = base + c < n ? __ldg(cmf + base + c) : INFINITY;
+    float tmin = v[15];
+#pragma unroll
+    for (int c = 14; c >= 0; --c) tmin = fminf(tmin, v[c]);
+    // minimum over the later threads of the tile (exclusive), then over the later tiles
+    float inc = tmin;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const float o = __shfl_down_sync(0xffffffffu, inc, d);
+        if (lane + d < 32) inc = fminf(inc, o);
+    }
+    if (lane == 0) s_w[warp] = inc;  // warp's minimum
+    __syncthreads();
+    float after = __shfl_down_sync(0xffffffffu, inc, 1);
+    if (lane == 31) after = INFINITY;
+    for (int w = warp + 1; w < static_cast<int>(kSampleThreads / 32); ++w) after = fminf(after, s_w[w]);
+    if (blockIdx.x + 1u < tiles) after = fminf(after, suf[blockIdx.x + 1u]);
+    const float step = __fdiv_rn(__ldg(cmf + n - 1u), __uint2float_rn(G));
+    float s = after;  // S(i + 1) for the thread's last value
+#pragma unroll
+    for (int c = 15; c >= 0; --c) {
+        if (base + c < n && s < v[c]) mark_interval(s, v[c], step, G, cells, bad);
+        s = fminf(s, v[c]);
+    }
+}
+
+// every cell whose start x > 0 does not have cmf[x - 1] < c_k is marked; with `bad` every
+// cell is
+__global__ __launch_bounds__(kSampleThreads) void k_cells_check(const float* __restrict__ cmf,
+                                                                uint32_t n, uint32_t G,
+                                                                ItsCell* __restrict__ cells,
+                                                                const uint32_t* __restrict__ bad) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= G) return;
+    const bool all = *reinterpret_cast<const volatile uint32_t*>(bad) != 0u;
+    const uint32_t x = cells[k].x;
+    bool ok = !all;
+    if (ok && x > 0u) {
+        const float ck = __fmul_rn(__fdiv_rn(__ldg(cmf + n - 1u), __uint2float_rn(G)),
+                                   __uint2float_rn(k));
+        ok = x <= n - 1u && __ldg(cmf + x - 1u) < ck;
+    }
+    if (!ok) atomicOr(&cells[k].y, kCellUnsafe);
+}
+
+// The bisection of [0, n - 1] for target t (a probe c sends it right when t > c) through the
+// stored probe-tree blocks (L = its_tree_stored_levels(n) > 0 levels: the node alone above the
+// last one, whose slot 7 gives the range), then the CMF for the tail: the same probe sequence.
+__device__ uint32_t bisect_blocks(const float* __restrict__ cmf, uint32_t n,
+                                  const TreeBlock* __restrict__ blocks, uint32_t L, float t) {
+    uint32_t node = 1, level = 0, x = 0, y = 0;
+    const TreeBlock* lb = blocks;
+    for (uint32_t bl = 0; bl < L; ++bl, level += kTreeBlockLevels) {
+        const uint32_t first = 1u << level;
+        uint4 lo, hi;
+        ld_u32x8(reinterpret_cast<const uint32_t*>(lb + (node - first)), lo, hi);
+        lb += first;
+        const uint32_t r0 = t > __uint_as_float(lo.x) ? 1u : 0u;
+        const uint32_t c1 = r0 ? lo.z : lo.y;
+        const uint32_t r1 = t > __uint_as_float(c1) ? 1u : 0u;
+        const uint32_t c2 = r0 ? (r1 ? hi.z : hi.y) : (r1 ? hi.x : lo.w);
+        const uint32_t r2 = t > __uint_as_float(c2) ? 1u : 0u;
+        if (bl + 1u < L) {
+            node = 8u * node + 4u * r0 + 2u * r1 + r2;
+        } else {
+            x = hi.w & 0x7fffffffu;
+            y = x + (n >> level) + (hi.w >> 31) - 1u;
+            const uint32_t r[3] = {r0, r1, r2};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const uint32_t mid = x + ((y - x) >> 1);
+                x = r[d] ? mid + 1u : x;
+                y = r[d] ? y : mid;
+            }
+            y = min(y, n - 1u);
+            x = min(x, y);
+        }
+    }
+    while (x < y) {
+        const uint32_t mid = x + ((y - x) >> 1);
+        if (t > __ldg(cmf + mid))
+            x = mid + 1u;
+        else
+            y = mid;
+    }
+    return x;
+}
+
 // steps of the cell correction (beyond them the bracket check sends the sample to the
 // bisection, so the bound only caps the work)
 constexpr int kCellFix = 8;
@@ -638,7 +849,8 @@ constexpr int kCellFix = 8;
 template <uint32_t RNG>
 __global__ __launch_bounds__(kSampleThreads) void k_its_sample_cells(
     const float* __restrict__ cmf, uint32_t n, const ItsCell* __restrict__ cells, uint32_t G,
-    uint64_t S, uint64_t seed, uint64_t offset, uint32_t* __restrict__ out) {
+    uint64_t S, uint64_t seed, uint64_t offset, uint32_t* __restrict__ out,
+    const TreeBlock* __restrict__ blocks, uint32_t L) {
     const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (s >= S) return;
     const uint32_t last = n - 1u;
@@ -670,18 +882,23 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_cells(
     for (int it = 0; it < kCellFix && k + 1u < G && above(__fmul_rn(step, __uint2float_rn(k + 1u)));
          ++it)
         ++k;
-    // c_k < T (then cmf[x_k - 1] < c_k < T); the upper side is checked on the block
-    const bool settled = k == 0u || above(__fmul_rn(step, __uint2float_rn(k)));
+    // c_k < T <= c_{k+1} (then cmf[x_k - 1] < c_k < T, and T is in the range the cell's
+    // inversion mark covers); cmf[y_k] >= T is checked on the block
+    const bool settled = (k == 0u || above(__fmul_rn(step, __uint2float_rn(k)))) &&
+                         (k + 1u >= G || !above(__fmul_rn(step, __uint2float_rn(k + 1u))));
     const uint64_t once = l2_policy_evict_first();
     uint4 q0, q1;
     ld_u32x8_policy(reinterpret_cast<const uint32_t*>(cells + k), once, q0, q1);
-    uint32_t x = q0.x, y = q0.y;
+    // an FP32 CMF's cell may be marked (its targets can meet an inversion, or its start is not
+    // below c_k): bisect those (the compensated CMF's cells are never marked)
+    const bool unsafe = (q0.y & kCellUnsafe) != 0u;
+    uint32_t x = q0.x, y = q0.y & ~kCellUnsafe;
     const float v[kCellParts] = {__uint_as_float(q0.z), __uint_as_float(q0.w),
                                  __uint_as_float(q1.x), __uint_as_float(q1.y),
                                  __uint_as_float(q1.z), __uint_as_float(q1.w)};
     // (y >= x holds for every non-decreasing CMF; the test keeps weights outside the
     // contract -- NaN, negative -- from producing an index outside [0, N))
-    if (settled && y >= x && !above(v[kCellParts - 1])) {
+    if (!unsafe && settled && y >= x && !above(v[kCellParts - 1])) {
         // the first part whose last value is >= T (the values are non-decreasing)
         uint32_t part = 0;
 #pragma unroll
@@ -694,6 +911,12 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_cells(
         }
         y = min(lo + d - 1u, y);  // cmf[y] >= T and cmf[lo - 1] < T
         x = lo;
+    } else if (blocks) {
+        // the bisection through the stored probe tree (t_hi with the tie folded in: T > c
+        // exactly when the next float above t_hi is > c, for t_sgn > 0)
+        const float t = t_sgn > 0 ? __uint_as_float(__float_as_uint(t_hi) + 1u) : t_hi;
+        __stcs(out + s, bisect_blocks(cmf, n, blocks, L, t));
+        return;
     } else {
         x = 0;
         y = last;
@@ -748,18 +971,34 @@ cudaError_t launch_its_cells(cudaStream_t st, const float* cmf, uint32_t n, uint
     return cudaGetLastError();
 }
 
+cudaError_t launch_its_marks(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
+                             ItsCell* cells, float* tile_scratch, uint32_t* bad) {
+    const uint32_t tiles = tiles_for(n);
+    float* tile_min = tile_scratch;
+    float* suf = tile_scratch + tiles;
+    cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    k_cmf_tile_min<<<tiles, kSampleThreads, 0, st>>>(cmf, n, tile_min, bad);
+    k_tile_suffix_min<<<1, 1024, 0, st>>>(tile_min, tiles, suf);
+    k_cmf_mark<<<tiles, kSampleThreads, 0, st>>>(cmf, n, G, suf, tiles, cells, bad);
+    k_cells_check<<<(G + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(cmf, n, G,
+                                                                                      cells, bad);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_its_sample_cells(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
                                     const ItsCell* cells, uint32_t G, uint64_t S, uint64_t seed,
-                                    uint64_t offset, uint32_t* out) {
-    const uint64_t blocks = (S + kSampleThreads - 1) / kSampleThreads;
-    if (blocks == 0) return cudaSuccess;
-    if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
+                                    uint64_t offset, uint32_t* out, const TreeBlock* blocks,
+                                    uint32_t L) {
+    const uint64_t grid = (S + kSampleThreads - 1) / kSampleThreads;
+    if (grid == 0) return cudaSuccess;
+    if (grid > 0x7fffffffull) return cudaErrorInvalidValue;
     if (rng == RNG_REF)
-        k_its_sample_cells<RNG_REF><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
-            cmf, n, cells, G, S, seed, offset, out);
+        k_its_sample_cells<RNG_REF><<<static_cast<unsigned>(grid), kSampleThreads, 0, st>>>(
+            cmf, n, cells, G, S, seed, offset, out, blocks, L);
     else
-        k_its_sample_cells<RNG_PHILOX><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
-            cmf, n, cells, G, S, seed, offset, out);
+        k_its_sample_cells<RNG_PHILOX><<<static_cast<unsigned>(grid), kSampleThreads, 0, st>>>(
+            cmf, n, cells, G, S, seed, offset, out, blocks, L);
     return cudaGetLastError();
 }
 
@@ -875,13 +1114,13 @@ cudaError_t launch_batch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t co
     return cudaGetLastError();
 }
 
-cudaError_t launch_its_tree(cudaStream_t st, const float* cmf, uint32_t n, uint32_t B,
+cudaError_t launch_its_tree(cudaStream_t st, const float* cmf, uint32_t n, uint32_t L,
                             TreeBlock* blocks) {
-    const size_t count = its_tree_blocks(B);
+    const size_t count = its_tree_blocks(L);
     if (count == 0) return cudaSuccess;
     const size_t grid = (count + kSampleThreads - 1) / kSampleThreads;
     if (grid > 0x7fffffffull) return cudaErrorInvalidValue;
-    k_its_tree<<<static_cast<unsigned>(grid), kSampleThreads, 0, st>>>(cmf, n, B, blocks);
+    k_its_tree<<<static_cast<unsigned>(grid), kSampleThreads, 0, st>>>(cmf, n, L, blocks);
     return cudaGetLastError();
 }
 

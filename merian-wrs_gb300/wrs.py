@@ -256,8 +256,9 @@ def AliasTableConfig(split_size: int = 2, use_partition_elements: bool = True,
 def ITSConfig(coop_size: int = 0, parray: bool = False, guiding_entry_size: int = 4,
               **kw) -> WRSConfig:
     """ITSConfig(DecoupledPrefixSumConfig(), InverseTransformSamplingConfig(512, coop, parray)).
-    guiding_entry_size: weights per entry of the table that steers the compensated CMF's
-    searches (0 = none); indices do not depend on it."""
+    guiding_entry_size: weights per cell of the cell blocks that steer the searches (both
+    precisions; on an FP32 CMF the cells its decreases can reach bisect); 0 = none (the
+    bisection through the stored probe tree).  Indices do not depend on it."""
     return WRSConfig(METHOD_ITS, coop_size=coop_size, its_parray=parray,
                      guiding_entry_size=guiding_entry_size, **kw)
 

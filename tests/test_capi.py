@@ -82,15 +82,20 @@ def test_argument_validation_without_device_work(pkg):
     assert L.wrs_cutpoint_guide(h.ptr, None, 8, 16, 8) == 1  # alias handle
     assert L.wrs_cutpoint_sample(cp.ptr, None, 8, 0, 8, 16, 1, 0, 8) == 1  # n == 0
     assert L.wrs_version() == 100
-    # a buffers object needs ~20 B per weight for the alias method, ~4 B for ITS; FP32 ITS
-    # above 2^16 weights adds the stored probe-tree blocks (2^20 weights: tree levels 12 .. 17,
-    # 4096 + 32768 blocks of 32 B)
+    # a buffers object needs ~20 B per weight for the alias method, ~4 B for ITS (the CMF);
+    # ITS with cells adds 32 B per cell (8 B per weight at the default cell size 4), and FP32
+    # ITS above 2^16 weights the stored probe-tree blocks (2^20 weights: tree levels 0 .. 17,
+    # 1 + 8 + 64 + 512 + 4096 + 32768 blocks of 32 B)
     n = 1 << 20
     assert 20 * n <= L.wrs_buffers_bytes(h.ptr, n) <= 21 * n + (1 << 20)
-    hi = w.Handle(w.ITSConfig())
-    tree = 32 * (4096 + 32768)
-    assert 4 * n + tree <= L.wrs_buffers_bytes(hi.ptr, n) <= 5 * n + tree + (1 << 20)
-    assert L.wrs_buffers_bytes(hi.ptr, 1 << 16) <= 5 * (1 << 16) + (1 << 20)
+    tree = 32 * (585 + 4096 + 32768)
+    plain = w.Handle(w.ITSConfig(guiding_entry_size=0))  # FP32, bisection only
+    assert 4 * n + tree <= L.wrs_buffers_bytes(plain.ptr, n) <= 5 * n + tree + (1 << 20)
+    assert L.wrs_buffers_bytes(plain.ptr, 1 << 16) <= 5 * (1 << 16) + (1 << 20)
+    cells = w.Handle(w.ITSConfig())  # FP32, cells of 4 and the tree for marked cells
+    assert 12 * n + tree <= L.wrs_buffers_bytes(cells.ptr, n) <= 13 * n + tree + (1 << 20)
+    comp = w.Handle(w.ITSConfig(scan_precision=w.SCAN_COMPENSATED))  # cells alone
+    assert 12 * n <= L.wrs_buffers_bytes(comp.ptr, n) <= 13 * n + (1 << 20)
 
 
 def test_cpp_facade_compiles(pkg, tmp_path):

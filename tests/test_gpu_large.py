@@ -65,14 +65,17 @@ def test_max_size_build_and_sample(pkg, cuda, method):
     assert abs(st["rmse"] / ideal - 1.0) < 0.02, (st["rmse"], ideal)
 
 
-@pytest.mark.parametrize("rng", ["reference", "philox"])
-def test_max_size_its_fp32_stored_tree(pkg, cuda, rng):
-    """FP32 ITS at N = 2^30 + 7: the build stores 5 block levels of the bisection's probe tree
-    (tree levels 12 .. 26, 613 MB); 2^27 samples through the buffers equal those of the
-    primitive that probes the CMF alone (same probe sequence), all in range."""
+@pytest.mark.parametrize("rng,entry", [("reference", 4), ("philox", 4), ("philox", 0)])
+def test_max_size_its_fp32_stored_tree(pkg, cuda, rng, entry):
+    """FP32 ITS at N = 2^30 + 7: the build stores the bisection's probe tree as blocks (tree
+    levels 0 .. 26, 614 MB); cell size 0 samples with the tree sampler, cell size 4 with the
+    cell search on the unmarked cells and the block bisection on the marked ones.  2^27 samples
+    through the buffers equal those of the primitive that probes the CMF alone (same probe
+    sequence), all in range."""
     import torch
     W = pkg.wrs
-    cfg = pkg.ITSConfig(rng=W.RNG_PHILOX4X32_10 if rng == "philox" else W.RNG_REFERENCE)
+    cfg = pkg.ITSConfig(rng=W.RNG_PHILOX4X32_10 if rng == "philox" else W.RNG_REFERENCE,
+                        guiding_entry_size=entry)
     w = _weights(13)
     S = 1 << 27
     samples = torch.empty(S, dtype=torch.int32, device="cuda")

@@ -357,12 +357,12 @@ def test_its_cells_heavy_heads_and_crowded_cells(pkg, cuda, oracle, gen, entry):
 
 
 def test_its_buffers_must_hold_the_handles_cells(pkg, cuda):
-    """A compensated ITS handle refuses buffers made without cell blocks (an FP32 handle's)
-    or with another guiding-table granularity, instead of reading past them."""
+    """A compensated ITS handle refuses buffers made without cell blocks (an FP32 handle's
+    with cell size 0) or with another cell size, instead of reading past them."""
     W = pkg.wrs
     N = 10000
     w = h2d(weights_uniform(N, 3))
-    fp32 = W.WRS(pkg.ITSConfig(scan_precision=0))
+    fp32 = W.WRS(pkg.ITSConfig(scan_precision=0, guiding_entry_size=0))
     comp8 = W.WRS(pkg.ITSConfig(scan_precision=1, guiding_entry_size=8))
     comp4 = W.WRS(pkg.ITSConfig(scan_precision=1, guiding_entry_size=4))
     b32 = W.WRSBuffers.allocate(N, 16, fp32.config, handle=fp32.handle)
@@ -396,14 +396,17 @@ def test_its_sample_edge_sizes(pkg, cuda, oracle, N, rng):
 
 
 @pytest.mark.parametrize("rng", [RNG_REFERENCE, RNG_PHILOX4X32_10])
-def test_its_stored_tree_blocks(pkg, cuda, oracle, rng):
-    """The FP32 build stores the bisection's probe-tree levels below the shared-memory ones as
-    blocks of three levels: samples through the buffers equal those of the primitive that
-    probes the CMF itself at 2^22 + 3 (3 block levels), 2^19 + 1 (2) and 2^16 + 1 (1), the
-    same buffers rebuilt for each smaller size; the last equals the oracle."""
+@pytest.mark.parametrize("entry", [0, 4])
+def test_its_stored_tree_blocks(pkg, cuda, oracle, rng, entry):
+    """The FP32 build stores the bisection's probe tree as blocks of three levels.  Cell size 0:
+    the tree sampler (shared-memory top, block levels below); cell size 4: the cell search on
+    the unmarked cells of the (not monotone) FP32 CMF, the bisection through the blocks on the
+    marked ones.  Samples through the buffers equal those of the primitive that probes the CMF
+    itself at 2^22 + 3, 2^19 + 1 and 2^16 + 1, the same buffers rebuilt for each smaller size;
+    the last equals the oracle."""
     import torch
     W = pkg.wrs
-    cfg = pkg.ITSConfig(rng=rng)
+    cfg = pkg.ITSConfig(rng=rng, guiding_entry_size=entry)
     wrs = W.WRS(cfg)
     sizes = ((1 << 22) + 3, (1 << 19) + 1, (1 << 16) + 1)
     bufs = W.WRSBuffers.allocate(sizes[0], 1, cfg, handle=wrs.handle)
