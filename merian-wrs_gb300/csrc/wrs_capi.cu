@@ -533,8 +533,8 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
                           : launch_cutpoint_guide(st, b->cmf, n, G, b->guide),
                      "guiding table");
         else if (its_guided(h)) {
-            WRS_CUDA(launch_its_cells(st, b->cmf, n, G, b->coarse, b->cells), "ITS cells");
             // an FP32 CMF need not be monotone: mark the cells the search cannot serve
+            WRS_CUDA(launch_its_cells(st, b->cmf, n, G, b->coarse, b->cells, !comp), "ITS cells");
             if (!comp)
                 WRS_CUDA(launch_its_marks(st, b->cmf, n, G, b->cells,
                                           reinterpret_cast<float*>(b->tile_scratch),

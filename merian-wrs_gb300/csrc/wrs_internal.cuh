@@ -233,12 +233,13 @@ struct alignas(32) ItsCell {
 };
 static_assert(sizeof(ItsCell) == 32, "one cell block is one 32-byte sector");
 cudaError_t launch_its_cells(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
-                             uint32_t* coarse, ItsCell* cells);
+                             uint32_t* coarse, ItsCell* cells, bool check = false);
 cudaError_t launch_its_sample_cells(cudaStream_t st, uint32_t rng, const float* cmf, uint32_t n,
                                     const ItsCell* cells, uint32_t G, uint64_t S, uint64_t seed,
                                     uint64_t offset, uint32_t* out,
                                     const TreeBlock* blocks = nullptr, uint32_t L = 0);
-// FP32 CMF: marks the cells the cell search cannot serve (bit 31 of y), after launch_its_cells;
+// FP32 CMF: marks the cells whose targets can meet a decrease of the CMF (bit 31 of y), after
+// launch_its_cells with check (which marks the cells whose start is not below c_k);
 // tile_scratch: 2 * tiles_for(n) floats; bad: a device word (set when every cell is marked)
 cudaError_t launch_its_marks(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
                              ItsCell* cells, float* tile_scratch, uint32_t* bad);

@@ -603,10 +603,16 @@ __device__ __forceinline__ uint32_t cell_start_warp(const float* __restrict__ cm
     return k < G ? x : n - 1u;
 }
 
+// bit 31 of a cell's y: an FP32 CMF's cell the search cannot serve (the search bisects it)
+constexpr uint32_t kCellUnsafe = 0x80000000u;
+
 __device__ __forceinline__ uint32_t cell_part(uint32_t x, uint32_t y) {
     return (y - x + kCellParts) / kCellParts;  // ceil((y - x + 1) / kCellParts)
 }
 
+// CHECK (an FP32 CMF, which need not be monotone): a cell whose start x > 0 does not have
+// cmf[x - 1] < c_k is marked for the bisection as it is written
+template <bool CHECK>
 __global__ __launch_bounds__(kSampleThreads) void k_its_cells(const float* __restrict__ cmf,
                                                               uint32_t n, uint32_t G,
                                                               const uint32_t* __restrict__ group,
@@ -626,8 +632,13 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_cells(const float* __res
 #pragma unroll
     for (int j = 0; j < kCellParts; ++j)
         v[j] = __ldg(cmf + min(x + (j + 1) * d - 1u, y));
+    uint32_t ym = y;
+    if (CHECK && x > 0u) {
+        const float ck = __fmul_rn(cell_step(cmf, n, G), __uint2float_rn(k));
+        if (!(x <= n - 1u && __ldg(cmf + x - 1u) < ck)) ym |= kCellUnsafe;
+    }
     uint4* dst = reinterpret_cast<uint4*>(cells + k);
-    dst[0] = make_uint4(x, y, __float_as_uint(v[0]), __float_as_uint(v[1]));
+    dst[0] = make_uint4(x, ym, __float_as_uint(v[0]), __float_as_uint(v[1]));
     dst[1] = make_uint4(__float_as_uint(v[2]), __float_as_uint(v[3]), __float_as_uint(v[4]),
                         __float_as_uint(v[5]));
 }
@@ -641,7 +652,6 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_cells(const float* __res
 // cells whose target range meets one (bit 31 of the cell's y; n < 2^31), and the cells whose
 // start x does not have cmf[x - 1] < c_k; a CMF with a value that is not finite or is negative
 // marks every cell.  The cell search serves the unmarked cells and the bisection the others.
-constexpr uint32_t kCellUnsafe = 0x80000000u;
 constexpr uint32_t kMarkSpan = 64;  // an interval over more cells marks the whole CMF unsafe
 
 // the largest k < G with c_k = fl(step * k) < t (0 if none): the cell of targets just above t
@@ -780,23 +790,14 @@ __global__ __launch_bounds__(kSampleThreads) void k_cmf_mark(const float* __rest
     }
 }
 
-// every cell whose start x > 0 does not have cmf[x - 1] < c_k is marked; with `bad` every
-// cell is
-__global__ __launch_bounds__(kSampleThreads) void k_cells_check(const float* __restrict__ cmf,
-                                                                uint32_t n, uint32_t G,
-                                                                ItsCell* __restrict__ cells,
-                                                                const uint32_t* __restrict__ bad) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= G) return;
-    const bool all = *reinterpret_cast<const volatile uint32_t*>(bad) != 0u;
-    const uint32_t x = cells[k].x;
-    bool ok = !all;
-    if (ok && x > 0u) {
-        const float ck = __fmul_rn(__fdiv_rn(__ldg(cmf + n - 1u), __uint2float_rn(G)),
-                                   __uint2float_rn(k));
-        ok = x <= n - 1u && __ldg(cmf + x - 1u) < ck;
-    }
-    if (!ok) atomicOr(&cells[k].y, kCellUnsafe);
+// with `bad` raised (a value that is not finite or is negative, or an interval over too many
+// cells) every cell is marked
+__global__ __launch_bounds__(kSampleThreads) void k_cells_mark_all(uint32_t G,
+                                                                   ItsCell* __restrict__ cells,
+                                                                   const uint32_t* __restrict__ bad) {
+    if (*reinterpret_cast<const volatile uint32_t*>(bad) == 0u) return;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < G; k += gridDim.x * blockDim.x)
+        cells[k].y |= kCellUnsafe;
 }
 
 // The bisection of [0, n - 1] for target t (a probe c sends it right when t > c) through the
@@ -965,9 +966,12 @@ static uint32_t warp_blocks(uint32_t G) {
 }
 
 cudaError_t launch_its_cells(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
-                             uint32_t* coarse, ItsCell* cells) {
+                             uint32_t* coarse, ItsCell* cells, bool check) {
     uint32_t* group = launch_cell_brackets(st, cmf, n, G, coarse);
-    k_its_cells<<<warp_blocks(G), kSampleThreads, 0, st>>>(cmf, n, G, group, cells);
+    if (check)
+        k_its_cells<true><<<warp_blocks(G), kSampleThreads, 0, st>>>(cmf, n, G, group, cells);
+    else
+        k_its_cells<false><<<warp_blocks(G), kSampleThreads, 0, st>>>(cmf, n, G, group, cells);
     return cudaGetLastError();
 }
 
@@ -981,8 +985,7 @@ cudaError_t launch_its_marks(cudaStream_t st, const float* cmf, uint32_t n, uint
     k_cmf_tile_min<<<tiles, kSampleThreads, 0, st>>>(cmf, n, tile_min, bad);
     k_tile_suffix_min<<<1, 1024, 0, st>>>(tile_min, tiles, suf);
     k_cmf_mark<<<tiles, kSampleThreads, 0, st>>>(cmf, n, G, suf, tiles, cells, bad);
-    k_cells_check<<<(G + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(cmf, n, G,
-                                                                                      cells, bad);
+    k_cells_mark_all<<<152 * 4, kSampleThreads, 0, st>>>(G, cells, bad);
     return cudaGetLastError();
 }
 
