@@ -261,6 +261,44 @@ def test_scan_precision(pkg, cuda, oracle, N, comp):
     assert err.max() <= (1e-6 if comp else 1e-4), err.max()
 
 
+@pytest.mark.parametrize("case", ["dips", "deep_dips", "nan"])
+@pytest.mark.parametrize("rng", [RNG_REFERENCE, RNG_PHILOX4X32_10])
+def test_its_fp32_cells_on_a_decreasing_cmf(pkg, cuda, oracle, case, rng):
+    """The cell search on an FP32 CMF that really decreases (weights outside the contract):
+    small negative weights (dips the marks cover cell by cell), large ones (intervals over
+    more cells than the marking takes, so every cell bisects), NaN weights (every cell
+    bisects).  Samples equal those of the primitive that bisects the CMF, and the oracle's."""
+    import torch
+    W = pkg.wrs
+    N = 300001
+    w = weights_lognormal(N, 21)
+    r = np.random.default_rng(5)
+    pick = r.random(N) < 0.01
+    if case == "dips":
+        w[pick] = -w[pick] * np.float32(0.01)
+    elif case == "deep_dips":
+        w[pick] = -w[pick] * np.float32(50.0)
+    else:
+        w[r.integers(N // 2, N, 3)] = np.float32("nan")
+    wrs = W.WRS(pkg.ITSConfig(rng=rng))
+    bufs = W.WRSBuffers.allocate(N, 1, wrs.config, handle=wrs.handle)
+    bufs.weights.copy_(h2d(w))
+    wrs.build(None, bufs, N)
+    S = (1 << 20) + 3
+    out = torch.empty(S, dtype=torch.int32, device="cuda")
+    bufs.samples = out
+    wrs.sample(None, bufs, N, S, 17, offset=2)
+    cmf = bufs.internals.views()["cmf"]
+    plain = torch.empty(S, dtype=torch.int32, device="cuda")
+    wrs.its_sample(None, cmf, N, S, 17, 2, plain)
+    torch.cuda.synchronize()
+    assert torch.equal(out, plain)
+    if case != "nan":  # (a NaN total makes every target NaN-derived; the primitive is the bar)
+        got = t2h(out, np.uint32)
+        ref = oracle.its_sample(d2h(cmf, N, np.float32), S, 17, rng=rng, offset=2, nthreads=8)
+        assert np.array_equal(got, ref)
+
+
 @pytest.mark.parametrize("N", [8191, 8192, 8193, 3 * 8192 + 5])
 @pytest.mark.parametrize("comp", [False, True])
 @pytest.mark.parametrize("shift_in,shift_out", [(0, 0), (1, 0), (0, 1), (3, 2)])
