@@ -985,7 +985,9 @@ cudaError_t launch_its_marks(cudaStream_t st, const float* cmf, uint32_t n, uint
     k_cmf_tile_min<<<tiles, kSampleThreads, 0, st>>>(cmf, n, tile_min, bad);
     k_tile_suffix_min<<<1, 1024, 0, st>>>(tile_min, tiles, suf);
     k_cmf_mark<<<tiles, kSampleThreads, 0, st>>>(cmf, n, G, suf, tiles, cells, bad);
-    k_cells_mark_all<<<152 * 4, kSampleThreads, 0, st>>>(G, cells, bad);
+    // (a grid-stride loop: any grid covers the cells; most launches return at once)
+    const uint32_t mark_grid = min((G + kSampleThreads - 1) / kSampleThreads, 1024u);
+    k_cells_mark_all<<<mark_grid, kSampleThreads, 0, st>>>(G, cells, bad);
     return cudaGetLastError();
 }
 
