@@ -6,9 +6,10 @@
 //   alias build : k_total_mass -> k_prefix_partition -> k_split_pack
 //                 (PSA::run, src/device/wrs/alias/psa/PSA.hpp:170-237)
 //   ITS build   : k_scan_bulk, or k_total_mass -> k_scan_exact in the compensated precisions
-//                 (ITS::build, src/device/wrs/its/ITS.hpp:90-108), then in the compensated
-//                 precisions k_its_cells (the cell blocks k_its_sample_cells reads), otherwise
-//                 k_its_tree (the bisection's probe-tree block levels)
+//                 (ITS::build, src/device/wrs/its/ITS.hpp:90-108), then with a cell size
+//                 k_its_cells (the cell blocks k_its_sample_cells reads); on the FP32 CMF also
+//                 the cell marks (k_cmf_tile_min -> k_tile_suffix_min -> k_cmf_mark) and
+//                 k_its_tree (the probe-tree blocks the marked cells and cell size 0 bisect in)
 //   Cutpoint    : the same scan -> k_cutpoint_guide, or k_guide_monotone on the compensated CMF
 //                 (Cutpoint::build, src/device/wrs/cutpoint/Cutpoint.hpp:108-138)
 //   sample      : k_alias_sample | k_its_sample (k_its_sample_cells) | k_cutpoint_sample
