@@ -34,8 +34,14 @@
  *   wrs_cutpoint_guide            CutpointGuidingTable::run     src/device/wrs/cutpoint/guiding_table/CutpointGuidingTable.hpp
  *   wrs_cutpoint_sample           CutpointSampling::run         src/device/wrs/cutpoint/sampling/CutpointSampling.hpp
  *                                 (Cutpoint::build / ::sample,  src/device/wrs/cutpoint/Cutpoint.hpp:108-158)
- *   wrs_batch_*                   no counterpart (the reference builds and samples one
- *                                 distribution per call)
+ *   wrs_philox                    PRNG::run / Philox::run       src/device/prng/PRNG.hpp:15-56,
+ *                                                               src/device/prng/philox/Philox.hpp:94-108
+ *   wrs_histogram,                Histogram, ChiSquare, RMSE    src/device/statistics
+ *   wrs_sample_statistics
+ *   wrs_batch_*, wrs_server_*,    no counterpart (the reference builds and samples one
+ *   wrs_autotune_*                distribution per call, with a configuration fixed at
+ *                                 construction)
+ * The last section (test and calibration hooks) is not part of the drop-in path.
  *
  * Errors: the reference throws std::runtime_error("NOT-IMPLEMENTED") for unknown
  * variants (src/device/wrs/WRS.hpp:40,111,141,166); here every entry point returns a
@@ -268,6 +274,12 @@ wrs_status wrs_cutpoint_guide(const wrs_handle* h, void* stream, const float* cm
 wrs_status wrs_cutpoint_sample(const wrs_handle* h, void* stream, const float* cmf, uint32_t n,
                                const uint32_t* guide, uint64_t s, uint64_t seed,
                                uint64_t offset, uint32_t* samples);
+/* The standalone PRNG operator (PRNG::run with PhiloxConfig, src/device/prng/PRNG.hpp:15-56;
+ * src/device/prng/philox/shader.comp:47-55): out[i] = float(x1) / 2^32 for i < n, with
+ * (x0, x1) = the shaders' Philox2x32-7 (7 rounds, multiplier 0xD256D193, Weyl 0x9E3779B9) of
+ * counter (i, 0) and key = seed; the float conversion rounds to nearest, so 1.0f can occur.
+ * (The alias sampler's stream uses counter (0, i).)  out: n device floats. */
+wrs_status wrs_philox(void* stream, uint32_t seed, uint32_t n, float* out);
 /* Inclusive prefix sum (the scan of wrs_prefix_sum) that allocates no device memory, for
  * callers that cannot call cudaMalloc -- e.g. code running under a host application whose
  * pool already holds all device memory, code that must not take the device-wide
@@ -283,21 +295,6 @@ wrs_status wrs_cutpoint_sample(const wrs_handle* h, void* stream, const float* c
  * caller-owned device word on `stream`. */
 wrs_status wrs_prefix_sum_noalloc(void* stream, const float* in, uint32_t n, float* out,
                                   uint32_t scan_precision, uint32_t* device_status);
-/* Test hook for the bounded-wait path: runs the scan of wrs_prefix_sum with its first
- * tile never scheduled (the tile ticket starts at 1) and a wait budget of `spin_limit`
- * polls, so every other tile's lookback runs out of budget.  The kernel still ends;
- * wrs_buffers_status then reports WRS_ERR_TIMEOUT and the context stays usable.
- * No counterpart in the reference (its DecoupledMean lookback breaks silently after
- * MAX_IT polls, src/device/mean/decoupled/float.comp:143). */
-wrs_status wrs_test_prefix_sum_stalled(const wrs_handle* h, void* stream, const float* in,
-                                       uint32_t n, float* out, wrs_buffers* b,
-                                       uint32_t spin_limit);
-/* Test hook for the server's table arena (host only, no device work): `iterations` random
- * allocations and releases of up to 4 MiB in a 1 GiB arena, checked against a shadow map
- * (no two live blocks overlap, the used byte count matches, everything released coalesces
- * back into one block).  Returns 0 when every check held, else the number of the first
- * check that failed. */
-int wrs_test_arena(uint64_t seed, uint32_t iterations);
 /* Host helper: upload the FP32 mean, the FP64 mean (total / N, used by the float-float
  * mode's split targets) and the heavy count into b, for driving wrs_split_pack directly. */
 wrs_status wrs_buffers_set_partition_info(wrs_buffers* b, void* stream, float mean,
@@ -435,15 +432,6 @@ size_t wrs_statistics_scratch_bytes(uint32_t n);
 wrs_status wrs_sample_statistics(void* stream, const uint64_t* hist, const float* weights,
                                  uint32_t n, uint64_t s, void* scratch, double* out);
 
-/* ---- device calibration ----------------------------------------------------------------
- * Launches one `width`-byte load (4, 8, 16, 32, 64 or 128) per thread from a hashed,
- * width-aligned position in `buffer` (device memory, `bytes` long), `accesses` threads in
- * all; `sink` is a device word the kernel may write.  Time it with events on `stream`: with
- * width 8 the result is the device's random-gather rate, the bound of alias sampling from
- * tables larger than L2.  No counterpart in the reference. */
-wrs_status wrs_probe_random_gather(void* stream, const void* buffer, uint64_t bytes,
-                                   uint64_t accesses, uint32_t width, uint32_t* sink);
-
 /* ---- autotuning (alias method) -----------------------------------------------------------
  * No counterpart in the reference, whose WRSConfig is fixed at construction
  * (src/device/wrs/WRS.hpp:116-119).  Two knobs are tuned by measurement (CUDA events on
@@ -500,6 +488,31 @@ wrs_status wrs_autotune_alias(const wrs_config* base, void* stream, const float*
 wrs_status wrs_autotune_batch(const wrs_config* base, void* stream, const wrs_dist_desc* descs,
                               uint32_t count, const wrs_tune_space* space, wrs_tune_result* out,
                               wrs_tune_trial* trials, uint32_t max_trials);
+
+/* ---- test and calibration hooks ------------------------------------------------------
+ * Not part of the drop-in path: used by this library's own tests and benchmark. */
+/* Test hook for the bounded-wait path: runs the scan of wrs_prefix_sum with its first
+ * tile never scheduled (the tile ticket starts at 1) and a wait budget of `spin_limit`
+ * polls, so every other tile's lookback runs out of budget.  The kernel still ends;
+ * wrs_buffers_status then reports WRS_ERR_TIMEOUT and the context stays usable.
+ * No counterpart in the reference (its DecoupledMean lookback breaks silently after
+ * MAX_IT polls, src/device/mean/decoupled/float.comp:143). */
+wrs_status wrs_test_prefix_sum_stalled(const wrs_handle* h, void* stream, const float* in,
+                                       uint32_t n, float* out, wrs_buffers* b,
+                                       uint32_t spin_limit);
+/* Test hook for the server's table arena (host only, no device work): `iterations` random
+ * allocations and releases of up to 4 MiB in a 1 GiB arena, checked against a shadow map
+ * (no two live blocks overlap, the used byte count matches, everything released coalesces
+ * back into one block).  Returns 0 when every check held, else the number of the first
+ * check that failed. */
+int wrs_test_arena(uint64_t seed, uint32_t iterations);
+/* Device calibration: launches one `width`-byte load (4, 8, 16, 32, 64 or 128) per thread
+ * from a hashed, width-aligned position in `buffer` (device memory, `bytes` long), `accesses`
+ * threads in all; `sink` is a device word the kernel may write.  Time it with events on `stream`: with
+ * width 8 the result is the device's random-gather rate, the bound of alias sampling from
+ * tables larger than L2.  No counterpart in the reference. */
+wrs_status wrs_probe_random_gather(void* stream, const void* buffer, uint64_t bytes,
+                                   uint64_t accesses, uint32_t width, uint32_t* sink);
 
 #ifdef __cplusplus
 }

@@ -822,19 +822,19 @@ __global__ __launch_bounds__(kTileThreads) void k_scan_bulk(const float* __restr
     const bool whole = aligned_in && tbase + kItems <= n;
     bool landed = true;
     if (whole) {
-        landed = mbar_wait_bounded(&s_bar, 0u, spin_limit);
+        // the copy's own budget, not the caller's lookback budget: whether it lands depends
+        // on no other CTA
+        landed = mbar_wait_bounded(&s_bar, 0u, kSpinLimit);
     } else {
         for (uint32_t e = threadIdx.x; e < kItems; e += kTileThreads)
             s_tile[e] = tbase + e < n ? __ldg(in + tbase + e) : 0.0f;
     }
     if (__syncthreads_or(!landed)) {
-        // the copy did not land in time: report it, wait (bounded) once more for it to end
-        // before the CTA's shared memory goes, and leave the tile unpublished (its
-        // successors' lookbacks give up in turn)
-        if (threadIdx.x == 0) {
-            atomicOr(&ctrl->status, kStatusTimeout);
-            mbar_wait_bounded(&s_bar, 0u, spin_limit);
-        }
+        // the copy did not land in time: report it, keep waiting (kCopyDrainLimit more tries)
+        // for it to end before the CTA's shared memory goes, and leave the tile unpublished
+        // (its successors' lookbacks give up in turn)
+        if (threadIdx.x == 0) atomicOr(&ctrl->status, kStatusTimeout);
+        if (whole) mbar_wait_bounded(&s_bar, 0u, kCopyDrainLimit);
         lookback_end(lb);
         return;
     }
@@ -1362,11 +1362,21 @@ __device__ __forceinline__ uint2 light_item(const PackIn& c, const PackWin& win,
                                      : item_global(c, c.n - 1u - rank);
 }
 
+//
+// Table end (with the full light cap, c.lcap == c.lc): the shader takes the item at partition
+// position j + 1 as the next heavy even when j + 1 = heavyCount, i.e. the first light one, so
+// the last heavy bucket's residual -- and every light bucket packed after the heavies ran out
+// -- aliases that light item, which may have weight zero.  Here the current heavy never leaves
+// the heavy range: the last heavy item is packed as (1, itself) and later light buckets alias
+// it.  In exact arithmetic its residual is exactly one mean there, so nothing moves; in
+// floating point the residual's error stays on a heavy item and no zero-weight item can be
+// drawn.
 __device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ table, uint32_t i0,
                      uint32_t i1, uint32_t j0, uint32_t j1, float spill,
                      const LaterSplits* later) {
     uint32_t i = i0, j = j0;
     float wv = spill;
+    const bool close_last = c.lcap == c.lc;
     // h: the original index of heavy item j, the current heavy; a heavy step moves it to
     // item j + 1, whose index that step has just read
     uint32_t h = 0;
@@ -1374,6 +1384,7 @@ __device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ ta
         const uint2 first = heavy_item(c, win, j);
         h = first.x;
         if (wv == 0.0f) wv = __uint_as_float(first.y);
+        if (close_last && j >= c.hc) h = heavy_item(c, win, c.hc - 1u).x;
     }
     while (i < i1 || j < j1) {
         bool heavy_step;
@@ -1390,12 +1401,13 @@ __device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ ta
         uint32_t tidx, al;
         bool owned = true;
         if (heavy_step) {
-            p = __fdiv_rn(wv, c.mean);
-            al = widx;
+            const bool last = close_last && j + 1u == c.hc;
+            p = last ? 1.0f : __fdiv_rn(wv, c.mean);
+            al = last ? h : widx;
             tidx = h;
             if (later) owned = !covered_later(*later, j, false);
             ++j;
-            h = widx;
+            if (!last) h = widx;
         } else {
             p = __fdiv_rn(weight, c.mean);
             al = h;
@@ -1892,15 +1904,15 @@ cudaError_t launch_split_records(cudaStream_t st, bool r64, bool full_light, con
 // pack/scalar/float.comp (ScalarPack): one thread per subproblem [split_k, split_{k+1}) with the
 // splits read from the records; the same pack loop, ownership window and status bit as the
 // inline kernel (whose slot machinery k_split_pack<..., RECORDS> reuses).
-cudaError_t launch_pack_records(cudaStream_t st, const float* w, const uint32_t* idx,
-                                const float* elems, const BuildCtrl* ctrl, uint32_t* status,
-                                uint32_t n, uint32_t split_size, const SplitRecord* records,
-                                uint2* table) {
+cudaError_t launch_pack_records(cudaStream_t st, bool full_light, const float* w,
+                                const uint32_t* idx, const float* elems, const BuildCtrl* ctrl,
+                                uint32_t* status, uint32_t n, uint32_t split_size,
+                                const SplitRecord* records, uint2* table) {
     // the CTA's items fit the staging window up to split size kPackWin / kSplitPack (12)
     const uint32_t stage = split_size * kSplitPack <= kPackWin ? 1u : 0u;
     const SplitArgs a{w,       n,       ctrl,   table,      idx, elems,
-                      nullptr, nullptr, status, split_size, 0u,  const_cast<SplitRecord*>(records),
-                      nullptr, stage};
+                      nullptr, nullptr, status, split_size, full_light ? 1u : 0u,
+                      const_cast<SplitRecord*>(records), nullptr, stage};
     const uint32_t blocks = (records_for(n, split_size) + kSplitPack - 1) / kSplitPack;
     launch_split_kernel<false, false, false, true>(st, blocks, a, BatchView{});
     return cudaGetLastError();
@@ -2013,14 +2025,17 @@ __global__ __launch_bounds__(256) void k_pack_records_warp(SplitArgs a) {
     float wv = spill;
     if (wv == 0.0f) wv = __shfl_sync(0xffffffffu, hw, 0);  // elem(j0): lane 0 of the heavy chunk
     // the current heavy item's original index (lane 0 of the heavy chunk); a heavy step moves
-    // it to item j + 1, whose index that step fetches
+    // it to item j + 1, whose index that step fetches.  With the table-end rule (full light
+    // cap, as pack()) it never leaves the heavy range.
+    const bool close_last = a.full_light != 0u;
     uint32_t h = __shfl_sync(0xffffffffu, hidx, 0);
+    if (close_last && j0 >= hc) h = __ldg(idx + hc - 1u);
     // pending entries: lane e holds step e of the current group of 32 -- the numerator of its
     // p (divided by the mean when the group is written, one division per lane), its alias,
     // its table index and its partition position
     uint32_t e_out = 0u, e_a = 0u, e_pos = 0u;
     float e_num = 0.0f;
-    bool e_light = false;
+    bool e_light = false, e_one = false;
     uint32_t pend = 0;
     while (i < i1 || j < j1) {
         bool heavy_step;
@@ -2047,16 +2062,18 @@ __global__ __launch_bounds__(256) void k_pack_records_warp(SplitArgs a) {
             widx = __shfl_sync(0xffffffffu, lidx, i - lb);
             weight = __shfl_sync(0xffffffffu, lw, i - lb);
         }
+        const bool last = heavy_step && close_last && j + 1u == hc;
         if (lane == pend) {
             e_num = heavy_step ? wv : weight;
-            e_a = heavy_step ? widx : h;
+            e_a = heavy_step && !last ? widx : h;
             e_out = heavy_step ? h : widx;
             e_pos = heavy_step ? j : i;
             e_light = !heavy_step;
+            e_one = last;
         }
         if (heavy_step) {
             ++j;
-            h = widx;
+            if (!last) h = widx;
         } else {
             ++i;
         }
@@ -2065,22 +2082,25 @@ __global__ __launch_bounds__(256) void k_pack_records_warp(SplitArgs a) {
             // whole warp: the shuffles of the ownership test need every lane
             const bool owned = clean || !covered_later_warp(li, lj, count, e_pos, e_light);
             if (owned && e_out < n)
-                table[e_out] = make_uint2(__float_as_uint(__fdiv_rn(e_num, mean)), e_a);
+                table[e_out] = make_uint2(
+                    __float_as_uint(e_one ? 1.0f : __fdiv_rn(e_num, mean)), e_a);
             pend = 0;
         }
     }
     // the last, partial group
     const bool owned = clean || !covered_later_warp(li, lj, count, e_pos, e_light);
     if (lane < pend && owned && e_out < n)
-        table[e_out] = make_uint2(__float_as_uint(__fdiv_rn(e_num, mean)), e_a);
+        table[e_out] = make_uint2(__float_as_uint(e_one ? 1.0f : __fdiv_rn(e_num, mean)), e_a);
 }
 
-cudaError_t launch_pack_records_warp(cudaStream_t st, const float* w, const uint32_t* idx,
-                                     const float* elems, const BuildCtrl* ctrl, uint32_t* status,
-                                     uint32_t n, uint32_t split_size, const SplitRecord* records,
+cudaError_t launch_pack_records_warp(cudaStream_t st, bool full_light, const float* w,
+                                     const uint32_t* idx, const float* elems,
+                                     const BuildCtrl* ctrl, uint32_t* status, uint32_t n,
+                                     uint32_t split_size, const SplitRecord* records,
                                      uint2* table) {
     const SplitArgs a{w,       n,       ctrl,   table,      idx, elems,
-                      nullptr, nullptr, status, split_size, 0u,  const_cast<SplitRecord*>(records)};
+                      nullptr, nullptr, status, split_size, full_light ? 1u : 0u,
+                      const_cast<SplitRecord*>(records)};
     const uint64_t threads = static_cast<uint64_t>(records_for(n, split_size)) * 32u;
     k_pack_records_warp<<<static_cast<unsigned>((threads + 255u) / 256u), 256, 0, st>>>(a);
     return cudaGetLastError();

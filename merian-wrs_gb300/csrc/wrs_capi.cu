@@ -53,6 +53,7 @@ struct wrs_buffers {
     ItsCell* cells = nullptr;
     TreeBlock* tree = nullptr;   // ITS bisection: the probe tree's stored block levels
     uint32_t tree_n = 0;         // the n the last build stored them for (0: none)
+    uint32_t cells_n = 0;        // the n the last build wrote the ITS cell blocks for (0: none)
     uint32_t* coarse = nullptr;  // scratch of the guiding-table / cell construction
     uint32_t* tile_scratch = nullptr;  // block-wise baselines: 3 words per tile
     int2* descent = nullptr;           // split-pack: shared bisection tops per CTA
@@ -451,11 +452,12 @@ wrs_status wrs_pack(const wrs_handle* h, void* stream, const float* weights,
     if (h->cfg.split_size == 0) return fail(WRS_ERR_INVALID_ARG, "split_size must be >= 1");
     const SplitRecord* r = reinterpret_cast<const SplitRecord*>(records);
     uint2* t = reinterpret_cast<uint2*>(table);
+    const bool fl = h->cfg.split_full_light != 0;
     WRS_CUDA(h->cfg.split_pack_mode == WRS_SPLITPACK_SERIAL_SUBGROUP
-                 ? launch_pack_records_warp(as_stream(stream), weights, partition_indices,
+                 ? launch_pack_records_warp(as_stream(stream), fl, weights, partition_indices,
                                             partition_elements, b->ctrl, &b->ctrl->status, n,
                                             h->cfg.split_size, r, t)
-                 : launch_pack_records(as_stream(stream), weights, partition_indices,
+                 : launch_pack_records(as_stream(stream), fl, weights, partition_indices,
                                        partition_elements, b->ctrl, &b->ctrl->status, n,
                                        h->cfg.split_size, r, t),
              "pack");
@@ -535,12 +537,14 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
                      "guiding table");
         else if (its_guided(h)) {
             // an FP32 CMF need not be monotone: mark the cells the search cannot serve
+            b->cells_n = 0;
             WRS_CUDA(launch_its_cells(st, b->cmf, n, G, b->coarse, b->cells, !comp), "ITS cells");
             if (!comp)
                 WRS_CUDA(launch_its_marks(st, b->cmf, n, G, b->cells,
                                           reinterpret_cast<float*>(b->tile_scratch),
                                           b->tile_scratch + 2u * b->cap_tiles),
                          "ITS cell marks");
+            b->cells_n = n;
         }
         b->tree_n = 0;
         if (b->tree && its_tree_levels(h->cfg, n)) {
@@ -569,12 +573,14 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
                                       h->cfg.split_full_light != 0, b->prefix, lo, b->ctrl, n,
                                       h->cfg.split_size, b->records),
                  "split records");
+        const bool fl = h->cfg.split_full_light != 0;
         WRS_CUDA(h->cfg.split_pack_mode == WRS_SPLITPACK_SERIAL_SUBGROUP
-                     ? launch_pack_records_warp(st, weights, b->idx, elems, b->ctrl,
+                     ? launch_pack_records_warp(st, fl, weights, b->idx, elems, b->ctrl,
                                                 &b->ctrl->status, n, h->cfg.split_size,
                                                 b->records, b->table)
-                     : launch_pack_records(st, weights, b->idx, elems, b->ctrl, &b->ctrl->status,
-                                           n, h->cfg.split_size, b->records, b->table),
+                     : launch_pack_records(st, fl, weights, b->idx, elems, b->ctrl,
+                                           &b->ctrl->status, n, h->cfg.split_size, b->records,
+                                           b->table),
                  "pack");
         return WRS_OK;
     }
@@ -594,10 +600,12 @@ wrs_status wrs_sample_at(const wrs_handle* h, void* stream, const wrs_buffers* b
         return fail(WRS_ERR_INVALID_ARG, "buffers were created for another method");
     if ((st = check_tables(h, b)) != WRS_OK) return st;
     if (h->cfg.method == WRS_METHOD_ITS) {
-        if (its_guided(h) && s) {
+        if (its_guided(h) && s && b->cells_n == n) {
             // the cell-block search returns the bisection's index: for every target on the
             // compensated (non-decreasing) CMF, for the unmarked cells' targets on an FP32 one;
-            // the marked cells bisect, through the stored probe tree when the build made it
+            // the marked cells bisect, through the stored probe tree when the build made it.
+            // Cells written for another n (or none yet) are not read: the bisections below
+            // give the same samples
             if (!samples) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
             const bool tree = !compensated(h) && b->tree && b->tree_n == n;
             WRS_CUDA(launch_its_sample_cells(as_stream(stream), h->cfg.rng, b->cmf, n, b->cells,

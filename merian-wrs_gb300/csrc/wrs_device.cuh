@@ -19,6 +19,10 @@ constexpr uint32_t kStatusTimeout = 1u;      // a lookback spin exhausted its bu
 constexpr uint32_t kStatusNonMonotone = 2u;  // split k+1 < split k (overlapping subproblems)
 
 constexpr uint32_t kSpinLimit = 1u << 21;  // lookback polls before giving up (>= ~1 s)
+// mbarrier tries a CTA spends on its own bulk copy after the first kSpinLimit ran out: the copy's
+// completion depends on no other CTA, so this only bounds a wait that ends in practice; the CTA
+// leaves before the copy lands only after both budgets
+constexpr uint32_t kCopyDrainLimit = 1u << 25;
 
 // ---------------------------------------------------------------------------
 // float-float arithmetic (Knuth two-sum); every operation rounds once.

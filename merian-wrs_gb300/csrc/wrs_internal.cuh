@@ -142,13 +142,16 @@ static_assert(sizeof(SplitRecord) == 12, "split record layout");
 cudaError_t launch_split_records(cudaStream_t st, bool r64, bool full_light, const float* prefix,
                                  const float* prefix_lo, const BuildCtrl* ctrl, uint32_t n,
                                  uint32_t split_size, SplitRecord* records);
-cudaError_t launch_pack_records(cudaStream_t st, const float* w, const uint32_t* idx,
-                                const float* elems, const BuildCtrl* ctrl, uint32_t* status,
-                                uint32_t n, uint32_t split_size, const SplitRecord* records,
-                                uint2* table);
-cudaError_t launch_pack_records_warp(cudaStream_t st, const float* w, const uint32_t* idx,
-                                     const float* elems, const BuildCtrl* ctrl, uint32_t* status,
-                                     uint32_t n, uint32_t split_size, const SplitRecord* records,
+// full_light: the table-end rule of the full light cap (the current heavy stays in the heavy
+// range), as the split-pack with split_full_light
+cudaError_t launch_pack_records(cudaStream_t st, bool full_light, const float* w,
+                                const uint32_t* idx, const float* elems, const BuildCtrl* ctrl,
+                                uint32_t* status, uint32_t n, uint32_t split_size,
+                                const SplitRecord* records, uint2* table);
+cudaError_t launch_pack_records_warp(cudaStream_t st, bool full_light, const float* w,
+                                     const uint32_t* idx, const float* elems,
+                                     const BuildCtrl* ctrl, uint32_t* status, uint32_t n,
+                                     uint32_t split_size, const SplitRecord* records,
                                      uint2* table);
 // descent: scratch of descent_entries(n) int2 (or null: every bisection starts at the top)
 __host__ __device__ inline uint32_t descent_entries(uint32_t max_n) {

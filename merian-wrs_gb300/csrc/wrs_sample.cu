@@ -893,7 +893,9 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_cells(
     // an FP32 CMF's cell may be marked (its targets can meet an inversion, or its start is not
     // below c_k): bisect those (the compensated CMF's cells are never marked)
     const bool unsafe = (q0.y & kCellUnsafe) != 0u;
-    uint32_t x = q0.x, y = q0.y & ~kCellUnsafe;
+    // (a cell block holds indices < n for the n it was built for; the clamp keeps any other
+    // block's search inside the CMF)
+    uint32_t x = q0.x, y = min(q0.y & ~kCellUnsafe, last);
     const float v[kCellParts] = {__uint_as_float(q0.z), __uint_as_float(q0.w),
                                  __uint_as_float(q1.x), __uint_as_float(q1.y),
                                  __uint_as_float(q1.z), __uint_as_float(q1.w)};
@@ -1051,8 +1053,10 @@ __global__ __launch_bounds__(kSampleThreads) void k_cutpoint_sample(
     }
     uint32_t k = __float2uint_rz(__fmul_rn(u1, __uint2float_rn(G)));
     k = k < G - 1u ? k : G - 1u;
-    const uint32_t x = __ldg(guide + k);
-    const uint32_t y = k != G - 1u ? __ldg(guide + k + 1u) : n - 1u;
+    // (entries are < n for the CMF the table was built from; the clamps keep a table built
+    // for another n from reading outside the CMF)
+    const uint32_t x = min(__ldg(guide + k), n - 1u);
+    const uint32_t y = k != G - 1u ? max(min(__ldg(guide + k + 1u), n - 1u), x) : n - 1u;
     const float u2 = search_range_u(cmf, x, y, uu);
     __stcs(out + s, bisect(cmf, x, y, u2));
 }

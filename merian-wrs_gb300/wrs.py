@@ -146,6 +146,7 @@ def lib() -> C.CDLL:
             "wrs_test_prefix_sum_stalled": (i32, [vp, vp, vp, u32, vp, vp, u32]),
             "wrs_test_arena": (i32, [u64, u32]),
             "wrs_prefix_sum_noalloc": (i32, [vp, vp, u32, vp, u32, vp]),
+            "wrs_philox": (i32, [vp, u32, u32, vp]),
             "wrs_batch_bytes": (sz, [vp, u32, u64, u64]),
             "wrs_batch_create": (i32, [vp, u32, u64, u64, C.POINTER(vp)]),
             "wrs_batch_destroy": (None, [vp]),
@@ -418,6 +419,17 @@ class WRS:
     def cutpoint_sample(self, stream, cmf, N, guide, S, seed, offset, out) -> None:
         check(lib().wrs_cutpoint_sample(self.handle.ptr, _stream_ptr(stream), _dev_ptr(cmf), N,
                                         _dev_ptr(guide), S, seed, offset, _dev_ptr(out)))
+
+
+class PRNG:
+    """The reference's PRNG operator with its one alternative, PhiloxConfig
+    (src/device/prng/PRNG.hpp:15-56): run(cmd, buffers, S, seed = 12345) fills buffers.samples
+    with S uniform floats, element i = float(x1) / 2^32 of the shaders' Philox2x32-7 at counter
+    (i, 0), key = seed (src/device/prng/philox/shader.comp:47-55).  `samples` is a float32
+    device tensor (or a raw device address)."""
+
+    def run(self, stream, samples, S: int, seed: int = 12345) -> None:
+        check(lib().wrs_philox(_stream_ptr(stream), seed & 0xFFFFFFFF, S, _dev_ptr(samples)))
 
 
 class DistDesc(C.Structure):

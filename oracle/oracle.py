@@ -60,6 +60,7 @@ class Oracle:
                 "wrso_philox2x32_7": (None, [u32, u32, u32, vp]),
                 "wrso_philox4x32_10": (None, [vp, vp, vp]),
                 "wrso_wang_hash": (u32, [u32]),
+                "wrso_philox_uniform": (None, [u32, u32, vp]),
                 "wrso_unit_ref": (f32, [u32]),
                 "wrso_total_mass": (f64, [vp, u64]),
                 "wrso_mean": (f32, [vp, u64]),
@@ -71,9 +72,11 @@ class Oracle:
                 "wrso_split": (None, [vp, vp, u32, u32, f32, f64, u32, i32, vp, vp, vp]),
                 "wrso_split_pack": (None, [vp, vp, vp, vp, vp, u32, f32, f64, u32, u32, i32, vp,
                                            vp]),
+                "wrso_split_pack_mt": (None, [vp, vp, vp, vp, vp, u32, f32, f64, u32, u32, i32,
+                                              i32, vp, vp]),
                 "wrso_psa_build": (None, [vp, u32, u32, i32, i32, vp, vp, vp]),
                 "wrso_scalar_split": (None, [vp, vp, u32, u32, f32, f64, u32, i32, vp]),
-                "wrso_scalar_pack": (None, [vp, vp, vp, u32, f32, u32, u32, vp, vp]),
+                "wrso_scalar_pack": (None, [vp, vp, vp, u32, f32, u32, u32, i32, vp, vp]),
                 "wrso_alias_sample": (None, [vp, u32, u64, u64, u64, u32, u32, i32, vp]),
                 "wrso_its_sample": (None, [vp, u32, u64, u64, u64, u32, u32, i32, i32, vp]),
                 "wrso_cutpoint_guide": (None, [vp, u32, u32, vp]),
@@ -105,6 +108,12 @@ class Oracle:
         out = np.zeros(4, np.uint32)
         self.lib.wrso_philox4x32_10(_ptr(c), _ptr(k), _ptr(out))
         return [int(x) for x in out]
+
+    def philox_uniform(self, seed: int, n: int) -> np.ndarray:
+        """The PRNG operator's n floats (prng/philox/shader.comp:47-55)."""
+        out = np.empty(n, np.float32)
+        self.lib.wrso_philox_uniform(seed & 0xFFFFFFFF, n, _ptr(out))
+        return out
 
     def wang_hash(self, x: int) -> int:
         return int(self.lib.wrso_wang_hash(x & 0xFFFFFFFF))
@@ -163,8 +172,9 @@ class Oracle:
         return int(i[0]), int(j[0]), np.float32(s[0])
 
     def split_pack(self, w, idx, prefix, heavy_count, mean, split_size, flags=0, elems=None,
-                   return_splits=False, prefix_lo=None, mean64=0.0):
-        """prefix_lo / mean64: the float-float mode's low words and FP64 mean."""
+                   return_splits=False, prefix_lo=None, mean64=0.0, nthreads=1):
+        """prefix_lo / mean64: the float-float mode's low words and FP64 mean; nthreads
+        spreads the split searches (the table does not depend on it)."""
         w = np.ascontiguousarray(w, np.float32)
         idx = np.ascontiguousarray(idx, np.uint32)
         prefix = np.ascontiguousarray(prefix, np.float32)
@@ -173,11 +183,12 @@ class Oracle:
         table = np.zeros(N, ENTRY_DTYPE)
         K = max(N // split_size, 1)
         splits = np.zeros(3 * (K + 1), np.uint32) if return_splits else None
-        self.lib.wrso_split_pack(_ptr(w), _ptr(idx),
-                                 _ptr(np.ascontiguousarray(elems, np.float32))
-                                 if elems is not None else None,
-                                 _ptr(prefix), _ptr(lo), heavy_count, np.float32(mean),
-                                 float(mean64), N, split_size, flags, _ptr(table), _ptr(splits))
+        self.lib.wrso_split_pack_mt(_ptr(w), _ptr(idx),
+                                    _ptr(np.ascontiguousarray(elems, np.float32))
+                                    if elems is not None else None,
+                                    _ptr(prefix), _ptr(lo), heavy_count, np.float32(mean),
+                                    float(mean64), N, split_size, flags, int(nthreads),
+                                    _ptr(table), _ptr(splits))
         if return_splits:
             sp = splits.reshape(K + 1, 3)
             return table, (sp[:, 0].copy(), sp[:, 1].copy(), sp[:, 2].view(np.float32).copy())
@@ -195,8 +206,9 @@ class Oracle:
                                    float(mean64), split_size, flags, _ptr(rec))
         return rec
 
-    def scalar_pack(self, w, idx, heavy_count, mean, split_size, records, elems=None):
-        """ScalarPack from split records (SPLIT_DTYPE)."""
+    def scalar_pack(self, w, idx, heavy_count, mean, split_size, records, elems=None, flags=0):
+        """ScalarPack from split records (SPLIT_DTYPE); flags & SPLIT_FULL_LIGHT applies the
+        table-end rule of the full light cap."""
         w = np.ascontiguousarray(w, np.float32)
         idx = np.ascontiguousarray(idx, np.uint32)
         rec = np.ascontiguousarray(records, SPLIT_DTYPE)
@@ -204,8 +216,8 @@ class Oracle:
         self.lib.wrso_scalar_pack(_ptr(w), _ptr(idx),
                                   _ptr(np.ascontiguousarray(elems, np.float32))
                                   if elems is not None else None,
-                                  heavy_count, np.float32(mean), w.size, split_size, _ptr(rec),
-                                  _ptr(table))
+                                  heavy_count, np.float32(mean), w.size, split_size, int(flags),
+                                  _ptr(rec), _ptr(table))
         return table
 
     def psa_build(self, w, split_size=2, nthreads=1, flags=0):

@@ -54,6 +54,16 @@ void wrso_philox2x32_7(uint32_t c0, uint32_t c1, uint32_t key, uint32_t out[2]) 
     out[1] = x1;
 }
 
+/* src/device/prng/philox/shader.comp:47-55 (the PRNG operator): out[i] = float(x1) / 2^32 of
+ * Philox2x32-7 at counter (i, 0), key = seed; the conversion rounds to nearest. */
+void wrso_philox_uniform(uint32_t seed, uint32_t n, float* out) {
+    uint32_t r[2];
+    for (uint32_t i = 0; i < n; ++i) {
+        wrso_philox2x32_7(i, 0u, seed, r);
+        out[i] = wrso_unit_ref(r[1]);
+    }
+}
+
 /* Random123 Philox4x32 with 10 rounds; key schedule bumped between rounds. */
 void wrso_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
     uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
@@ -324,13 +334,20 @@ typedef struct {
     uint32_t N, hc, lc;
     float mean;
     wrso_entry* table;
+    int close_last; /* table-end rule (flags & WRSO_SPLIT_FULL_LIGHT), see wrso_pack */
 } wrso_pack_ctx;
 
 static inline float wrso_elem(const wrso_pack_ctx* c, uint32_t pos) {
     return c->elems ? c->elems[pos] : c->w[c->idx[pos]];
 }
 
-/* splitpack/inline/shader.comp:130-223 (pack).  Every arithmetic step rounds once. */
+/* splitpack/inline/shader.comp:130-223 (pack).  Every arithmetic step rounds once.
+ * close_last (the table-end rule that goes with the full light cap): the shader reads the
+ * current heavy h = idx[j] and the next heavy idx[j + 1] even at j + 1 = heavyCount, where
+ * position j + 1 holds the first light item, so the last heavy bucket's residual and every
+ * light bucket packed after the heavies ran out alias a light item (possibly of weight zero).
+ * With close_last, h = idx[min(j, heavyCount - 1)] and a heavy step at j + 1 = heavyCount
+ * writes (1, h): the residual stays on the last heavy item. */
 static void wrso_pack(const wrso_pack_ctx* c, uint32_t i0, uint32_t i1, uint32_t j0, uint32_t j1,
                       float spill) {
     const uint32_t N = c->N, hc = c->hc, lc = c->lc;
@@ -347,7 +364,8 @@ static void wrso_pack(const wrso_pack_ctx* c, uint32_t i0, uint32_t i1, uint32_t
             packHeavy = 1;
         else
             packHeavy = w <= mean;
-        uint32_t h = c->idx[j];
+        uint32_t h = c->idx[(c->close_last && j >= hc) ? hc - 1 : j];
+        const int last = c->close_last && j + 1 == hc;
         uint32_t weightIdx;
         float weight;
         if (packHeavy) {
@@ -360,8 +378,8 @@ static void wrso_pack(const wrso_pack_ctx* c, uint32_t i0, uint32_t i1, uint32_t
         float p;
         uint32_t idx, a;
         if (packHeavy) {
-            p = w / mean;
-            a = weightIdx;
+            p = last ? 1.0f : w / mean;
+            a = last ? h : weightIdx;
             idx = h;
             j += 1;
         } else {
@@ -382,15 +400,40 @@ static void wrso_pack(const wrso_pack_ctx* c, uint32_t i0, uint32_t i1, uint32_t
     }
 }
 
+typedef struct {
+    const float* prefix;
+    const float* prefix_lo;
+    uint32_t N, hc, split_size, K;
+    float mean;
+    double mean64;
+    int flags;
+    uint32_t* si;
+    uint32_t* sj;
+    float* ss;
+} wrso_splits_ctx;
+
+/* splits k in [1, K) of one thread's share (each split is independent of the others) */
+static void wrso_splits_task(void* p, int t, int nt) {
+    wrso_splits_ctx* c = (wrso_splits_ctx*)p;
+    uint64_t lo, hi;
+    wrso_range(c->K - 1u, t, nt, &lo, &hi);
+    for (uint64_t k = lo + 1; k < hi + 1; ++k)
+        wrso_split(c->prefix, c->prefix_lo, c->N, c->hc, c->mean, c->mean64,
+                   (uint32_t)k * c->split_size, c->flags, &c->si[k], &c->sj[k], &c->ss[k]);
+}
+
 /* Driver of splitpack/inline/shader.comp:225-270: split k packs [split_k, split_{k+1})
  * for k in [0, K) with K = N / splitSize; split_0 = (0,0,0), split_K = (lc, hc, 0);
  * i1 = max(split_{k+1}.i, i0), j1 = max(split_{k+1}.j, j0).  Subproblems run in
  * increasing k, so where two subproblems write one entry the later k wins.
  * Guards beyond the shader (which is undefined there): heavyCount == 0 or N gives
- * table[i] = (1, i); K == 0 (N < splitSize) is treated as K = 1. */
-void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, const float* prefix,
-                     const float* prefix_lo, uint32_t hc, float mean, double mean64, uint32_t N,
-                     uint32_t split_size, int flags, wrso_entry* table, uint32_t* splits) {
+ * table[i] = (1, i); K == 0 (N < splitSize) is treated as K = 1.
+ * The K - 1 split searches (independent of each other) are spread over nthreads threads; the
+ * pack loop then runs once, in increasing k, so the table does not depend on nthreads. */
+void wrso_split_pack_mt(const float* w, const uint32_t* idx, const float* elems,
+                        const float* prefix, const float* prefix_lo, uint32_t hc, float mean,
+                        double mean64, uint32_t N, uint32_t split_size, int flags, int nthreads,
+                        wrso_entry* table, uint32_t* splits) {
     if (N == 0) return;
     if (hc == 0 || hc == N) {
         for (uint32_t i = 0; i < N; ++i) {
@@ -401,37 +444,42 @@ void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, co
     }
     uint32_t K = N / split_size;
     if (K == 0) K = 1;
-    wrso_pack_ctx c = {w, idx, elems, N, hc, N - hc, mean, table};
-    uint32_t pi = 0, pj = 0;
-    float pspill = 0.0f;
-    if (splits) {
-        splits[0] = 0;
-        splits[1] = 0;
-        memcpy(&splits[2], &pspill, 4);
-    }
-    for (uint32_t k = 1; k <= K; ++k) {
-        uint32_t ni, nj;
-        float nspill;
-        if (k == K) {
-            ni = N - hc;
-            nj = hc;
-            nspill = 0.0f;
-        } else {
-            wrso_split(prefix, prefix_lo, N, hc, mean, mean64, k * split_size, flags, &ni, &nj,
-                       &nspill);
-        }
+    wrso_splits_ctx sc = {prefix, prefix_lo, N, hc, split_size, K, mean, mean64, flags,
+                          (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)K + 1)),
+                          (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)K + 1)),
+                          (float*)malloc(sizeof(float) * ((size_t)K + 1))};
+    sc.si[0] = 0;
+    sc.sj[0] = 0;
+    sc.ss[0] = 0.0f;
+    sc.si[K] = N - hc;
+    sc.sj[K] = hc;
+    sc.ss[K] = 0.0f;
+    if (K > 1) wrso_parallel(wrso_splits_task, &sc, nthreads < 1 ? 1 : nthreads);
+    wrso_pack_ctx c = {w, idx, elems, N, hc, N - hc, mean, table,
+                       (flags & WRSO_SPLIT_FULL_LIGHT) != 0};
+    for (uint32_t k = 0; k <= K; ++k) {
         if (splits) {
-            splits[3 * k + 0] = ni;
-            splits[3 * k + 1] = nj;
-            memcpy(&splits[3 * k + 2], &nspill, 4);
+            splits[3 * k + 0] = sc.si[k];
+            splits[3 * k + 1] = sc.sj[k];
+            memcpy(&splits[3 * k + 2], &sc.ss[k], 4);
         }
-        uint32_t i1 = ni > pi ? ni : pi;
-        uint32_t j1 = nj > pj ? nj : pj;
-        wrso_pack(&c, pi, i1, pj, j1, pspill);
-        pi = ni;
-        pj = nj;
-        pspill = nspill;
+        if (k == 0) continue;
+        const uint32_t pi = sc.si[k - 1], pj = sc.sj[k - 1];
+        const uint32_t i1 = sc.si[k] > pi ? sc.si[k] : pi;
+        const uint32_t j1 = sc.sj[k] > pj ? sc.sj[k] : pj;
+        wrso_pack(&c, pi, i1, pj, j1, sc.ss[k - 1]);
     }
+    free(sc.si);
+    free(sc.sj);
+    free(sc.ss);
+}
+
+/* wrso_split_pack_mt on one thread */
+void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, const float* prefix,
+                     const float* prefix_lo, uint32_t hc, float mean, double mean64, uint32_t N,
+                     uint32_t split_size, int flags, wrso_entry* table, uint32_t* splits) {
+    wrso_split_pack_mt(w, idx, elems, prefix, prefix_lo, hc, mean, mean64, N, split_size, flags,
+                       1, table, splits);
 }
 
 /* split/scalar/shader.comp:72-133 (ScalarSplit, the split half of SerialSplitPack):
@@ -468,8 +516,8 @@ void wrso_scalar_split(const float* prefix, const float* prefix_lo, uint32_t N, 
  * here i1 = max(split_{k+1}.i, i0), j1 = max(split_{k+1}.j, j0) and the later k's write stands,
  * as for the inline split-pack.  Guard: heavyCount == 0 or N gives table[i] = (1, i). */
 void wrso_scalar_pack(const float* w, const uint32_t* idx, const float* elems, uint32_t hc,
-                      float mean, uint32_t N, uint32_t split_size, const uint32_t* records,
-                      wrso_entry* table) {
+                      float mean, uint32_t N, uint32_t split_size, int flags,
+                      const uint32_t* records, wrso_entry* table) {
     if (N == 0) return;
     if (hc == 0 || hc >= N) {
         for (uint32_t i = 0; i < N; ++i) {
@@ -480,7 +528,8 @@ void wrso_scalar_pack(const float* w, const uint32_t* idx, const float* elems, u
     }
     uint32_t K = (uint32_t)(((uint64_t)N + split_size - 1) / split_size);
     if (K == 0) K = 1;
-    wrso_pack_ctx c = {w, idx, elems, N, hc, N - hc, mean, table};
+    wrso_pack_ctx c = {w, idx, elems, N, hc, N - hc, mean, table,
+                       (flags & WRSO_SPLIT_FULL_LIGHT) != 0};
     uint32_t pi = 0, pj = 0;
     float pspill = 0.0f;
     for (uint32_t k = 0; k < K; ++k) {
@@ -587,7 +636,8 @@ static void psa_splitpack_task(void* p, int t, int nt) {
     uint64_t lo, hi;
     wrso_range(c->K, t, nt, &lo, &hi);
     if (lo >= hi) return;
-    wrso_pack_ctx pc = {c->w, c->idx, c->elems, c->N, c->hc, c->N - c->hc, c->mean, c->table};
+    wrso_pack_ctx pc = {c->w,    c->idx,  c->elems, c->N, c->hc, c->N - c->hc, c->mean,
+                        c->table, (c->flags & WRSO_SPLIT_FULL_LIGHT) != 0};
     uint32_t pi, pj;
     float pspill;
     if (lo == 0) {

@@ -32,6 +32,8 @@ void wrso_philox2x32_7(uint32_t c0, uint32_t c1, uint32_t key, uint32_t out[2]);
 void wrso_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 uint32_t wrso_wang_hash(uint32_t seed);
 float wrso_unit_ref(uint32_t x); /* float(x) / 2^32, round-to-nearest conversion */
+/* the PRNG operator (prng/philox/shader.comp:47-55): out[i] = unit(Philox2x32-7((i, 0), seed).y) */
+void wrso_philox_uniform(uint32_t seed, uint32_t n, float* out);
 
 /* ---- build pieces ---------------------------------------------------------------- */
 double wrso_total_mass(const float* w, uint64_t N);
@@ -57,14 +59,19 @@ void wrso_split_pack(const float* w, const uint32_t* idx, const float* elems, co
                      const float* prefix_lo, uint32_t heavy_count, float mean, double mean64,
                      uint32_t N, uint32_t split_size, int flags, wrso_entry* table,
                      uint32_t* splits /* 3*(K+1) or NULL */);
+/* the same with the split searches on nthreads threads (the same table and splits) */
+void wrso_split_pack_mt(const float* w, const uint32_t* idx, const float* elems,
+                        const float* prefix, const float* prefix_lo, uint32_t heavy_count,
+                        float mean, double mean64, uint32_t N, uint32_t split_size, int flags,
+                        int nthreads, wrso_entry* table, uint32_t* splits);
 /* Serial split-pack: ScalarSplit's ceil(N / split_size) records {i, j, spill} (3 words each)
  * and ScalarPack from them. */
 void wrso_scalar_split(const float* prefix, const float* prefix_lo, uint32_t N, uint32_t heavy_count,
                        float mean, double mean64, uint32_t split_size, int flags,
                        uint32_t* records);
 void wrso_scalar_pack(const float* w, const uint32_t* idx, const float* elems, uint32_t heavy_count,
-                      float mean, uint32_t N, uint32_t split_size, const uint32_t* records,
-                      wrso_entry* table);
+                      float mean, uint32_t N, uint32_t split_size, int flags /* FULL_LIGHT */,
+                      const uint32_t* records, wrso_entry* table);
 /* Full PSA build on the CPU (mean -> partition -> prefix -> split+pack) with nthreads
  * worker threads.  Used as the timed CPU port of the reference path. */
 void wrso_psa_build(const float* w, uint32_t N, uint32_t split_size, int flags, int nthreads,

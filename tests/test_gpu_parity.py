@@ -183,6 +183,36 @@ def test_split_pack_partition_elements_switch(pkg, cuda, oracle, use_elems):
     assert same_table(b.table, ref)
 
 
+@pytest.mark.parametrize("full_light", [False, True])
+@pytest.mark.parametrize("split_size", [4, 12])
+def test_split_pack_table_end(pkg, cuda, oracle, full_light, split_size):
+    """wrs_split_pack on prefixes summed sequentially in FP32 (coarse enough that the last PSA
+    subproblem runs out of heavy items first) with a zero weight at the item past the heavy
+    range: the table equals the oracle's with and without the table-end rule of the full
+    light cap, and with it no entry aliases a light item."""
+    W = pkg.wrs
+    w = weights_precision(1 << 20, 5)
+    w[-1] = 0.0
+    mean = np.float32(oracle.mean(w))
+    idx, elems, hc = oracle.partition(w, mean)
+    prefix = np.concatenate([np.cumsum(elems[:hc], dtype=np.float32),
+                             np.cumsum(elems[hc:][::-1], dtype=np.float32)[::-1]])
+    wrs = W.WRS(pkg.AliasTableConfig(split_size=split_size, split_full_light=full_light))
+    internals = W.Internals(wrs.handle, w.size)
+    W.check(W.lib().wrs_buffers_set_partition_info(internals.ptr, None, float(mean),
+                                                   oracle.total_mass(w) / w.size, hc))
+    table = empty(2 * w.size, "i32")
+    wrs.split_pack(None, h2d(w), h2d(idx), h2d(prefix), h2d(elems), w.size, table, internals)
+    got = t2h(table, np.uint32).view(ENTRY_DTYPE)
+    assert internals.status() == 0
+    ref = oracle.split_pack(w, idx, prefix, hc, mean, split_size, flags=2 if full_light else 0,
+                            elems=elems)
+    assert same_table(got, ref)
+    heavy = np.zeros(w.size, bool)
+    heavy[idx[:hc]] = True
+    assert heavy[got["a"][got["p"] < 1]].all() == full_light
+
+
 def test_split_pack_primitive_on_oracle_inputs(pkg, cuda, oracle):
     """wrs_split_pack on inputs made entirely by the oracle (FP64-rounded prefix)."""
     W = pkg.wrs
@@ -246,6 +276,23 @@ def test_alias_sample_bit_exact(pkg, cuda, oracle, rng, coop, offset):
     ref = oracle.alias_sample(b.table, S, 0xDEADBEEF12345, rng=rng, coop=coop, offset=offset,
                               nthreads=8)
     assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("n", [1, 3, 4, 1023, 1024, 1025, (1 << 20) + 3, (1 << 24) + 1])
+@pytest.mark.parametrize("seed", [0, 12345, 0xFFFFFFFF])
+@pytest.mark.parametrize("shift", [0, 1])
+def test_philox_operator_bit_exact(pkg, cuda, oracle, n, seed, shift):
+    """The PRNG operator (PRNG::run with PhiloxConfig) equals the oracle's restatement of
+    prng/philox/shader.comp:47-55 bit for bit, into aligned and unaligned (shift 1) views,
+    and writes nothing past element n - 1."""
+    W = pkg.wrs
+    buf = empty(n + 8)
+    buf.fill_(-7.0)
+    W.PRNG().run(None, buf[shift:], n, seed)
+    got = t2h(buf, np.float32)
+    assert np.array_equal(got[shift:shift + n].view(np.uint32),
+                          oracle.philox_uniform(seed, n).view(np.uint32))
+    assert np.all(got[:shift] == -7.0) and np.all(got[shift + n:] == -7.0)
 
 
 @pytest.mark.parametrize("N", [1, 3, 4097, (1 << 20) + 1, 1 << 22])
@@ -466,6 +513,39 @@ def test_its_stored_tree_blocks(pkg, cuda, oracle, rng, entry):
     got = t2h(out, np.uint32)
     ref = oracle.its_sample(d2h(cmf, small, np.float32), S, 31, rng=rng, offset=4, nthreads=8)
     assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_its_sample_n_other_than_built(pkg, cuda, oracle, precision):
+    """Sampling with an n other than the last build's: the cell blocks and probe-tree blocks
+    were written for the built n and are not read; the samples equal the primitive's bisection
+    of the first n CMF values (and the oracle's).  A sample call on buffers never built returns
+    indices inside [0, n)."""
+    import torch
+    W = pkg.wrs
+    cfg = pkg.ITSConfig(rng=RNG_PHILOX4X32_10, scan_precision=precision)
+    wrs = W.WRS(cfg)
+    N, n = (1 << 20) + 3, 70001
+    fresh = W.WRSBuffers.allocate(N, 1, cfg, handle=wrs.handle)
+    S = (1 << 18) + 5
+    out = torch.empty(S, dtype=torch.int32, device="cuda")
+    fresh.samples = out
+    wrs.sample(None, fresh, n, S, 5, offset=2)
+    assert int(t2h(out, np.uint32).max()) < n
+    bufs = W.WRSBuffers.allocate(N, 1, cfg, handle=wrs.handle)
+    bufs.weights.copy_(h2d(weights_lognormal(N, 17)))
+    wrs.build(None, bufs, N)
+    bufs.samples = out
+    wrs.sample(None, bufs, n, S, 5, offset=2)
+    plain = torch.empty(S, dtype=torch.int32, device="cuda")
+    cmf = bufs.internals.views()["cmf"]
+    wrs.its_sample(None, cmf, n, S, 5, 2, plain)
+    torch.cuda.synchronize()
+    assert bufs.internals.status() == 0
+    assert torch.equal(out, plain)
+    ref = oracle.its_sample(d2h(cmf, n, np.float32), S, 5, rng=RNG_PHILOX4X32_10, offset=2,
+                            nthreads=8)
+    assert np.array_equal(t2h(out, np.uint32), ref)
 
 
 # ------------------------------------------------------------------- cutpoint ---

@@ -70,24 +70,27 @@ def test_serial_records_and_table_bit_exact(pkg, cuda, oracle, N, split, precisi
     ref = oracle.scalar_split(b.prefix, b.hc, b.mean, split, flags=FLAGS[precision],
                               prefix_lo=b.lo, mean64=b.mean64)
     assert np.array_equal(b.records.view(np.uint32), ref.view(np.uint32))
-    table = oracle.scalar_pack(w, b.idx, b.hc, b.mean, split, b.records, elems=b.elems)
+    table = oracle.scalar_pack(w, b.idx, b.hc, b.mean, split, b.records, elems=b.elems,
+                               flags=FLAGS[precision])
     assert np.array_equal(b.table.view(np.uint64), table.view(np.uint64))
 
 
 @pytest.mark.parametrize("N", [4097, 300001, (1 << 22) + 17])
 @pytest.mark.parametrize("split", [2, 32, 1000])
 @pytest.mark.parametrize("elems", [True, False])
-def test_warp_pack_equals_scalar_pack(pkg, cuda, oracle, N, split, elems):
+@pytest.mark.parametrize("precision", ["fp32", "ff"])
+def test_warp_pack_equals_scalar_pack(pkg, cuda, oracle, N, split, elems, precision):
     """The warp-cooperative strategy writes the scalar pack's table from the same records and
     arrays, with and without partition elements (then the lanes gather the weights), FP32
-    prefixes included (where splits step back and later subproblems override); a build in
-    the warp mode matches the oracle's scalar pack of its own records."""
+    prefixes included (where splits step back and later subproblems override), with and
+    without the table-end rule of the full light cap ("ff"); a build in the warp mode matches
+    the oracle's scalar pack of its own records."""
     import torch
     W = pkg.wrs
     w = weights_lognormal(N, split + N)
-    a = Serial(pkg, w, _cfg(pkg, "fp32", W.SPLITPACK_SERIAL, split, elems))
+    a = Serial(pkg, w, _cfg(pkg, precision, W.SPLITPACK_SERIAL, split, elems))
     assert a.status == 0
-    warp = W.WRS(_cfg(pkg, "fp32", W.SPLITPACK_SERIAL_SUBGROUP, split, elems))
+    warp = W.WRS(_cfg(pkg, precision, W.SPLITPACK_SERIAL_SUBGROUP, split, elems))
     v = a.views
     table = torch.zeros(2 * N, dtype=torch.int32, device="cuda")
     warp.pack(None, a.bufs.weights, v["partition_indices"],
@@ -96,9 +99,10 @@ def test_warp_pack_equals_scalar_pack(pkg, cuda, oracle, N, split, elems):
     torch.cuda.synchronize()
     assert a.bufs.internals.status() == 0
     assert np.array_equal(table.cpu().numpy().view(np.uint64), a.table.view(np.uint64))
-    b = Serial(pkg, w, _cfg(pkg, "fp32", W.SPLITPACK_SERIAL_SUBGROUP, split, elems))
+    b = Serial(pkg, w, _cfg(pkg, precision, W.SPLITPACK_SERIAL_SUBGROUP, split, elems))
     assert b.status == 0
-    ref = oracle.scalar_pack(w, b.idx, b.hc, b.mean, split, b.records, elems=b.elems)
+    ref = oracle.scalar_pack(w, b.idx, b.hc, b.mean, split, b.records, elems=b.elems,
+                             flags=FLAGS[precision])
     assert np.array_equal(b.table.view(np.uint64), ref.view(np.uint64))
 
 

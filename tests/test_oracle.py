@@ -6,7 +6,8 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import golden_path, weights_lognormal, weights_uniform, weights_zipf
+from conftest import (golden_path, weights_lognormal, weights_precision, weights_uniform,
+                      weights_zipf)
 
 GOLDEN = ("ref_pru_1024.npz", "ref_pru_8192.npz")
 
@@ -170,6 +171,18 @@ def test_philox2x32_7_shader_variant(oracle):
         assert oracle.philox2x32_7(0, c1, key) == _philox2x32_7_py(0, c1, key)
 
 
+def test_philox_uniform_operator(oracle):
+    """The PRNG operator (src/device/prng/philox/shader.comp:47-55) restated in pure Python:
+    element i = float(x1) / 2^32 of Philox2x32-7 at counter (i, 0), key = seed, the float
+    conversion rounding to nearest (numpy's uint32 -> float32 conversion)."""
+    for seed in (0, 12345, 0xFFFFFFFF):
+        got = oracle.philox_uniform(seed, 1000)
+        x1 = np.array([_philox2x32_7_py(i, 0, seed)[1] for i in range(1000)], np.uint32)
+        want = x1.astype(np.float32) * np.float32(2.0 ** -32)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+        assert got.min() >= 0.0 and got.max() <= 1.0
+
+
 def test_wang_hash(oracle):
     def py(s):
         s = (s ^ 61) ^ (s >> 16)
@@ -205,6 +218,49 @@ def test_reference_split_tail_defect_and_fix(oracle):
     # the light item gains the mass the last heavy bucket loses
     assert ref_err.max() > 0.9 and np.count_nonzero(ref_err > 0.1) == 2
     assert fix_err.max() < 1e-3
+
+
+def _coarse_partition(oracle, w):
+    """The stable partition with prefixes summed sequentially in FP32 (each class's running
+    sum rounded at every step): prefixes far coarser than the device's, so that PSA's last
+    subproblem runs out of heavy items before its light ones."""
+    mean = np.float32(oracle.mean(w))
+    idx, elems, hc = oracle.partition(w, mean)
+    heavy = np.cumsum(elems[:hc], dtype=np.float32)
+    light = np.cumsum(elems[hc:][::-1], dtype=np.float32)[::-1]
+    return mean, idx, elems, hc, np.concatenate([heavy, light])
+
+
+def test_table_end_rule_never_aliases_a_light_item(oracle):
+    """When a PSA walk runs out of heavy items (the last heavy residual's rounding error),
+    the shader's next heavy is the first light item: with the reference's table end the last
+    light item -- here of weight zero -- is aliased by the last heavy bucket and by every
+    light bucket packed after it.  The table-end rule of the full light cap keeps the last
+    heavy item as (1, itself) and the later light buckets alias it: no entry aliases a light
+    item and zero weights keep p = 0."""
+    from oracle.oracle import SPLIT_FULL_LIGHT
+    w = weights_precision(1 << 20, 5)
+    w[-1] = 0.0  # the light item past the heavy range (position heavyCount)
+    mean, idx, elems, hc, prefix = _coarse_partition(oracle, w)
+    heavy = np.zeros(w.size, bool)
+    heavy[idx[:hc]] = True
+    zero = w == 0
+    for flags in (0, SPLIT_FULL_LIGHT):
+        table = oracle.split_pack(w, idx, prefix, hc, mean, 4, flags=flags, elems=elems)
+        aliased = table["a"][table["p"] < 1]
+        if flags:
+            assert heavy[aliased].all()
+            assert np.all(table["p"][zero] == 0)
+            assert table["p"][idx[hc - 1]] == np.float32(1.0)
+            assert table["a"][idx[hc - 1]] == idx[hc - 1]
+        else:
+            # the reference's table end: the item at position heavyCount is aliased
+            assert np.count_nonzero(aliased == w.size - 1) >= 1
+            assert not heavy[aliased].all()
+    # a single subproblem walks the whole table: the same holds with split size >= N
+    table = oracle.split_pack(w, idx, prefix, hc, mean, w.size, flags=SPLIT_FULL_LIGHT,
+                              elems=elems)
+    assert heavy[table["a"][table["p"] < 1]].all()
 
 
 @pytest.mark.parametrize("gen", [weights_uniform, weights_zipf, weights_lognormal])
@@ -329,7 +385,7 @@ def test_serial_split_pack_equals_inline_when_n_divides(oracle, gen, s):
         inline, (si, sj, ss) = oracle.split_pack(w, idx, prefix, hc, mean, s,
                                                  flags=SPLIT_FULL_LIGHT, return_splits=True)
         rec = oracle.scalar_split(prefix, hc, mean, s, flags=SPLIT_FULL_LIGHT)
-        table = oracle.scalar_pack(w, idx, hc, mean, s, rec)
+        table = oracle.scalar_pack(w, idx, hc, mean, s, rec, flags=SPLIT_FULL_LIGHT)
         if N % s == 0:
             assert np.array_equal(rec["i"], si[1:]) and np.array_equal(rec["j"], sj[1:])
             assert np.array_equal(rec["spill"].view(np.uint32), ss[1:].view(np.uint32))
