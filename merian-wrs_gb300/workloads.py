@@ -1,5 +1,8 @@
-"""Seeded synthetic workloads of the batched and served configurations (device tensors).
+"""Seeded synthetic workloads of the benchmark configurations (device tensors).
 
+headline(): the single large distribution's three shapes -- uniform(0,1] on a 2^-24 grid,
+    Zipf-like (i+1)^-1.1 randomly permuted, log-normal(0, 2).
+precision(): log-normal(0, 3) with 1% forced to 0 and 0.01% scaled by 1e6.
 batched(): 4096 distributions, N_d = floor(exp(U(ln 64, ln 2^20))), each uniform(0,1] or
     Zipf s=1.1 (permuted) by a seeded coin, S_d proportional to N_d with a fixed total.
 served(): a request stream -- Poisson arrivals, N log-uniform in [256, 2^22] log-normal
@@ -15,6 +18,38 @@ import numpy as np
 
 def _pad(x, a=32):
     return (x + a - 1) // a * a
+
+
+HEADLINE_SEEDS = (2, 3, 4)   # uniform, Zipf-like, log-normal
+PRECISION_SEED = 5
+
+
+def headline(dist: int, n: int, seed: int, dev):
+    """Weights of shape `dist` (0 uniform(0,1]: ((x >> 40) + 1) * 2^-24, 1 Zipf-like permuted,
+    2 log-normal(0, 2)), generated on the device with PyTorch's Philox generator."""
+    import torch
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    if dist == 0:
+        x = torch.randint(0, 1 << 24, (n,), generator=g, device=dev, dtype=torch.int64)
+        return ((x + 1).to(torch.float64) * 2.0 ** -24).to(torch.float32)
+    if dist == 1:
+        w = torch.arange(1, n + 1, device=dev, dtype=torch.float64).pow(-1.1).to(torch.float32)
+        return w[torch.randperm(n, generator=g, device=dev)]
+    z = torch.randn(n, generator=g, device=dev, dtype=torch.float32)
+    return torch.exp(2.0 * z)
+
+
+def precision(n: int, dev, seed: int = PRECISION_SEED):
+    """log-normal(0, 3) weights with 1% forced to 0 and 0.01% scaled by 1e6 (device)."""
+    import torch
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    w = torch.exp(3.0 * torch.randn(n, generator=g, device=dev, dtype=torch.float32))
+    w[torch.rand(n, generator=g, device=dev) < 0.01] = 0.0
+    big = torch.rand(n, generator=g, device=dev) < 1e-4
+    w[big] = (w[big].double() * 1e6).float()
+    return w
 
 
 def batched(dev, n_dists: int = 4096, log2_s: int = 30, seed: int = 6,
