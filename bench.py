@@ -47,7 +47,7 @@ sys.path.insert(0, ROOT)
 
 LOG2_N = 26
 LOG2_S = 28
-SEEDS = (2, 3, 4)
+SEEDS = (2, 3, 4)  # the workloads' HEADLINE_SEEDS
 DISTS = ("uniform(0,1]", "zipf(s=1.1, permuted)", "lognormal(0,2)")
 WORKLOAD = ("single large distribution: N=2^26 FP32 weights x 3 seeded distributions "
             "(uniform(0,1], Zipf s=1.1 permuted, log-normal(0,2)); step = PSA alias build + "
@@ -131,19 +131,10 @@ def profiled_traffic() -> float | None:
 # ------------------------------------------------------------------ inputs ---
 
 def make_weights(dist: int, n: int, seed: int, device):
-    """Seeded synthetic weights of the configuration's three shapes (generated on the GPU
-    with PyTorch's Philox generator; the CPU legs copy them back)."""
-    import torch
-    g = torch.Generator(device=device)
-    g.manual_seed(seed)
-    if dist == 0:   # uniform(0,1]: ((x >> 40) + 1) * 2^-24
-        x = torch.randint(0, 1 << 24, (n,), generator=g, device=device, dtype=torch.int64)
-        return ((x + 1).to(torch.float64) * 2.0 ** -24).to(torch.float32)
-    if dist == 1:   # Zipf-like, permuted
-        w = torch.arange(1, n + 1, device=device, dtype=torch.float64).pow(-1.1).to(torch.float32)
-        return w[torch.randperm(n, generator=g, device=device)]
-    z = torch.randn(n, generator=g, device=device, dtype=torch.float32)
-    return torch.exp(2.0 * z)
+    """Seeded synthetic weights of the configuration's three shapes (generated on the GPU;
+    the CPU legs copy them back)."""
+    from importlib import import_module
+    return import_module("merian-wrs_gb300.workloads").headline(dist, n, seed, device)
 
 
 # ------------------------------------------------------------------ clocks ---
@@ -204,48 +195,73 @@ def cpu_threads() -> int:
         return os.cpu_count() or 1
 
 
-def cpu_step(w_host, n: int, s: int, nthreads: int, s_sample: int) -> tuple[float, dict]:
-    """One step of the CPU path: full PSA build of n weights + s_sample alias samples,
-    extrapolated to s samples.  Returns (seconds per step, description)."""
+def cpu_step(w_host, n: int, s: int, nthreads: int) -> tuple[float, dict]:
+    """One whole step of the CPU path, nothing extrapolated: PSA build of n weights (the
+    headline's split size and float-float split) + s alias samples (Philox4x32-10), on
+    nthreads threads.  Returns (seconds, description)."""
     from oracle.oracle import RNG_PHILOX4X32_10, SPLIT_FLOAT_FLOAT, SPLIT_FULL_LIGHT, Oracle
     orc = Oracle()
     t0 = time.perf_counter()
     table, _, _ = orc.psa_build(w_host, SPLIT_SIZE, nthreads=nthreads,
                                 flags=SPLIT_FLOAT_FLOAT | SPLIT_FULL_LIGHT)
     t1 = time.perf_counter()
-    orc.alias_sample(table, s_sample, 7, rng=RNG_PHILOX4X32_10, nthreads=nthreads)
+    orc.alias_sample(table, s, 7, rng=RNG_PHILOX4X32_10, nthreads=nthreads)
     t2 = time.perf_counter()
-    t_step = (t1 - t0) + (t2 - t1) * (s / s_sample)
-    return t_step, {"build_s": t1 - t0, "sample_s": t2 - t1, "samples_timed": s_sample}
+    return t2 - t0, {"build_s": t1 - t0, "sample_s": t2 - t1}
 
 
-def cpu_kind() -> str:
-    from oracle.oracle import Reference
-    return "reference" if Reference.available() else "port"
+def reference_cpu(w_host, split_size: int = 32) -> dict:
+    """The reference's own CPU code (oracle/_ref, compiled from its sources where the
+    reference checkout is present), single-threaded as it is written: the PSA alias table
+    host::reference::pmr::psa_alias_table at split size 32 (src/host/reference/
+    psa_alias_table.hpp:23-67) and the Kahan prefix_sum (src/host/reference/prefix_sum.hpp:
+    17-74), beside the oracle port's single-thread PSA build of the same weights at the same
+    split size.  The reference has no sampler on the host, so samples/s is the port's only."""
+    from oracle.oracle import Oracle, Reference
+    if not Reference.available():
+        return {"unavailable": "oracle/_ref (the reference's CPU code, compiled from the "
+                               "reference checkout) is not built on this machine; the "
+                               "reference checkout is not present here"}
+    ref, orc = Reference(), Oracle()
+    n = w_host.size
+    t0 = time.perf_counter()
+    ref.psa_alias_table(w_host, max(1, n // split_size))
+    t1 = time.perf_counter()
+    ref.prefix_sum(w_host)
+    t2 = time.perf_counter()
+    orc.psa_build(w_host, split_size, nthreads=1)
+    t3 = time.perf_counter()
+    return {"kind": "reference", "cores": 1, "N": n, "split_size": split_size,
+            "psa_alias_table_s": t1 - t0, "alias_builds_per_s": 1.0 / (t1 - t0),
+            "kahan_prefix_sum_s": t2 - t1, "weights_scanned_per_s": n / (t2 - t1),
+            "port_psa_build_s_1thread": t3 - t2}
 
 
 def run_reference(args) -> None:
-    """--impl reference: the reference path's CPU implementation on all host cores."""
+    """--impl reference: the reference path's CPU implementation on all host cores; every step
+    is one whole step of the workload (PSA build of N weights + S samples), timed."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import numpy as np
     import torch
     n, s = 1 << args.log2n, 1 << args.log2s
     nthreads = cpu_threads()
     dev = "cuda" if torch.cuda.is_available() else "cpu"
     hosts = [make_weights(d, n, SEEDS[d], dev).cpu().numpy() for d in range(3)]
-    s_sample = 1 << min(args.log2s, 25)
     for k in range(args.warmup):
-        cpu_step(hosts[k % 3], n, s, nthreads, s_sample)
+        cpu_step(hosts[k % 3], n, s, nthreads)
     times, descs = [], []
+    t_run = time.perf_counter()
     for k in range(args.steps):
-        t, d = cpu_step(hosts[k % 3], n, s, nthreads, s_sample)
+        t, d = cpu_step(hosts[k % 3], n, s, nthreads)
         times.append(t)
         descs.append(d)
+    t_run = time.perf_counter() - t_run
     total = sum(times)
     value = args.steps * s / total
-    kind = "port"  # the oracle's restatement; the reference's CPU code has no sampler API
+    # the timed step is the oracle's port: the reference's own CPU code (reference_cpu below,
+    # where it is built) has a PSA build and a scan but no sampler
+    kind = "port"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "samples/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -253,12 +269,17 @@ def run_reference(args) -> None:
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": headline_config(n, s, args.gpus),
         "cpu_baseline": {"value": value, "unit": "samples/s", "cores": nthreads, "kind": kind,
-                         "sample": f"per step: full PSA build of N=2^{args.log2n} + "
-                                   f"{s_sample} alias samples timed, sampling extrapolated to "
-                                   f"S=2^{args.log2s}; {nthreads} threads"},
+                         "sample": f"every step whole: PSA build of N=2^{args.log2n} (split "
+                                   f"{SPLIT_SIZE}, float-float split) + S=2^{args.log2s} "
+                                   f"Philox4x32-10 alias samples, the three distributions in "
+                                   f"turn; {nthreads} threads (the oracle's threaded port of "
+                                   "the path: the reference's CPU code has no sampler)"},
         "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "cpu_build_s_mean": statistics.mean(d["build_s"] for d in descs),
+        "cpu_sample_s_mean": statistics.mean(d["sample_s"] for d in descs),
+        "timed_wall_s": t_run,
+        "reference_cpu": reference_cpu(hosts[0]),
     }
     print(json.dumps(line), flush=True)
 
@@ -514,6 +535,11 @@ def main() -> None:
                           "split_overlap_beyond_window": bool(dev_status & W.DEVICE_NONMONOTONE_SPLIT)},
     }
 
+    # every distribution of the configuration: its kernels timed alone and the statistics of
+    # its alias and ITS samples
+    dists = per_distribution(W, wrs, internals, weights, samples, n, s, stream, pk["hbm_gbs"])
+    line["statistics"] = {name: row["alias_statistics"] for name, row in dists.items()}
+    line["per_distribution"] = dists
     if not args.no_extras:
         line["kernels"] = kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s,
                                            stream, pk["hbm_gbs"], args)
@@ -528,13 +554,15 @@ def main() -> None:
         line["precision"] = precision_leg(W, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         w0 = weights[0].cpu().numpy()
-        s_sample = 1 << min(args.log2s, 25)
-        t_step, desc = cpu_step(w0, n, s, 1, s_sample)
+        nthreads = cpu_threads()
+        t_step, desc = cpu_step(w0, n, s, nthreads)
         line["cpu_baseline"] = {
-            "value": s / t_step, "unit": "samples/s", "cores": 1, "kind": "port",
-            "sample": f"PSA build of N=2^{args.log2n} uniform weights ({desc['build_s']:.2f} s) "
-                      f"+ {s_sample} alias samples ({desc['sample_s']:.2f} s), sampling "
-                      f"extrapolated to S=2^{args.log2s}; 1 thread"}
+            "value": s / t_step, "unit": "samples/s", "cores": nthreads, "kind": "port",
+            "sample": f"one whole step, nothing extrapolated: PSA build of N=2^{args.log2n} "
+                      f"uniform weights ({desc['build_s']:.2f} s) + S=2^{args.log2s} "
+                      f"Philox4x32-10 alias samples ({desc['sample_s']:.2f} s); {nthreads} "
+                      "threads (the oracle's threaded port of the path)",
+            "reference_cpu": reference_cpu(w0)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -669,20 +697,58 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int, cpu: bool = True) 
         per_call_pass()
     e1.record(stream)
     torch.cuda.synchronize()
-    per_call_ms = e0.elapsed_time(e1) / steps
+    per_call_py_ms = e0.elapsed_time(e1) / steps
     assert internals.status() == 0
+    # the same per-call loop driven from C++ through include/wrs.hpp (libwrs_percall.so):
+    # the primary per-call arm, with no interpreter between the calls
+    import ctypes as C
+    drv = C.CDLL(os.path.join(os.path.dirname(W.LIB_PATH), "libwrs_percall.so"))
+    drv.wrs_percall_run.restype = C.c_int
+    drv.wrs_percall_run.argtypes = [C.POINTER(W._Config), C.c_void_p, C.c_uint32, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                    C.POINTER(C.c_float)]
+    arr_w = (C.c_void_p * D)(*[c[0] for c in calls])
+    arr_n = (C.c_uint32 * D)(*[c[1] for c in calls])
+    arr_s = (C.c_uint64 * D)(*[c[2] for c in calls])
+    arr_seed = (C.c_uint64 * D)(*[c[3] for c in calls])
+    arr_out = (C.c_void_p * D)(*[c[4] for c in calls])
+    ccfg = cfg.c()
+    ms = C.c_float(0.0)
+    args_c = (C.byref(ccfg), stream.cuda_stream, D, arr_w, arr_n, arr_s, arr_seed, arr_out)
+    W.check(drv.wrs_percall_run(*args_c, warmup, C.byref(ms)))
+    W.check(drv.wrs_percall_run(*args_c, steps, C.byref(ms)))
+    per_call_ms = ms.value / steps
 
     # accuracy: both arms bit for bit, and the RMSE of each distribution's histogram
     identical = bool(torch.equal(out_b, out_p))
-    rmse = []
+    # per distribution: the reference's chi-square over its items (df = items - 1) with its
+    # p-value, the RMSE of the normalised histogram and the RMSE a multinomial draw has in
+    # expectation; aggregated as the sum of the chi-squares over the sum of the dfs
+    rmse, rmse_ratio, chi2s, dfs, pvals, bchi2, bdfs, bpvals = [], [], [], [], [], [], [], []
     for d in range(D):
         n, s = int(sizes[d]), int(counts[d])
         if s == 0:
             continue
         smp = out_b[int(s_off[d]):int(s_off[d]) + s].long()
-        hist = torch.bincount(smp, minlength=n).double() / s
+        o = torch.bincount(smp, minlength=n).double()
         wd = w[int(w_off[d]):int(w_off[d]) + n].double()
-        rmse.append(float(torch.sqrt(torch.mean((hist - wd / wd.sum()) ** 2))))
+        p = wd / wd.sum()
+        e = p * s
+        pos = e > 0
+        chi2 = float((((o - e) ** 2)[pos] / e[pos]).sum())
+        r = float(torch.sqrt(torch.mean((o / s - p) ** 2)))
+        rmse.append(r)
+        rmse_ratio.append(r / float(torch.sqrt(torch.mean(p * (1 - p) / s))))
+        chi2s.append(chi2)
+        dfs.append(int(pos.sum()) - 1)
+        pvals.append(chi2_report(chi2, dfs[-1])["p_value"])
+        b = binned_chi2(o, e, 256.0)
+        if b["df"] > 0:
+            bchi2.append(b["chi2"])
+            bdfs.append(b["df"])
+            bpvals.append(b["p_value"])
+    pv = [x for x in pvals if x is not None]
+    bpv = [x for x in bpvals if x is not None]
     total_s = int(counts.sum())
     return {
         "workload": f"batched mixed sizes: {D} distributions, N log-uniform in [64, 2^20] "
@@ -699,11 +765,34 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int, cpu: bool = True) 
         "per_call_samples_per_s": total_s / (per_call_ms / 1e3),
         "builds_per_s": D / (batched_ms / 1e3),
         "speedup_vs_per_call": per_call_ms / batched_ms,
+        "per_call_python_ms": per_call_py_ms,
+        "speedup_vs_per_call_python": per_call_py_ms / batched_ms,
         "graph_launches": 5, "per_call_launches": 5 * D,
         "samples_bitwise_equal": identical,
         "rmse_mean": statistics.mean(rmse), "rmse_max": max(rmse),
-        "per_call_driver": "Python loop over the C ABI (wrs_build + wrs_sample_at per "
-                           "distribution), one reused buffers object",
+        "statistics": {
+            **chi2_report(sum(chi2s), sum(dfs)),
+            "what": "sum over the distributions of the reference's chi-square (its items with "
+                    "nonzero expectation, df = items - 1 each) and its p-value; per "
+                    "distribution p-values summarised",
+            "rmse_mean": statistics.mean(rmse),
+            "rmse_over_ideal_mean": statistics.mean(rmse_ratio),
+            "rmse_over_ideal_max": max(rmse_ratio),
+            "p_value_min": min(pv) if pv else None,
+            "p_below_0.01_fraction": (sum(x < 0.01 for x in pv) / len(pv)) if pv else None,
+            "distributions": len(chi2s),
+            "binned": {**chi2_report(sum(bchi2), sum(bdfs)),
+                       "what": "per distribution the chi-square over bins of consecutive items "
+                               "with a mean expectation of >= 256 samples (a distribution "
+                               "that fills one bin has none), summed",
+                       "distributions": len(bchi2),
+                       "p_below_0.01_fraction": (sum(x < 0.01 for x in bpv) / len(bpv))
+                       if bpv else None}},
+        "per_call_driver": "C++ loop over the C++ facade of include/wrs.hpp (wrs::WRS::build + "
+                           "sample per distribution, one reused wrs::WRSBuffers; "
+                           "libwrs_percall.so, CUDA events around the loop); "
+                           "per_call_python_ms: the same calls from a Python loop over the "
+                           "C ABI",
         "cpu_baseline": cpu_batch_baseline(
             [(w[int(w_off[d]):int(w_off[d]) + int(sizes[d])], int(counts[d]), seeds[d])
              for d in range(D)], total_s, "distributions", split_size=cfg.split_size)
@@ -755,12 +844,28 @@ def served_leg(W, cfg, dev, n_requests: int = SERVED_REQUESTS) -> dict:
     tab = torch.empty(2 * int(wl["n"].max()), dtype=torch.int32, device=dev)
     alone = torch.empty(int(wl["s"].max()), dtype=torch.int32, device=dev)
     equal = 0
+    chi2s, dfs, ratios, bchi2, bdfs = [], [], [], [], []
     for i in pick:
         n, s_i = int(wl["n"][i]), int(wl["s"][i])
         batch.set(None, [(wp + 4 * int(wl["w_off"][i]), tab, alone, n, s_i, int(wl["seeds"][i]))])
         batch.build(None)
         batch.sample(None)
-        equal += bool(torch.equal(alone[:s_i], out[int(s_off[i]):int(s_off[i]) + s_i]))
+        served_i = out[int(s_off[i]):int(s_off[i]) + s_i]
+        equal += bool(torch.equal(alone[:s_i], served_i))
+        # the served samples against the request's weights
+        o = torch.bincount(served_i.long(), minlength=n).double()
+        p = w[int(wl["w_off"][i]):int(wl["w_off"][i]) + n].double()
+        p = p / p.sum()
+        e = p * s_i
+        pos = e > 0
+        chi2s.append(float((((o - e) ** 2)[pos] / e[pos]).sum()))
+        dfs.append(int(pos.sum()) - 1)
+        b = binned_chi2(o, e, 64.0)
+        if b["df"] > 0:
+            bchi2.append(b["chi2"])
+            bdfs.append(b["df"])
+        ratios.append(float(torch.sqrt(torch.mean((o / s_i - p) ** 2))) /
+                      float(torch.sqrt(torch.mean(p * (1 - p) / s_i))))
     return {
         "workload": f"served request stream: {n_requests} build+sample requests, Poisson "
                     f"arrivals at {SERVED_RATE:.0f} req/s, N log-uniform in [256, 2^22] "
@@ -776,6 +881,19 @@ def served_leg(W, cfg, dev, n_requests: int = SERVED_REQUESTS) -> dict:
         "evictions": st["evictions"], "table_bytes_peak": st["table_bytes_peak"],
         "scratch_bytes": st["scratch_bytes"], "device_status": st["device_status"],
         "alone_vs_mix_equal": f"{equal}/{len(pick)}",
+        "statistics": {
+            **chi2_report(sum(chi2s), sum(dfs)),
+            "what": f"the {len(pick)} alone-vs-mix requests' served samples: sum of the "
+                    "reference's chi-squares over their items (df = items - 1 each) and its "
+                    "p-value (most requests draw far fewer samples than they have items, so "
+                    "the RMSE ratio is the sharper check)",
+            "rmse_over_ideal_mean": statistics.mean(ratios),
+            "rmse_over_ideal_max": max(ratios),
+            "binned": {**chi2_report(sum(bchi2), sum(bdfs)),
+                       "what": "per request the chi-square over bins of consecutive items with "
+                               "a mean expectation of >= 64 samples (requests of fewer samples "
+                               "fill one bin and have none), summed",
+                       "requests": len(bchi2)}},
         "cpu_baseline": cpu_batch_baseline(
             [(w[int(wl["w_off"][i]):int(wl["w_off"][i]) + int(wl["n"][i])], int(wl["s"][i]),
               int(wl["seeds"][i])) for i in range(n_requests)], total_s, "requests",
@@ -811,12 +929,7 @@ def precision_leg(W, dev, log2n: int = 28, log2s: int = 30) -> dict:
     indices must never be drawn."""
     import torch
     n, s = 1 << log2n, 1 << log2s
-    g = torch.Generator(device=dev)
-    g.manual_seed(5)
-    w = torch.exp(3.0 * torch.randn(n, generator=g, device=dev, dtype=torch.float32))
-    w[torch.rand(n, generator=g, device=dev) < 0.01] = 0.0
-    big = torch.rand(n, generator=g, device=dev) < 1e-4
-    w[big] = (w[big].double() * 1e6).float()
+    w = importlib.import_module("merian-wrs_gb300.workloads").precision(n, dev)
     ref = torch.cumsum(w.double(), 0)
     pos = ref > 0
     total = float(ref[-1])
@@ -838,9 +951,10 @@ def precision_leg(W, dev, log2n: int = 28, log2s: int = 30) -> dict:
         if prec == W.SCAN_COMPENSATED:
             samples = torch.empty(s, dtype=torch.int32, device=dev)
             its.its_sample(None, cmf, n, s, 11, 0, samples)
-            r = stats(None, samples, s, w)
+            r = sample_statistics(stats, samples, s, w, n)
             scans[name]["its_rmse"] = r["rmse"]
             scans[name]["its_zero_weight_draws"] = r["zero_weight_draws"]
+            scans[name]["its_statistics"] = r
             del samples
         del internals
     out["scan"] = scans
@@ -861,11 +975,13 @@ def precision_leg(W, dev, log2n: int = 28, log2s: int = 30) -> dict:
         _dev_copy(table_t, internals.views()["alias_table"], 8 * n)
         imp = _implied(table_t, n)
         err = (imp - mean_units).abs()
-        r = stats(None, samples, s, w)
+        r = sample_statistics(stats, samples, s, w, n)
         tables[name] = {"max_abs_err_mean_units": float(err.max()),
                         "max_rel_err_w_ge_mean": float((err / mean_units)[mean_units >= 1].max()),
-                        "alias_rmse": r["rmse"], "chi2": r["chi2"],
+                        "alias_rmse": r["rmse"], "chi2": r["chi2"], "df": r["df"],
+                        "p_value": r["p_value"], "z_score": r["z_score"], "binned": r["binned"],
                         "zero_weight_draws": r["zero_weight_draws"],
+                        "zero_weight_mass": float(imp[w == 0].sum()),
                         "status": internals.status()}
         del internals, samples, table_t, imp, err
         torch.cuda.empty_cache()
@@ -918,14 +1034,7 @@ def small_leg(W, dev, steps: int = 20) -> dict:
     torch.cuda.synchronize()
     graph_build_s = e[0].elapsed_time(e[1]) / (steps * per_graph) / 1e3
     assert bufs.internals.status() == 0
-    st = W.Statistics(n)(stream, samples, s, w)  # on-device histogram, chi-square, RMSE
-    p = w.double().cpu().numpy()
-    p /= p.sum()
-    try:
-        from scipy.stats import chi2 as chi2_dist
-        pval = float(chi2_dist.sf(st["chi2"], n - 1))
-    except ImportError:
-        pval = None
+    st = sample_statistics(W.Statistics(n), samples, s, w, n)  # histogram etc. on the device
     return {"workload": "plain path, small: N=65,536 uniform(0,1] (seed 1), PSA build (split 2) "
                         "+ S=2^20 Philox4x32-10 samples (seed 1)",
             "builds_per_s": 1.0 / build_s, "samples_per_s": s / sample_s,
@@ -933,9 +1042,67 @@ def small_leg(W, dev, steps: int = 20) -> dict:
             "graph_builds_per_s": 1.0 / graph_build_s, "graph_build_us": graph_build_s * 1e6,
             "graph_note": "per-call builds from a Python loop over the C ABI include the host's "
                           "launch gaps; graph_* replays 8 builds captured in one CUDA graph",
-            "chi2": st["chi2"], "df": n - 1, "p_value": pval, "rmse": st["rmse"],
-            "rmse_ideal": float(np.sqrt(np.mean(p * (1 - p) / s))),
+            "chi2": st["chi2"], "df": st["df"], "p_value": st["p_value"],
+            "z_score": st["z_score"], "rmse": st["rmse"], "rmse_ideal": st["rmse_ideal"],
+            "zero_weight_draws": st["zero_weight_draws"], "binned": st["binned"],
             "statistics": "wrs_histogram + wrs_sample_statistics on the device"}
+
+
+def chi2_report(chi2: float, df: int) -> dict:
+    """The chi-square statistic with its degrees of freedom, upper-tail p-value (scipy) and the
+    reference's z-score (chi2 - df) / sqrt(2 df) (src/host/statistics/chi_square.hpp:11-15)."""
+    try:
+        from scipy.stats import chi2 as chi2_dist
+        p = float(chi2_dist.sf(chi2, df)) if df > 0 else None
+    except ImportError:
+        p = None
+    return {"chi2": chi2, "df": df, "p_value": p,
+            "z_score": (chi2 - df) / math.sqrt(2.0 * df) if df > 0 else None}
+
+
+def binned_chi2(o, e, target: float) -> dict:
+    """Chi-square over bins of G consecutive items (device tensors o: observed counts, e:
+    expected counts), G the smallest power of two whose mean expected count per bin is at
+    least `target`: the chi-square distribution describes the statistic only where expected
+    counts are large, which item by item they are not for skewed weights.  Bins with no
+    expectation are left out; df = bins - 1."""
+    import torch
+    n = int(e.numel())
+    mean_e = float(e.sum()) / max(n, 1)
+    G = 1
+    while G < n and G * mean_e < target:
+        G *= 2
+    pad = (-n) % G
+    if pad:
+        o = torch.cat([o, o.new_zeros(pad)])
+        e = torch.cat([e, e.new_zeros(pad)])
+    O = o.view(-1, G).sum(1)
+    E = e.view(-1, G).sum(1)
+    keep = E > 0
+    chi2 = float((((O - E) ** 2)[keep] / E[keep]).sum())
+    bins = int(keep.sum())
+    return {**chi2_report(chi2, bins - 1), "bin_items": G,
+            "min_expected": float(E[keep].min()) if bins else None}
+
+
+def sample_statistics(stats, samples, s: int, w, n: int, bin_target: float = 1024.0) -> dict:
+    """Statistics of s samples of the n weights w (device tensors): the on-device histogram,
+    chi-square and RMSE (wrs_histogram + wrs_sample_statistics) -- the reference's chi_square
+    over the items with nonzero expectation (src/host/statistics/chi_square.hpp:17-37), df =
+    those items - 1, and its RMSE of the normalised histogram (src/dep/eval/rms.hpp:44-63) --
+    with the RMSE a multinomial draw of s samples has in expectation (rmse_ideal), and the
+    binned chi-square (binned_chi2), whose p-value holds where items' expected counts are
+    small."""
+    import torch
+    r = stats(None, samples, s, w)
+    w64 = w[:n].double()
+    total = w64.sum()
+    p = w64 / total
+    out = chi2_report(r["chi2"], int((w64 > 0).sum()) - 1)
+    out.update({"rmse": r["rmse"], "rmse_ideal": float(torch.sqrt(torch.mean(p * (1 - p) / s))),
+                "zero_weight_draws": r["zero_weight_draws"],
+                "binned": binned_chi2(stats.hist[:n].double(), p * s, bin_target)})
+    return out
 
 
 def host_link_rates(host_s, dev_s, host_w, dev_w, stream) -> dict:
@@ -977,6 +1144,68 @@ def random_gather_rate(W, internals, n: int, s: int, stream) -> float:
     e1.record(stream)
     torch.cuda.synchronize()
     return s / (e0.elapsed_time(e1) / 3 / 1e3)
+
+
+def _timed(stream, fn, reps: int = 5) -> float:
+    """Seconds per call of fn: CUDA events on `stream` around reps calls after 2 warm-up
+    calls."""
+    import torch
+    for _ in range(2):
+        fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps / 1e3
+
+
+def per_distribution(W, wrs, internals, weights, samples, n: int, s: int, stream,
+                     peak: float) -> dict:
+    """The single large distribution on each of its three shapes: the headline step's PSA
+    build and alias sampling, the decoupled scan (exact and FP32 carries), ITS (build = scan +
+    cell blocks; compensated CMF, and the FP32 CMF of the reference's precision) and Cutpoint
+    (entry 128, compensated CMF), each timed alone (CUDA events, mean of 5 calls after 2
+    warm-up calls), with the statistics of the alias and ITS samples against the weights."""
+    import torch
+    stats = W.Statistics(n)
+    its = W.WRS(W.ITSConfig(rng=W.RNG_PHILOX4X32_10, scan_precision=W.SCAN_COMPENSATED))
+    its32 = W.WRS(W.ITSConfig(rng=W.RNG_PHILOX4X32_10))
+    cp = W.WRS(W.CutpointConfig(128, rng=W.RNG_PHILOX4X32_10,
+                                scan_precision=W.SCAN_COMPENSATED))
+    its_int, its32_int, cp_int = (W.Internals(h.handle, n) for h in (its, its32, cp))
+    cmf = torch.empty(n, dtype=torch.float32, device=weights[0].device)
+    out = {}
+    for d, name in enumerate(DISTS):
+        w = weights[d]
+        row = {}
+        ab = W.WRSBuffers(w, samples, internals)
+        row["alias_build_ms"] = _timed(stream, lambda: wrs.build(stream, ab, n)) * 1e3
+        row["alias_builds_per_s"] = 1e3 / row["alias_build_ms"]
+        row["alias_build_frac"] = 32.0 * n / (row["alias_build_ms"] / 1e3) / 1e9 / peak
+        row["alias_sample_ms"] = _timed(stream, lambda: wrs.sample(stream, ab, n, s,
+                                                                   seed=1234 + d)) * 1e3
+        row["alias_samples_per_s"] = s / (row["alias_sample_ms"] / 1e3)
+        row["alias_statistics"] = sample_statistics(stats, samples, s, w, n)
+        for key, h, hi in (("scan", its, its_int), ("scan_fp32", its32, its32_int)):
+            sec = _timed(stream, lambda: h.prefix_sum(stream, w, n, cmf, hi))
+            row[f"{key}_ms"] = sec * 1e3
+            row[f"{key}_weights_per_s"] = n / sec
+            row[f"{key}_frac"] = 8.0 * n / sec / 1e9 / peak
+        for key, h, hi in (("its", its, its_int), ("its_fp32", its32, its32_int),
+                           ("cutpoint", cp, cp_int)):
+            b = W.WRSBuffers(w, samples, hi)
+            row[f"{key}_build_ms"] = _timed(stream, lambda: h.build(stream, b, n)) * 1e3
+            sec = _timed(stream, lambda: h.sample(stream, b, n, s, seed=99))
+            row[f"{key}_sample_ms"] = sec * 1e3
+            row[f"{key}_samples_per_s"] = s / sec
+            if key == "its":
+                row["its_statistics"] = sample_statistics(stats, samples, s, w, n)
+        for hi in (internals, its_int, its32_int, cp_int):
+            assert not hi.status() & W.DEVICE_TIMEOUT
+        out[name] = row
+    return out
 
 
 def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, peak, args):

@@ -3,7 +3,9 @@
 Each translation unit is compiled in parallel with
     nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo -Xcompiler -fPIC
 and linked into merian-wrs_gb300/libwrs_gb300.so.  Objects go to merian-wrs_gb300/_build/.
-Rebuilds only what changed (by mtime against sources and headers).
+Rebuilds only what changed (by mtime against sources and headers).  The benchmark's C++
+per-call driver (percall_driver.cpp, host code over include/wrs.hpp) is linked against it as
+merian-wrs_gb300/libwrs_percall.so.
 """
 from __future__ import annotations
 
@@ -19,6 +21,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libwrs_gb300.so")
+DRIVER_SRC = os.path.join(PKG, "percall_driver.cpp")
+DRIVER_LIB = os.path.join(PKG, "libwrs_percall.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
@@ -65,6 +69,13 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    if _stale(DRIVER_LIB, [DRIVER_SRC, LIB] + _headers()):
+        cmd = [nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-I",
+               os.path.join(ROOT, "include"), DRIVER_SRC, "-o", DRIVER_LIB, "-L", PKG,
+               "-lwrs_gb300", "-lcudart", "-Xlinker", "-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"per-call driver build failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
         print(LIB)
     return LIB
