@@ -93,7 +93,10 @@ def parse_args():
     p.add_argument("--log2n", type=int, default=LOG2_N)
     p.add_argument("--log2s", type=int, default=LOG2_S)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--no-extras", action="store_true", help="skip the per-kernel breakdown")
+    p.add_argument("--l2-fetch", type=int, default=None,
+                   help="set the context's L2 fetch granularity (bytes) instead of tuning it")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the per-distribution rows, statistics and per-kernel breakdown")
     p.add_argument("--no-batched", action="store_true",
                    help="skip the batched mixed-size configuration (4096 distributions)")
     p.add_argument("--no-served", action="store_true",
@@ -104,6 +107,8 @@ def parse_args():
                    help="skip the precision study (N = 2^28, S = 2^30)")
     p.add_argument("--batched-only", action="store_true",
                    help="only run the batched configuration and print its object (profiling)")
+    p.add_argument("--small-only", action="store_true",
+                   help="only run the plain small configuration and print its object")
     p.add_argument("--probe-gather", action="store_true",
                    help="only measure the random-gather rate per load width and exit")
     return p.parse_args()
@@ -118,12 +123,15 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def profiled_traffic() -> float | None:
-    """DRAM bytes per alias-sampling launch from the committed ncu summary, if present."""
+def profiled_traffic(l2_fetch: int) -> float | None:
+    """DRAM bytes of one headline alias-sampling launch at the given L2 fetch granularity,
+    from the committed ncu summary (a line `dram_bytes_per_launch[l2=B]: X` per granularity),
+    if it holds that granularity."""
     if not os.path.exists(PROFILE_TRAFFIC):
         return None
+    key = f"dram_bytes_per_launch[l2={l2_fetch}]:"
     for line in open(PROFILE_TRAFFIC):
-        if line.strip().startswith("dram_bytes_per_launch:"):
+        if line.strip().startswith(key):
             return float(line.split(":", 1)[1].split()[0])
     return None
 
@@ -344,6 +352,9 @@ def main() -> None:
     wrs = W.WRS(cfg)
     stream = torch.cuda.current_stream()
     dev = torch.device("cuda", local)
+    if args.small_only:
+        print(json.dumps({"small": small_leg(W, dev)}))
+        return
     if args.batched_only:
         print(json.dumps({"batched": batched_leg(W, cfg, dev, stream, max(3, args.steps // 2),
                                                  max(3, args.warmup),
@@ -356,8 +367,12 @@ def main() -> None:
 
     # the context's L2 fetch granularity, tuned live on the first distribution (the split
     # size stays fixed); it changes no result
-    tune = W.autotune_alias(cfg, stream, weights[0], n, s, samples, split_sizes=[],
-                            l2_fetch=None, warmup=1, reps=2)
+    if args.l2_fetch is None:
+        tune = W.autotune_alias(cfg, stream, weights[0], n, s, samples, split_sizes=[],
+                                l2_fetch=None, warmup=1, reps=2)
+    else:
+        W.set_l2_fetch_granularity(args.l2_fetch)
+        tune = {"l2_fetch": W.get_l2_fetch_granularity(), "trials": []}
 
     def step(k: int, ev=None):
         b = bufs[k % 3]
@@ -490,10 +505,14 @@ def main() -> None:
     pk = peaks()
     samp_s = statistics.mean(sample_ms) / 1e3
     achieved = 12.0 * s / samp_s / 1e9
-    traffic = profiled_traffic()
+    traffic = profiled_traffic(tune["l2_fetch"])
     gather_rate = random_gather_rate(W, internals, n, s, stream)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+                "traffic_l2_fetch": tune["l2_fetch"],
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                  "headline launch at this run's L2 fetch granularity "
+                                  "(profiles/alias_sample_n26_s28.md)",
                 "kernel": "k_alias_sample", "bytes_model": "12 B/sample (8 B entry + 4 B index)",
                 "peak_source": pk["source"],
                 "sector_model_frac": (36.0 * s / samp_s / 1e9) / pk["hbm_gbs"],
@@ -537,10 +556,11 @@ def main() -> None:
 
     # every distribution of the configuration: its kernels timed alone and the statistics of
     # its alias and ITS samples
-    dists = per_distribution(W, wrs, internals, weights, samples, n, s, stream, pk["hbm_gbs"])
-    line["statistics"] = {name: row["alias_statistics"] for name, row in dists.items()}
-    line["per_distribution"] = dists
     if not args.no_extras:
+        dists = per_distribution(W, wrs, internals, weights, samples, n, s, stream,
+                                 pk["hbm_gbs"])
+        line["statistics"] = {name: row["alias_statistics"] for name, row in dists.items()}
+        line["per_distribution"] = dists
         line["kernels"] = kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s,
                                            stream, pk["hbm_gbs"], args)
     if not args.no_batched:
@@ -951,7 +971,7 @@ def precision_leg(W, dev, log2n: int = 28, log2s: int = 30) -> dict:
         if prec == W.SCAN_COMPENSATED:
             samples = torch.empty(s, dtype=torch.int32, device=dev)
             its.its_sample(None, cmf, n, s, 11, 0, samples)
-            r = sample_statistics(stats, samples, s, w, n)
+            r = sample_statistics(stats, samples, s, w, n, bin_target=8192.0)
             scans[name]["its_rmse"] = r["rmse"]
             scans[name]["its_zero_weight_draws"] = r["zero_weight_draws"]
             scans[name]["its_statistics"] = r
@@ -975,7 +995,7 @@ def precision_leg(W, dev, log2n: int = 28, log2s: int = 30) -> dict:
         _dev_copy(table_t, internals.views()["alias_table"], 8 * n)
         imp = _implied(table_t, n)
         err = (imp - mean_units).abs()
-        r = sample_statistics(stats, samples, s, w, n)
+        r = sample_statistics(stats, samples, s, w, n, bin_target=8192.0)
         tables[name] = {"max_abs_err_mean_units": float(err.max()),
                         "max_rel_err_w_ge_mean": float((err / mean_units)[mean_units >= 1].max()),
                         "alias_rmse": r["rmse"], "chi2": r["chi2"], "df": r["df"],

@@ -95,6 +95,7 @@ __global__ __launch_bounds__(kTileThreads) void k_total_mass(const float* __rest
                                                              double* __restrict__ partials,
                                                              BuildCtrl* __restrict__ ctrl_in,
                                                              BatchView bv) {
+    pdl_entry();
     __shared__ double s_red[kTileWarps];
     __shared__ ff s_part[kTileWarps];
     __shared__ bool s_last;
@@ -157,7 +158,7 @@ __global__ __launch_bounds__(kTileThreads) void k_total_mass(const float* __rest
 
 cudaError_t launch_total_mass(cudaStream_t st, const float* w, uint32_t n, double* partials,
                               BuildCtrl* ctrl) {
-    k_total_mass<false><<<tiles_for(n), kTileThreads, 0, st>>>(w, n, partials, ctrl, BatchView{});
+    launch_pdl(k_total_mass<false>, tiles_for(n), kTileThreads, 0, st, w, n, partials, ctrl, BatchView{});
     return cudaGetLastError();
 }
 
@@ -393,6 +394,7 @@ struct PartArgs {
 template <bool COMP, bool FFOUT, bool BATCH, bool BW = false>
 __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partition(PartArgs a,
                                                                                    BatchView bv) {
+    pdl_entry();
     // warp totals (phase A), turned into warp-exclusive offsets by warp 0 (phase B)
     __shared__ uint32_t s_wc[kTileWarps];
     __shared__ float s_wh[kTileWarps], s_wl[kTileWarps];  // local FP32 sums (!FFOUT)
@@ -717,11 +719,11 @@ template <bool BATCH>
 static void part_dispatch(cudaStream_t st, uint32_t precision, uint32_t grid, const PartArgs& a,
                           const BatchView& bv) {
     if (precision == 2)
-        k_prefix_partition<true, true, BATCH><<<grid, kTileThreads, 0, st>>>(a, bv);
+        launch_pdl(k_prefix_partition<true, true, BATCH>, grid, kTileThreads, 0, st, a, bv);
     else if (precision == 1)
-        k_prefix_partition<true, false, BATCH><<<grid, kTileThreads, 0, st>>>(a, bv);
+        launch_pdl(k_prefix_partition<true, false, BATCH>, grid, kTileThreads, 0, st, a, bv);
     else
-        k_prefix_partition<false, false, BATCH><<<grid, kTileThreads, 0, st>>>(a, bv);
+        launch_pdl(k_prefix_partition<false, false, BATCH>, grid, kTileThreads, 0, st, a, bv);
 }
 
 cudaError_t launch_prefix_partition(cudaStream_t st, bool comp, const float* w, uint32_t n,
@@ -786,6 +788,7 @@ __global__ __launch_bounds__(kTileThreads) void k_scan_bulk(const float* __restr
                                                             ScanState* __restrict__ states,
                                                             uint32_t cap_tiles,
                                                             uint32_t spin_limit) {
+    pdl_entry();
     constexpr uint32_t kItems = kTileThreads * 4u * V;  // per tile
     constexpr uint32_t kWarpSpan = 128u * V;             // per warp
     extern __shared__ __align__(128) float s_tile[];     // kItems floats
@@ -938,6 +941,7 @@ __global__ __launch_bounds__(kTileThreads) void k_scan_exact(const float* __rest
                                                              ScanState* __restrict__ states,
                                                              uint32_t cap_tiles,
                                                              uint32_t spin_limit) {
+    pdl_entry();
     __shared__ float4 s_x[kTileItems / 4];  // the tile (park_slot), later its outputs
     __shared__ u128 s_e[kTileThreads];       // exact thread-exclusive sums within the warp
     __shared__ u128 s_wt[kTileWarps];        // exact warp totals -> warp-exclusive sums
@@ -1051,11 +1055,11 @@ cudaError_t launch_scan(cudaStream_t st, bool comp, const float* in, uint32_t n,
         // the exact carries need the distribution's fixed-point grid: its total mass first
         cudaError_t e = launch_total_mass(st, in, n, partials, ctrl);
         if (e != cudaSuccess) return e;
-        k_scan_exact<<<tiles, kTileThreads, 0, st>>>(in, n, out, ctrl, states, cap_tiles, spin_limit);
+        launch_pdl(k_scan_exact, tiles, kTileThreads, 0, st, in, n, out, ctrl, states, cap_tiles, spin_limit);
     } else {
         constexpr uint32_t items = kTileThreads * 4u * kScanBulkV;
         const uint32_t bulk_tiles = static_cast<uint32_t>((static_cast<uint64_t>(n) + items - 1) / items);
-        k_scan_bulk<false, kScanBulkV><<<bulk_tiles, kTileThreads, items * sizeof(float), st>>>(
+        launch_pdl(k_scan_bulk<false, kScanBulkV>, bulk_tiles, kTileThreads, items * sizeof(float), st, 
             in, n, out, ctrl, states, cap_tiles, spin_limit);
     }
     return cudaGetLastError();
@@ -1442,6 +1446,7 @@ struct SplitArgs {
 // (BATCH: one thread per split-pack CTA of the whole batch, each of its distribution)
 template <bool FF, bool BATCH>
 __global__ __launch_bounds__(256) void k_split_descent(SplitArgs a, BatchView bv) {
+    pdl_entry();
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;  // the split-pack CTA
     uint32_t blk = g, n = a.n;
     const BuildCtrl* ctrl = a.ctrl;
@@ -1482,6 +1487,7 @@ __global__ __launch_bounds__(256) void k_split_descent(SplitArgs a, BatchView bv
 // ownership window.
 template <bool R64, bool FF, bool BATCH, bool RECORDS = false>
 __global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, BatchView bv) {
+    pdl_entry();
     __shared__ uint32_t s_i[kSplitSlots], s_j[kSplitSlots];
     __shared__ float s_spill[kSplitSlots];
     const float* w = a.w;
@@ -1603,7 +1609,7 @@ template <bool R64, bool FF, bool BATCH, bool RECORDS>
 static void launch_split_kernel(cudaStream_t st, uint32_t grid, const SplitArgs& a,
                                 const BatchView& bv) {
     if (!a.stage) {
-        k_split_pack<R64, FF, BATCH, RECORDS><<<grid, kSplitThreads, 0, st>>>(a, bv);
+        launch_pdl(k_split_pack<R64, FF, BATCH, RECORDS>, grid, kSplitThreads, 0, st, a, bv);
         return;
     }
     // the attribute belongs to the current device's context: set it for every launch (a
@@ -1611,7 +1617,7 @@ static void launch_split_kernel(cudaStream_t st, uint32_t grid, const SplitArgs&
     cudaFuncSetAttribute(k_split_pack<R64, FF, BATCH, RECORDS>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(kPackWinBytes));
-    k_split_pack<R64, FF, BATCH, RECORDS><<<grid, kSplitThreads, kPackWinBytes, st>>>(a, bv);
+    launch_pdl(k_split_pack<R64, FF, BATCH, RECORDS>, grid, kSplitThreads, kPackWinBytes, st, a, bv);
 }
 
 template <bool BATCH>
@@ -1639,9 +1645,9 @@ cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const 
     // the extra launch pays off once there are several waves of split-pack CTAs
     if (descent && blocks >= kDescentMinBlocks) {
         if (prefix_lo)
-            k_split_descent<true, false><<<(blocks + 255u) / 256u, 256, 0, st>>>(a, BatchView{});
+            launch_pdl(k_split_descent<true, false>, (blocks + 255u) / 256u, 256, 0, st, a, BatchView{});
         else
-            k_split_descent<false, false><<<(blocks + 255u) / 256u, 256, 0, st>>>(a, BatchView{});
+            launch_pdl(k_split_descent<false, false>, (blocks + 255u) / 256u, 256, 0, st, a, BatchView{});
     }
     split_dispatch<false>(st, r64, prefix_lo != nullptr, blocks, a, BatchView{});
     return cudaGetLastError();
@@ -1666,6 +1672,7 @@ template <bool APPLY>
 __global__ __launch_bounds__(kTileThreads) void k_bw_scan(const float* __restrict__ in, uint32_t n,
                                                           float* __restrict__ out,
                                                           float* __restrict__ tile_val) {
+    pdl_entry();
     __shared__ float s_w[kTileWarps];
     const uint32_t tile = blockIdx.x;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1726,6 +1733,7 @@ __global__ __launch_bounds__(kTileThreads) void k_bw_part_reduce(const float* __
                                                                  uint32_t* __restrict__ tc,
                                                                  float* __restrict__ th,
                                                                  float* __restrict__ tl) {
+    pdl_entry();
     __shared__ uint32_t s_c[kTileWarps];
     __shared__ float s_h[kTileWarps], s_l[kTileWarps];
     const uint32_t tile = blockIdx.x;
@@ -1776,6 +1784,7 @@ constexpr int kBwThreads = 1024;
 __global__ __launch_bounds__(kBwThreads) void k_bw_tiles(uint32_t T, uint32_t* __restrict__ c,
                                                          float* __restrict__ h,
                                                          float* __restrict__ l) {
+    pdl_entry();
     __shared__ uint32_t s_c[32];
     __shared__ float s_h[32], s_l[32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1835,9 +1844,9 @@ __global__ __launch_bounds__(kBwThreads) void k_bw_tiles(uint32_t T, uint32_t* _
 cudaError_t launch_prefix_sum_blockwise(cudaStream_t st, const float* in, uint32_t n, float* out,
                                         float* tile_scratch) {
     const uint32_t T = tiles_for(n);
-    k_bw_scan<false><<<T, kTileThreads, 0, st>>>(in, n, out, tile_scratch);
-    k_bw_tiles<<<1, kBwThreads, 0, st>>>(T, nullptr, tile_scratch, nullptr);
-    k_bw_scan<true><<<T, kTileThreads, 0, st>>>(in, n, out, tile_scratch);
+    launch_pdl(k_bw_scan<false>, T, kTileThreads, 0, st, in, n, out, tile_scratch);
+    launch_pdl(k_bw_tiles, 1, kBwThreads, 0, st, T, nullptr, tile_scratch, nullptr);
+    launch_pdl(k_bw_scan<true>, T, kTileThreads, 0, st, in, n, out, tile_scratch);
     return cudaGetLastError();
 }
 
@@ -1849,12 +1858,12 @@ cudaError_t launch_prefix_partition_blockwise(cudaStream_t st, const float* w, u
     uint32_t* tc = tile_scratch;
     float* th = reinterpret_cast<float*>(tile_scratch + T);
     float* tl = reinterpret_cast<float*>(tile_scratch + 2 * static_cast<size_t>(T));
-    k_bw_part_reduce<<<T, kTileThreads, 0, st>>>(w, n, ctrl, tc, th, tl);
-    k_bw_tiles<<<1, kBwThreads, 0, st>>>(T, tc, th, tl);
+    launch_pdl(k_bw_part_reduce, T, kTileThreads, 0, st, w, n, ctrl, tc, th, tl);
+    launch_pdl(k_bw_tiles, 1, kBwThreads, 0, st, T, tc, th, tl);
     const PartArgs a{w,       n,        ctrl,     nullptr,  nullptr,   0u,
                      0u,      &ctrl->status, idx_out, prefix_out, elems_out, nullptr,
                      tc,      th,       tl};
-    k_prefix_partition<false, false, false, true><<<T, kTileThreads, 0, st>>>(a, BatchView{});
+    launch_pdl(k_prefix_partition<false, false, false, true>, T, kTileThreads, 0, st, a, BatchView{});
     return cudaGetLastError();
 }
 
@@ -1869,6 +1878,7 @@ cudaError_t launch_prefix_partition_blockwise(cudaStream_t st, const float* w, u
 // light: every record is the final one (the shader's bisection would underflow).
 template <bool R64, bool FF>
 __global__ __launch_bounds__(256) void k_split_records(SplitArgs a) {
+    pdl_entry();
     const uint32_t n = a.n;
     const uint32_t K = records_for(n, a.split_size);
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;  // record t: split k = t + 1
@@ -1893,11 +1903,11 @@ cudaError_t launch_split_records(cudaStream_t st, bool r64, bool full_light, con
     const uint32_t K = records_for(n, split_size);
     const uint32_t blocks = (K + 255u) / 256u;
     if (prefix_lo)
-        k_split_records<true, true><<<blocks, 256, 0, st>>>(a);
+        launch_pdl(k_split_records<true, true>, blocks, 256, 0, st, a);
     else if (r64)
-        k_split_records<true, false><<<blocks, 256, 0, st>>>(a);
+        launch_pdl(k_split_records<true, false>, blocks, 256, 0, st, a);
     else
-        k_split_records<false, false><<<blocks, 256, 0, st>>>(a);
+        launch_pdl(k_split_records<false, false>, blocks, 256, 0, st, a);
     return cudaGetLastError();
 }
 
@@ -1966,6 +1976,7 @@ __device__ __forceinline__ bool covered_later_warp(uint32_t li, uint32_t lj, uin
 }
 
 __global__ __launch_bounds__(256) void k_pack_records_warp(SplitArgs a) {
+    pdl_entry();
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // subproblem
     const uint32_t n = a.n;
@@ -2102,7 +2113,7 @@ cudaError_t launch_pack_records_warp(cudaStream_t st, bool full_light, const flo
                       nullptr, nullptr, status, split_size, full_light ? 1u : 0u,
                       const_cast<SplitRecord*>(records)};
     const uint64_t threads = static_cast<uint64_t>(records_for(n, split_size)) * 32u;
-    k_pack_records_warp<<<static_cast<unsigned>((threads + 255u) / 256u), 256, 0, st>>>(a);
+    launch_pdl(k_pack_records_warp, static_cast<unsigned>((threads + 255u) / 256u), 256, 0, st, a);
     return cudaGetLastError();
 }
 
@@ -2143,7 +2154,7 @@ cudaError_t launch_batch_maps(cudaStream_t st, const DistDesc* dist, uint32_t co
 // the distributions.
 cudaError_t launch_batch_build(cudaStream_t st, uint32_t precision, bool r64, const BatchView& b) {
     if (b.tiles == 0) return cudaSuccess;
-    k_total_mass<true><<<b.tiles, kTileThreads, 0, st>>>(nullptr, 0u, b.partials, nullptr, b);
+    launch_pdl(k_total_mass<true>, b.tiles, kTileThreads, 0, st, nullptr, 0u, b.partials, nullptr, b);
     const PartArgs pa{nullptr,    0u,       nullptr,  b.lb,   b.states,  b.cap_tiles,
                       kSpinLimit, b.status, b.idx,    b.prefix, b.elems, b.prefix_lo};
     part_dispatch<true>(st, precision, b.tiles, pa, b);
@@ -2152,9 +2163,9 @@ cudaError_t launch_batch_build(cudaStream_t st, uint32_t precision, bool r64, co
     if (b.descent && b.split_blocks) {
         const uint32_t g = (b.split_blocks + 255u) / 256u;
         if (precision == 2)
-            k_split_descent<true, true><<<g, 256, 0, st>>>(sa, b);
+            launch_pdl(k_split_descent<true, true>, g, 256, 0, st, sa, b);
         else
-            k_split_descent<false, true><<<g, 256, 0, st>>>(sa, b);
+            launch_pdl(k_split_descent<false, true>, g, 256, 0, st, sa, b);
     }
     split_dispatch<true>(st, r64, precision == 2, b.split_blocks, sa, b);
     return cudaGetLastError();

@@ -24,6 +24,16 @@ constexpr uint32_t kSpinLimit = 1u << 21;  // lookback polls before giving up (>
 // leaves before the copy lands only after both budgets
 constexpr uint32_t kCopyDrainLimit = 1u << 25;
 
+// Programmatic dependent launch.  A kernel launched with programmatic stream serialization
+// (launch_pdl) may be scheduled while the kernel before it in the stream still runs: its CTAs
+// wait here until that kernel has completed and its memory is visible, so the launch and the
+// CTAs' start overlap the predecessor's tail instead of following it.  The kernel then lets its
+// own dependent be scheduled.  For an ordinary launch both instructions do nothing.
+__device__ __forceinline__ void pdl_entry() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------
 // float-float arithmetic (Knuth two-sum); every operation rounds once.
 // ---------------------------------------------------------------------------

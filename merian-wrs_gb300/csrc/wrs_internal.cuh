@@ -112,6 +112,24 @@ struct BatchView {
     int2* descent;               // per split-pack CTA: the shared top of its bisections
 };
 
+// Launches `kernel` with programmatic stream serialization (the kernel starts with
+// pdl_entry()): it may be scheduled before its predecessor in the stream has finished.
+template <class... KArgs, class... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 // ---- launchers (defined in wrs_build.cu / wrs_sample.cu) -------------------------
 cudaError_t launch_total_mass(cudaStream_t st, const float* w, uint32_t n, double* partials,
                               BuildCtrl* ctrl);

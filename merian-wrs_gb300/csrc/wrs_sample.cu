@@ -109,6 +109,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_alias_sample(const uint2* __
                                                                  uint64_t seed, uint64_t offset,
                                                                  uint32_t coop,
                                                                  uint32_t* __restrict__ out) {
+    pdl_entry();
     alias_block<RNG, COOP>(table, n, S, seed, offset, coop, out, blockIdx.x);
 }
 
@@ -118,6 +119,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_alias_sample(const uint2* __
 template <uint32_t RNG, bool COOP>
 __global__ __launch_bounds__(kSampleThreads) void k_alias_sample_batch(BatchView bv,
                                                                        uint32_t coop) {
+    pdl_entry();
     const uint32_t d = __ldg(bv.sample_map + blockIdx.x);
     const DistDesc* D = bv.dist + d;
     alias_block<RNG, COOP>(D->table, D->n, D->s, D->seed, 0ull, coop, D->out,
@@ -203,6 +205,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample(const float* __re
                                                                uint64_t seed, uint64_t offset,
                                                                uint32_t coop,
                                                                uint32_t* __restrict__ out) {
+    pdl_entry();
     const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if constexpr (COOP == 0) {
         if (s >= S) return;
@@ -303,6 +306,7 @@ static_assert(kItsTreeLevels == static_cast<int>(kTreeTop), "shared levels above
 __global__ __launch_bounds__(kSampleThreads) void k_its_tree(const float* __restrict__ cmf,
                                                              uint32_t n, uint32_t L,
                                                              TreeBlock* __restrict__ blocks) {
+    pdl_entry();
     static_assert(its_tree_blocks(kTopBlockLevels) == kTopBlocks, "top block count");
     const size_t gb = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (gb >= its_tree_blocks(L)) return;
@@ -348,6 +352,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_tree(const float*
                                                                     uint32_t* __restrict__ out,
                                                                     const TreeBlock* __restrict__ blocks,
                                                                     uint32_t B) {
+    pdl_entry();
     __shared__ float s_tree[kItsTreeNodes];
     const uint32_t last = n - 1u;
     for (uint32_t k = threadIdx.x + 1; k < kItsTreeNodes; k += blockDim.x) {
@@ -527,6 +532,7 @@ __device__ __forceinline__ float cell_step(const float* __restrict__ cmf, uint32
 __global__ __launch_bounds__(kSampleThreads) void k_cell_coarse(const float* __restrict__ cmf,
                                                                 uint32_t n, uint32_t G,
                                                                 uint32_t* __restrict__ coarse) {
+    pdl_entry();
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= coarse_entries(G)) return;
     const uint64_t k = static_cast<uint64_t>(j) * kCoarseStride;
@@ -550,6 +556,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_cell_groups(const float* __r
                                                                 uint32_t n, uint32_t G,
                                                                 const uint32_t* __restrict__ coarse,
                                                                 uint32_t* __restrict__ group) {
+    pdl_entry();
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= group_entries(G)) return;
     const uint64_t k = static_cast<uint64_t>(g) * 32u;
@@ -617,6 +624,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_cells(const float* __res
                                                               uint32_t n, uint32_t G,
                                                               const uint32_t* __restrict__ group,
                                                               ItsCell* __restrict__ cells) {
+    pdl_entry();
     const uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // whole warps
     if (g * 32u >= G) return;
     uint32_t hi;
@@ -673,6 +681,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_cmf_tile_min(const float* __
                                                                  uint32_t n,
                                                                  float* __restrict__ tile_min,
                                                                  uint32_t* __restrict__ bad) {
+    pdl_entry();
     __shared__ float s_m[kSampleThreads / 32];
     const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kTileItems;
     float m = INFINITY;
@@ -699,6 +708,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_cmf_tile_min(const float* __
 __global__ __launch_bounds__(1024) void k_tile_suffix_min(const float* __restrict__ tile_min,
                                                           uint32_t tiles,
                                                           float* __restrict__ suf) {
+    pdl_entry();
     __shared__ float s_w[32];
     __shared__ float s_carry;
     if (threadIdx.x == 0) s_carry = INFINITY;
@@ -757,6 +767,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_cmf_mark(const float* __rest
                                                              uint32_t tiles,
                                                              ItsCell* __restrict__ cells,
                                                              uint32_t* __restrict__ bad) {
+    pdl_entry();
     __shared__ float s_w[kSampleThreads / 32];
     // one decision for the whole CTA (other CTAs may raise `bad` meanwhile)
     if (__syncthreads_or(*reinterpret_cast<volatile uint32_t*>(bad) != 0u)) return;
@@ -795,6 +806,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_cmf_mark(const float* __rest
 __global__ __launch_bounds__(kSampleThreads) void k_cells_mark_all(uint32_t G,
                                                                    ItsCell* __restrict__ cells,
                                                                    const uint32_t* __restrict__ bad) {
+    pdl_entry();
     if (*reinterpret_cast<const volatile uint32_t*>(bad) == 0u) return;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < G; k += gridDim.x * blockDim.x)
         cells[k].y |= kCellUnsafe;
@@ -852,6 +864,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_its_sample_cells(
     const float* __restrict__ cmf, uint32_t n, const ItsCell* __restrict__ cells, uint32_t G,
     uint64_t S, uint64_t seed, uint64_t offset, uint32_t* __restrict__ out,
     const TreeBlock* __restrict__ blocks, uint32_t L) {
+    pdl_entry();
     const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (s >= S) return;
     const uint32_t last = n - 1u;
@@ -941,6 +954,7 @@ __global__ __launch_bounds__(kSampleThreads) void k_guide_monotone(const float* 
                                                                    uint32_t n, uint32_t G,
                                                                    const uint32_t* __restrict__ group,
                                                                    uint32_t* __restrict__ guide) {
+    pdl_entry();
     const uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // whole warps
     if (g * 32u >= G) return;
     uint32_t hi;
@@ -955,9 +969,9 @@ static uint32_t* launch_cell_brackets(cudaStream_t st, const float* cmf, uint32_
                                       uint32_t* scratch) {
     const uint32_t m = coarse_entries(G), ng = group_entries(G);
     uint32_t* group = scratch + m;
-    k_cell_coarse<<<(m + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(cmf, n, G,
+    launch_pdl(k_cell_coarse, (m + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st, cmf, n, G,
                                                                                         scratch);
-    k_cell_groups<<<(ng + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(
+    launch_pdl(k_cell_groups, (ng + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st, 
         cmf, n, G, scratch, group);
     return group;
 }
@@ -971,9 +985,9 @@ cudaError_t launch_its_cells(cudaStream_t st, const float* cmf, uint32_t n, uint
                              uint32_t* coarse, ItsCell* cells, bool check) {
     uint32_t* group = launch_cell_brackets(st, cmf, n, G, coarse);
     if (check)
-        k_its_cells<true><<<warp_blocks(G), kSampleThreads, 0, st>>>(cmf, n, G, group, cells);
+        launch_pdl(k_its_cells<true>, warp_blocks(G), kSampleThreads, 0, st, cmf, n, G, group, cells);
     else
-        k_its_cells<false><<<warp_blocks(G), kSampleThreads, 0, st>>>(cmf, n, G, group, cells);
+        launch_pdl(k_its_cells<false>, warp_blocks(G), kSampleThreads, 0, st, cmf, n, G, group, cells);
     return cudaGetLastError();
 }
 
@@ -984,12 +998,12 @@ cudaError_t launch_its_marks(cudaStream_t st, const float* cmf, uint32_t n, uint
     float* suf = tile_scratch + tiles;
     cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    k_cmf_tile_min<<<tiles, kSampleThreads, 0, st>>>(cmf, n, tile_min, bad);
-    k_tile_suffix_min<<<1, 1024, 0, st>>>(tile_min, tiles, suf);
-    k_cmf_mark<<<tiles, kSampleThreads, 0, st>>>(cmf, n, G, suf, tiles, cells, bad);
+    launch_pdl(k_cmf_tile_min, tiles, kSampleThreads, 0, st, cmf, n, tile_min, bad);
+    launch_pdl(k_tile_suffix_min, 1, 1024, 0, st, tile_min, tiles, suf);
+    launch_pdl(k_cmf_mark, tiles, kSampleThreads, 0, st, cmf, n, G, suf, tiles, cells, bad);
     // (a grid-stride loop: any grid covers the cells; most launches return at once)
     const uint32_t mark_grid = min((G + kSampleThreads - 1) / kSampleThreads, 1024u);
-    k_cells_mark_all<<<mark_grid, kSampleThreads, 0, st>>>(G, cells, bad);
+    launch_pdl(k_cells_mark_all, mark_grid, kSampleThreads, 0, st, G, cells, bad);
     return cudaGetLastError();
 }
 
@@ -1001,10 +1015,10 @@ cudaError_t launch_its_sample_cells(cudaStream_t st, uint32_t rng, const float* 
     if (grid == 0) return cudaSuccess;
     if (grid > 0x7fffffffull) return cudaErrorInvalidValue;
     if (rng == RNG_REF)
-        k_its_sample_cells<RNG_REF><<<static_cast<unsigned>(grid), kSampleThreads, 0, st>>>(
+        launch_pdl(k_its_sample_cells<RNG_REF>, static_cast<unsigned>(grid), kSampleThreads, 0, st, 
             cmf, n, cells, G, S, seed, offset, out, blocks, L);
     else
-        k_its_sample_cells<RNG_PHILOX><<<static_cast<unsigned>(grid), kSampleThreads, 0, st>>>(
+        launch_pdl(k_its_sample_cells<RNG_PHILOX>, static_cast<unsigned>(grid), kSampleThreads, 0, st, 
             cmf, n, cells, G, S, seed, offset, out, blocks, L);
     return cudaGetLastError();
 }
@@ -1016,6 +1030,7 @@ cudaError_t launch_its_sample_cells(cudaStream_t st, uint32_t rng, const float* 
 __global__ __launch_bounds__(kSampleThreads) void k_cutpoint_guide(const float* __restrict__ cmf,
                                                                    uint32_t n, uint32_t G,
                                                                    uint32_t* __restrict__ guide) {
+    pdl_entry();
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= G) return;
     const float total = __ldg(cmf + n - 1u);
@@ -1033,6 +1048,7 @@ template <uint32_t RNG>
 __global__ __launch_bounds__(kSampleThreads) void k_cutpoint_sample(
     const float* __restrict__ cmf, uint32_t n, const uint32_t* __restrict__ guide, uint32_t G,
     uint64_t S, uint64_t seed, uint64_t offset, uint32_t* __restrict__ out) {
+    pdl_entry();
     const uint64_t s = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (s >= S) return;
     const uint64_t g = offset + s, g0 = offset + (s & ~31ull);
@@ -1064,14 +1080,14 @@ __global__ __launch_bounds__(kSampleThreads) void k_cutpoint_sample(
 cudaError_t launch_cutpoint_guide(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
                                   uint32_t* guide) {
     const uint32_t blocks = (G + kSampleThreads - 1) / kSampleThreads;
-    k_cutpoint_guide<<<blocks, kSampleThreads, 0, st>>>(cmf, n, G, guide);
+    launch_pdl(k_cutpoint_guide, blocks, kSampleThreads, 0, st, cmf, n, G, guide);
     return cudaGetLastError();
 }
 
 cudaError_t launch_guide_monotone(cudaStream_t st, const float* cmf, uint32_t n, uint32_t G,
                                   uint32_t* coarse, uint32_t* guide) {
     uint32_t* group = launch_cell_brackets(st, cmf, n, G, coarse);
-    k_guide_monotone<<<warp_blocks(G), kSampleThreads, 0, st>>>(cmf, n, G, group, guide);
+    launch_pdl(k_guide_monotone, warp_blocks(G), kSampleThreads, 0, st, cmf, n, G, group, guide);
     return cudaGetLastError();
 }
 
@@ -1082,10 +1098,10 @@ cudaError_t launch_cutpoint_sample(cudaStream_t st, uint32_t rng, const float* c
     if (blocks == 0) return cudaSuccess;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
     if (rng == RNG_REF)
-        k_cutpoint_sample<RNG_REF><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
+        launch_pdl(k_cutpoint_sample<RNG_REF>, static_cast<unsigned>(blocks), kSampleThreads, 0, st, 
             cmf, n, guide, G, S, seed, offset, out);
     else
-        k_cutpoint_sample<RNG_PHILOX><<<static_cast<unsigned>(blocks), kSampleThreads, 0, st>>>(
+        launch_pdl(k_cutpoint_sample<RNG_PHILOX>, static_cast<unsigned>(blocks), kSampleThreads, 0, st, 
             cmf, n, guide, G, S, seed, offset, out);
     return cudaGetLastError();
 }
@@ -1100,11 +1116,11 @@ cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, co
     const dim3 grid(static_cast<unsigned>(blocks));
     if (rng == RNG_REF) {
         if (coop)
-            k_alias_sample<RNG_REF, true><<<grid, kSampleThreads, 0, st>>>(table, n, S, seed, offset, coop, out);
+            launch_pdl(k_alias_sample<RNG_REF, true>, grid, kSampleThreads, 0, st, table, n, S, seed, offset, coop, out);
         else
-            k_alias_sample<RNG_REF, false><<<grid, kSampleThreads, 0, st>>>(table, n, S, seed, offset, coop, out);
+            launch_pdl(k_alias_sample<RNG_REF, false>, grid, kSampleThreads, 0, st, table, n, S, seed, offset, coop, out);
     } else {
-        k_alias_sample<RNG_PHILOX, false><<<grid, kSampleThreads, 0, st>>>(table, n, S, seed, offset, coop, out);
+        launch_pdl(k_alias_sample<RNG_PHILOX, false>, grid, kSampleThreads, 0, st, table, n, S, seed, offset, coop, out);
     }
     return cudaGetLastError();
 }
@@ -1114,11 +1130,11 @@ cudaError_t launch_batch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t co
     if (b.sample_blocks == 0) return cudaSuccess;
     if (rng == RNG_REF) {
         if (coop)
-            k_alias_sample_batch<RNG_REF, true><<<b.sample_blocks, kSampleThreads, 0, st>>>(b, coop);
+            launch_pdl(k_alias_sample_batch<RNG_REF, true>, b.sample_blocks, kSampleThreads, 0, st, b, coop);
         else
-            k_alias_sample_batch<RNG_REF, false><<<b.sample_blocks, kSampleThreads, 0, st>>>(b, 0u);
+            launch_pdl(k_alias_sample_batch<RNG_REF, false>, b.sample_blocks, kSampleThreads, 0, st, b, 0u);
     } else {
-        k_alias_sample_batch<RNG_PHILOX, false><<<b.sample_blocks, kSampleThreads, 0, st>>>(b, 0u);
+        launch_pdl(k_alias_sample_batch<RNG_PHILOX, false>, b.sample_blocks, kSampleThreads, 0, st, b, 0u);
     }
     return cudaGetLastError();
 }
@@ -1129,7 +1145,7 @@ cudaError_t launch_its_tree(cudaStream_t st, const float* cmf, uint32_t n, uint3
     if (count == 0) return cudaSuccess;
     const size_t grid = (count + kSampleThreads - 1) / kSampleThreads;
     if (grid > 0x7fffffffull) return cudaErrorInvalidValue;
-    k_its_tree<<<static_cast<unsigned>(grid), kSampleThreads, 0, st>>>(cmf, n, L, blocks);
+    launch_pdl(k_its_tree, static_cast<unsigned>(grid), kSampleThreads, 0, st, cmf, n, L, blocks);
     return cudaGetLastError();
 }
 
@@ -1145,15 +1161,15 @@ cudaError_t launch_its_sample(cudaStream_t st, uint32_t rng, uint32_t coop, bool
         const uint64_t groups = (S + kItsGroup - 1) / kItsGroup;
         const unsigned tb = static_cast<unsigned>(groups < kItsMaxBlocks ? groups : kItsMaxBlocks);
         if (rng == RNG_REF)
-            k_its_sample_tree<RNG_REF><<<tb, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, out,
+            launch_pdl(k_its_sample_tree<RNG_REF>, tb, kSampleThreads, 0, st, cmf, n, S, seed, offset, out,
                                                                       tree, B);
         else
-            k_its_sample_tree<RNG_PHILOX><<<tb, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset,
+            launch_pdl(k_its_sample_tree<RNG_PHILOX>, tb, kSampleThreads, 0, st, cmf, n, S, seed, offset,
                                                                          out, tree, B);
     } else if (parray) {
-        k_its_sample<RNG_REF, 2><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
+        launch_pdl(k_its_sample<RNG_REF, 2>, grid, kSampleThreads, 0, st, cmf, n, S, seed, offset, coop, out);
     } else {
-        k_its_sample<RNG_REF, 1><<<grid, kSampleThreads, 0, st>>>(cmf, n, S, seed, offset, coop, out);
+        launch_pdl(k_its_sample<RNG_REF, 1>, grid, kSampleThreads, 0, st, cmf, n, S, seed, offset, coop, out);
     }
     return cudaGetLastError();
 }
