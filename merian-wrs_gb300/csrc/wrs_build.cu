@@ -1390,6 +1390,13 @@ __device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ ta
         if (wv == 0.0f) wv = __uint_as_float(first.y);
         if (close_last && j >= c.hc) h = heavy_item(c, win, c.hc - 1u).x;
     }
+    // The walk's two candidates are loaded one step ahead: the next heavy item (position j + 1,
+    // needed while j < min(j1, hc)) and the next light item (rank i, while i < min(i1, lc)).  A
+    // step takes one of them and loads its successor, so no load waits for the step's
+    // decision (the values are those the step would load).
+    const uint32_t jmax = min(j1, c.hc), imax = min(i1, c.lc);
+    uint2 next_h = j < jmax ? heavy_item(c, win, j + 1u) : make_uint2(0u, 0u);
+    uint2 next_l = i < imax ? light_item(c, win, i) : make_uint2(0u, 0u);
     while (i < i1 || j < j1) {
         bool heavy_step;
         if (j == j1 || j == c.hc)
@@ -1398,7 +1405,7 @@ __device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ ta
             heavy_step = true;
         else
             heavy_step = wv <= c.mean;
-        const uint2 it = heavy_step ? heavy_item(c, win, j + 1u) : light_item(c, win, i);
+        const uint2 it = heavy_step ? next_h : next_l;
         const uint32_t widx = it.x;
         const float weight = __uint_as_float(it.y);
         float p;
@@ -1412,12 +1419,14 @@ __device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ ta
             if (later) owned = !covered_later(*later, j, false);
             ++j;
             if (!last) h = widx;
+            if (j < jmax) next_h = heavy_item(c, win, j + 1u);
         } else {
             p = __fdiv_rn(weight, c.mean);
             al = h;
             tidx = widx;
             if (later) owned = !covered_later(*later, i, true);
             ++i;
+            if (i < imax) next_l = light_item(c, win, i);
         }
         if (owned && tidx < c.n) table[tidx] = make_uint2(__float_as_uint(p), al);
         wv = __fsub_rn(__fadd_rn(wv, weight), c.mean);
@@ -1486,7 +1495,7 @@ __global__ __launch_bounds__(256) void k_split_descent(SplitArgs a, BatchView bv
 // (shader.comp:225-270).  The last kSplitLook + 1 slots only hold look-ahead splits for the
 // ownership window.
 template <bool R64, bool FF, bool BATCH, bool RECORDS = false>
-__global__ __launch_bounds__(kSplitThreads) void k_split_pack(SplitArgs a, BatchView bv) {
+__global__ __launch_bounds__(kSplitThreads, 4) void k_split_pack(SplitArgs a, BatchView bv) {
     pdl_entry();
     __shared__ uint32_t s_i[kSplitSlots], s_j[kSplitSlots];
     __shared__ float s_spill[kSplitSlots];
