@@ -1433,6 +1433,97 @@ __device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ ta
     }
 }
 
+// The inline split-pack's walk with its results staged for a coalesced write-out.  In a walk,
+// only two things depend on the walk itself: the residual a heavy bucket is packed with (its
+// p = residual / mean) and the heavy item current when a light bucket is packed (its alias).
+// Everything else of an entry is a function of the item: a heavy bucket's table index and its
+// alias are the original indices of positions j and j + 1, a light bucket's p is its weight /
+// mean.  So the walk reads only the weights and records, per heavy position of the CTA's
+// range, the residual, and per light rank the current heavy's position; the CTA then writes
+// its entries position by position, consecutive lanes on consecutive positions, whose table
+// indices increase (the partition is stable) -- instead of one scattered 8-byte store per
+// step.  Decisions, arithmetic and the ownership of overlapping subproblems are pack()'s, so
+// the table is the same bit for bit.  A position outside the staged ranges (a split stepping
+// back past them) is written directly, as pack() writes it.
+constexpr uint32_t kStageEntries = 6144;  // heavy positions + light ranks staged per CTA
+constexpr uint32_t kNotStaged = 0xffffffffu;
+constexpr size_t kEntryStageBytes = kStageEntries * sizeof(uint32_t);
+// One 32-bit word per staged position: heavy positions [h0, h0 + hcnt) at words [0, hcnt) hold
+// the residual's bits (a NaN residual in its canonical form, so no residual equals kNotStaged;
+// the NaN table entry it gives is the same), light ranks [l0, l0 + lcnt) at words
+// [hcnt, hcnt + lcnt) the current heavy's position; kNotStaged where this CTA packed nothing.
+struct EntryStage {
+    uint32_t* w;
+    uint32_t h0, hcnt, l0, lcnt;
+};
+
+__device__ __forceinline__ float item_weight(const PackIn& c, uint32_t pos) {
+    if (c.elems) return __ldg(c.elems + pos);
+    const uint32_t widx = __ldg(c.idx + pos);
+    return widx < c.n ? __ldg(c.w + widx) : 0.f;
+}
+
+// the entry of heavy position j packed with residual res (pack()'s heavy step)
+__device__ __forceinline__ void write_heavy(const PackIn& c, uint2* __restrict__ table,
+                                            uint32_t j, float res, bool close_last) {
+    const uint32_t tidx = __ldg(c.idx + j);
+    const bool last = close_last && j + 1u == c.hc;
+    const uint32_t al = last ? tidx : __ldg(c.idx + j + 1u);
+    const float p = last ? 1.0f : __fdiv_rn(res, c.mean);
+    if (tidx < c.n) table[tidx] = make_uint2(__float_as_uint(p), al);
+}
+// the entry of light rank i packed while heavy position J was current (pack()'s light step)
+__device__ __forceinline__ void write_light(const PackIn& c, uint2* __restrict__ table,
+                                            uint32_t i, uint32_t J) {
+    const uint32_t pos = c.n - 1u - i;
+    const uint32_t tidx = __ldg(c.idx + pos);
+    const float weight = c.elems ? __ldg(c.elems + pos) : (tidx < c.n ? __ldg(c.w + tidx) : 0.f);
+    if (tidx < c.n)
+        table[tidx] = make_uint2(__float_as_uint(__fdiv_rn(weight, c.mean)), __ldg(c.idx + J));
+}
+
+// The walk's step is branch-free apart from the rare paths (ownership inside the look-ahead
+// window, positions outside the staged ranges): the weight is selected from the two
+// candidates, one 32-bit word is staged, and the stream that advanced loads its next weight.
+__device__ void pack_staged(const PackIn& c, const EntryStage& st, uint2* __restrict__ table,
+                            uint32_t i0, uint32_t i1, uint32_t j0, uint32_t j1, float spill,
+                            const LaterSplits* later) {
+    uint32_t i = i0, j = j0;
+    float wv = spill;
+    const bool close_last = c.lcap == c.lc;
+    if (wv == 0.0f && (i < i1 || j < j1)) wv = item_weight(c, j);
+    const uint32_t jmax = min(j1, c.hc), imax = min(i1, c.lc);
+    float next_h = j < jmax ? item_weight(c, j + 1u) : 0.f;
+    float next_l = i < imax ? item_weight(c, c.n - 1u - i) : 0.f;
+    while (i < i1 || j < j1) {
+        const bool heavy_step =
+            !(j == j1 || j == c.hc) && ((i == i1 || i == c.lc) || wv <= c.mean);
+        const float weight = heavy_step ? next_h : next_l;
+        // the current heavy item: position j (pack()'s h), kept inside the heavy range by the
+        // table-end rule
+        const uint32_t J = close_last && j >= c.hc ? c.hc - 1u : j;
+        const uint32_t rel = heavy_step ? j - st.h0 : i - st.l0;
+        const bool staged = rel < (heavy_step ? st.hcnt : st.lcnt);
+        const uint32_t word = heavy_step ? (wv != wv ? 0x7fffffffu : __float_as_uint(wv)) : J;
+        const bool owned = !later || !covered_later(*later, heavy_step ? j : i, !heavy_step);
+        if (owned) {
+            if (staged)
+                st.w[heavy_step ? rel : st.hcnt + rel] = word;
+            else if (heavy_step)
+                write_heavy(c, table, j, wv, close_last);
+            else
+                write_light(c, table, i, J);
+        }
+        j += heavy_step ? 1u : 0u;
+        i += heavy_step ? 0u : 1u;
+        const bool more = heavy_step ? j < jmax : i < imax;
+        const float nw = more ? item_weight(c, heavy_step ? j + 1u : c.n - 1u - i) : 0.f;
+        next_h = heavy_step ? nw : next_h;
+        next_l = heavy_step ? next_l : nw;
+        wv = __fsub_rn(__fadd_rn(wv, weight), c.mean);
+    }
+}
+
 struct SplitArgs {
     const float* w;  // single distribution: weights, n, control block, table
     uint32_t n;
@@ -1447,8 +1538,10 @@ struct SplitArgs {
     uint32_t full_light;
     SplitRecord* records;  // serial split-pack: the split records (split k = records[k - 1])
     int2* descent;         // per CTA: the shared top of its bisections (k_split_descent) or null
-    uint32_t stage;        // nonzero: stage the CTA's items in shared memory (kPackWin of them)
+    uint32_t stage;        // record packs: stage the CTA's items in shared memory (kPackWin of
+                           // them); the inline kernel always stages its walks' results
 };
+constexpr uint32_t kStageEntriesMode = 2;
 
 // One thread per split-pack CTA: the shared descent of its splits (k_split_pack's slots
 // 1 .. kSplitSlots - 1 of the CTA, the look-ahead slots included).
@@ -1576,6 +1669,50 @@ __global__ __launch_bounds__(kSplitThreads, 4) void k_split_pack(SplitArgs a, Ba
     // gave the shared memory for it (the serial pack at small split sizes: measured faster
     // there; the inline kernel's bisections lose more to the smaller L1 than its walks gain)
     extern __shared__ uint2 s_items[];
+    if constexpr (!RECORDS) {
+        // the CTA's heavy positions [s_j[0], s_j[npack]) and light ranks [s_i[0], s_i[npack]),
+        // with a margin for splits stepping back at the end; staged only if both fit
+        const uint32_t kb = blk * kSplitPack;
+        const uint32_t npack = min(static_cast<uint32_t>(kSplitPack), K - kb);
+        constexpr uint32_t kMargin = 64;
+        EntryStage es{reinterpret_cast<uint32_t*>(s_items), s_j[0], 0u, s_i[0], 0u};
+        const uint32_t hext = (s_j[npack] > es.h0 ? s_j[npack] - es.h0 : 0u) + kMargin;
+        const uint32_t lext = (s_i[npack] > es.l0 ? s_i[npack] - es.l0 : 0u) + kMargin;
+        if (hext + lext <= kStageEntries) {
+            es.hcnt = hext;
+            es.lcnt = lext;
+        }
+        for (uint32_t q = threadIdx.x; q < es.hcnt + es.lcnt; q += blockDim.x) es.w[q] = kNotStaged;
+        __syncthreads();
+#pragma unroll 1
+        for (int v = 0; v < kSplitPerThread; ++v) {
+            const int t = threadIdx.x + v * kSplitThreads;
+            const uint32_t k = kv[v];
+            if (t >= kSplitPack || k >= K) continue;
+            const uint32_t i1 = max(s_i[t + 1], si[v]), j1 = max(s_j[t + 1], sj[v]);
+            const int count = static_cast<int>(min(static_cast<uint32_t>(kSplitLook), K - 1u - k));
+            bool clean = true;
+            for (int d = 1; d <= count; ++d)
+                clean = clean && s_i[t + d] >= i1 && s_j[t + d] >= j1;
+            if (k + kSplitLook + 1u < K &&
+                (s_i[t + kSplitLook + 1] < i1 || s_j[t + kSplitLook + 1] < j1))
+                atomicOr(a.status, kStatusNonMonotone);
+            const LaterSplits later{s_i, s_j, t, count};
+            pack_staged(c, es, table, si[v], i1, sj[v], j1, sp[v], clean ? nullptr : &later);
+        }
+        __syncthreads();
+        // write-out: consecutive lanes on consecutive positions
+        const bool close_last = c.lcap == c.lc;
+        for (uint32_t q = threadIdx.x; q < es.hcnt; q += blockDim.x) {
+            const uint32_t r = es.w[q];
+            if (r != kNotStaged) write_heavy(c, table, es.h0 + q, __uint_as_float(r), close_last);
+        }
+        for (uint32_t q = threadIdx.x; q < es.lcnt; q += blockDim.x) {
+            const uint32_t J = es.w[es.hcnt + q];
+            if (J != kNotStaged) write_light(c, table, es.l0 + q, J);
+        }
+        return;
+    }
     PackWin win{s_items, 0u, 0u, 0u, 0u};
     if (a.stage) {
         const uint32_t kb = blk * kSplitPack;
@@ -1617,6 +1754,11 @@ constexpr size_t kPackWinBytes = kPackWin * sizeof(uint2);
 template <bool R64, bool FF, bool BATCH, bool RECORDS>
 static void launch_split_kernel(cudaStream_t st, uint32_t grid, const SplitArgs& a,
                                 const BatchView& bv) {
+    if (!RECORDS) {  // the inline kernel stages its walks' results (below 48 KB)
+        launch_pdl(k_split_pack<R64, FF, BATCH, RECORDS>, grid, kSplitThreads, kEntryStageBytes,
+                   st, a, bv);
+        return;
+    }
     if (!a.stage) {
         launch_pdl(k_split_pack<R64, FF, BATCH, RECORDS>, grid, kSplitThreads, 0, st, a, bv);
         return;
@@ -1649,7 +1791,8 @@ cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const 
     const SplitArgs a{w,      n,         ctrl,   table,      idx,
                       elems,  prefix,    prefix_lo, status,  split_size,
                       full_light ? 1u : 0u, nullptr,
-                      split_blocks_for(n, split_size) >= kDescentMinBlocks ? descent : nullptr};
+                      split_blocks_for(n, split_size) >= kDescentMinBlocks ? descent : nullptr,
+                      kStageEntriesMode};
     const uint32_t blocks = split_blocks_for(n, split_size);
     // the extra launch pays off once there are several waves of split-pack CTAs
     if (descent && blocks >= kDescentMinBlocks) {
@@ -2167,8 +2310,9 @@ cudaError_t launch_batch_build(cudaStream_t st, uint32_t precision, bool r64, co
     const PartArgs pa{nullptr,    0u,       nullptr,  b.lb,   b.states,  b.cap_tiles,
                       kSpinLimit, b.status, b.idx,    b.prefix, b.elems, b.prefix_lo};
     part_dispatch<true>(st, precision, b.tiles, pa, b);
-    const SplitArgs sa{nullptr, 0u,       nullptr,     nullptr,  b.idx,        b.elems,
-                       b.prefix, b.prefix_lo, b.status, b.split_size, b.full_light};
+    const SplitArgs sa{nullptr,  0u,          nullptr,  nullptr,      b.idx,
+                       b.elems,  b.prefix,    b.prefix_lo, b.status, b.split_size,
+                       b.full_light, nullptr, nullptr, kStageEntriesMode};
     if (b.descent && b.split_blocks) {
         const uint32_t g = (b.split_blocks + 255u) / 256u;
         if (precision == 2)
