@@ -1267,6 +1267,62 @@ __device__ __forceinline__ void compute_splits(const PackIn& c, const uint32_t (
     }
 }
 
+// one split per thread: compute_splits's probe sequence, FP32 pre-test and arithmetic for V = 1
+template <bool R64, bool FF>
+__device__ __forceinline__ void bisect_one(const PackIn& c, uint32_t nsplit, bool on, uint32_t& io,
+                                           uint32_t& jo, float& spill, int a, int b) {
+    if (!on) return;
+    const float target = __fmul_rn(c.mean, __uint2float_rn(nsplit));
+    ff tff{0.f, 0.f};
+    if constexpr (FF) tff = ff_target(c.mean, c.mean_lo, nsplit);
+    const uint32_t lcm1 = c.lcap;
+    while (a <= b) {
+        const uint32_t j = static_cast<uint32_t>(a + ((b - a) >> 1));
+        const uint32_t i = j > nsplit ? lcm1 : min(nsplit - j, lcm1);
+        const float heavy = j ? __ldg(c.prefix + j - 1) : 0.f;
+        const float light = i ? __ldg(c.prefix + c.n - i) : 0.f;
+        bool le;
+        if constexpr (FF) {
+            const float hs = __fadd_rn(heavy, light);
+            const float d = __fsub_rn(hs, tff.hi);
+            const float m = __fmul_rn(4.76837158203125e-07f, __fadd_rn(hs, tff.hi));
+            if (d > m) {
+                le = false;
+            } else if (d < -m) {
+                le = true;
+            } else {
+                const float hl = j ? __ldg(c.prefix_lo + j - 1) : 0.f;
+                const float ll = i ? __ldg(c.prefix_lo + c.n - i) : 0.f;
+                le = ff_sigma_minus(heavy, hl, light, ll, tff.hi, tff.lo) <= 0.0f;
+            }
+        } else {
+            le = __fadd_rn(light, heavy) <= target;
+        }
+        if (le)
+            a = static_cast<int>(j) + 1;
+        else
+            b = static_cast<int>(j) - 1;
+    }
+    const uint32_t j = b < 0 ? 0u : static_cast<uint32_t>(b);
+    const uint32_t i = j > nsplit ? lcm1 : min(nsplit - j, lcm1);
+    const float light = i == 0 ? 0.f : __ldg(c.prefix + c.n - i);
+    const float heavy2 = __ldg(c.prefix + j);
+    if constexpr (FF) {
+        const float hl2 = __ldg(c.prefix_lo + j);
+        const float l2 = i == 0 ? 0.f : __ldg(c.prefix_lo + c.n - i);
+        spill = ff_sigma_minus(heavy2, hl2, light, l2, tff.hi, tff.lo);
+    } else if constexpr (R64) {
+        const double target64 =
+            __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit));
+        spill = __double2float_rn(
+            __dsub_rn(__dadd_rn(static_cast<double>(heavy2), static_cast<double>(light)), target64));
+    } else {
+        spill = __fsub_rn(__fadd_rn(heavy2, light), target);
+    }
+    io = i;
+    jo = j;
+}
+
 // The top of the bisections of one CTA's splits, shared.  Every split of a CTA starts from
 // (a, b) = (0, hc - 1) and probes the same j while its decisions agree with the others'.  For a
 // fixed j the probed difference f(n) = heavy(j) + light(n - j) - mean * n does not increase
@@ -1524,6 +1580,39 @@ __device__ void pack_staged(const PackIn& c, const EntryStage& st, uint2* __rest
     }
 }
 
+// pack_staged for a subproblem whose items all lie inside the staged ranges, inside the heavy
+// and light ranges (j1 <= heavyCount, i1 <= the light count) and that no later subproblem in
+// the window covers: every step is owned and staged, and the end tests reduce to j == j1 and
+// i == i1.  Decisions, arithmetic and staged words are pack_staged's.
+__device__ __forceinline__ void pack_staged_fast(const PackIn& c, const EntryStage& st,
+                                                 uint32_t i0, uint32_t i1, uint32_t j0,
+                                                 uint32_t j1, float spill) {
+    uint32_t i = i0, j = j0;
+    float wv = spill;
+    const bool close_last = c.lcap == c.lc;
+    if (wv == 0.0f && (i < i1 || j < j1)) wv = item_weight(c, j);
+    float next_h = j < j1 ? item_weight(c, j + 1u) : 0.f;
+    float next_l = i < i1 ? item_weight(c, c.n - 1u - i) : 0.f;
+    uint32_t* const wh = st.w - st.h0;             // heavy position j -> its word
+    uint32_t* const wl = st.w + st.hcnt - st.l0;   // light rank i -> its word
+    while (i < i1 || j < j1) {
+        const bool heavy_step = j != j1 && (i == i1 || wv <= c.mean);
+        const float weight = heavy_step ? next_h : next_l;
+        const uint32_t J = close_last && j >= c.hc ? c.hc - 1u : j;
+        if (heavy_step)
+            wh[j] = wv != wv ? 0x7fffffffu : __float_as_uint(wv);
+        else
+            wl[i] = J;
+        j += heavy_step ? 1u : 0u;
+        i += heavy_step ? 0u : 1u;
+        const bool more = heavy_step ? j < j1 : i < i1;
+        const float nw = more ? item_weight(c, heavy_step ? j + 1u : c.n - 1u - i) : 0.f;
+        next_h = heavy_step ? nw : next_h;
+        next_l = heavy_step ? next_l : nw;
+        wv = __fsub_rn(__fadd_rn(wv, weight), c.mean);
+    }
+}
+
 struct SplitArgs {
     const float* w;  // single distribution: weights, n, control block, table
     uint32_t n;
@@ -1655,7 +1744,7 @@ __global__ __launch_bounds__(kSplitThreads, 4) void k_split_pack(SplitArgs a, Ba
         int2 d0 = make_int2(0, static_cast<int>(hc) - 1);
         const int2* desc = BATCH ? bv.descent : a.descent;
         if (desc) d0 = desc[BATCH ? blockIdx.x : blk];
-        compute_splits<R64, FF, kSplitPerThread>(c, nsplit, on, si, sj, sp, d0.x, d0.y);
+        bisect_one<R64, FF>(c, nsplit[0], on[0], si[0], sj[0], sp[0], d0.x, d0.y);
     }
 #pragma unroll
     for (int v = 0; v < kSplitPerThread; ++v) {
@@ -1682,23 +1771,39 @@ __global__ __launch_bounds__(kSplitThreads, 4) void k_split_pack(SplitArgs a, Ba
             es.hcnt = hext;
             es.lcnt = lext;
         }
+        // the CTA's splits in slot order never step back (the common case): then no later
+        // subproblem covers an earlier one's items, and the ownership window is not consulted
+        bool mono = true;
+#pragma unroll
+        for (int v = 0; v < kSplitPerThread; ++v) {
+            const int t = threadIdx.x + v * kSplitThreads;
+            if (t + 1 < kSplitSlots) mono = mono && s_i[t + 1] >= s_i[t] && s_j[t + 1] >= s_j[t];
+        }
         for (uint32_t q = threadIdx.x; q < es.hcnt + es.lcnt; q += blockDim.x) es.w[q] = kNotStaged;
-        __syncthreads();
+        const bool all_mono = __syncthreads_and(mono);
 #pragma unroll 1
         for (int v = 0; v < kSplitPerThread; ++v) {
             const int t = threadIdx.x + v * kSplitThreads;
             const uint32_t k = kv[v];
             if (t >= kSplitPack || k >= K) continue;
             const uint32_t i1 = max(s_i[t + 1], si[v]), j1 = max(s_j[t + 1], sj[v]);
-            const int count = static_cast<int>(min(static_cast<uint32_t>(kSplitLook), K - 1u - k));
             bool clean = true;
-            for (int d = 1; d <= count; ++d)
-                clean = clean && s_i[t + d] >= i1 && s_j[t + d] >= j1;
-            if (k + kSplitLook + 1u < K &&
-                (s_i[t + kSplitLook + 1] < i1 || s_j[t + kSplitLook + 1] < j1))
-                atomicOr(a.status, kStatusNonMonotone);
+            int count = 0;
+            if (!all_mono) {
+                count = static_cast<int>(min(static_cast<uint32_t>(kSplitLook), K - 1u - k));
+                for (int d = 1; d <= count; ++d)
+                    clean = clean && s_i[t + d] >= i1 && s_j[t + d] >= j1;
+                if (k + kSplitLook + 1u < K &&
+                    (s_i[t + kSplitLook + 1] < i1 || s_j[t + kSplitLook + 1] < j1))
+                    atomicOr(a.status, kStatusNonMonotone);
+            }
             const LaterSplits later{s_i, s_j, t, count};
-            pack_staged(c, es, table, si[v], i1, sj[v], j1, sp[v], clean ? nullptr : &later);
+            const bool inside = sj[v] >= es.h0 && j1 - es.h0 <= es.hcnt && si[v] >= es.l0 &&
+                                i1 - es.l0 <= es.lcnt && j1 <= c.hc && i1 <= c.lc;
+            if (clean && inside)
+                pack_staged_fast(c, es, si[v], i1, sj[v], j1, sp[v]);
+            else
+                pack_staged(c, es, table, si[v], i1, sj[v], j1, sp[v], clean ? nullptr : &later);
         }
         __syncthreads();
         // write-out: consecutive lanes on consecutive positions

@@ -112,8 +112,17 @@ struct BatchView {
     int2* descent;               // per split-pack CTA: the shared top of its bisections
 };
 
-// Launches `kernel` with programmatic stream serialization (the kernel starts with
-// pdl_entry()): it may be scheduled before its predecessor in the stream has finished.
+// Grids up to this many CTAs (about one wave of 256-thread CTAs on the device) are launched
+// with programmatic stream serialization; larger ones are launched plainly.  Measured on
+// GB300: the small configuration's per-call build takes 20.2 us with it against 24.6 us
+// without and its sampling 6.3 against 8.2 us, while a build of 2^26 weights takes 1.20
+// against 1.13 ms and a batch graph of 4096 distributions 15.8 against 10.8 ms -- the early
+// scheduled CTAs of a many-wave kernel cost more than the launch gap they hide.
+constexpr uint64_t kPdlMaxGrid = 2048;
+
+// Launches `kernel` (which starts with pdl_entry()) with programmatic stream serialization
+// when its grid is at most kPdlMaxGrid CTAs: it may then be scheduled before its predecessor
+// in the stream has finished.
 template <class... KArgs, class... Args>
 inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
                               cudaStream_t st, Args&&... args) {
@@ -126,7 +135,8 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    const uint64_t ctas = static_cast<uint64_t>(grid.x) * grid.y * grid.z;
+    cfg.numAttrs = ctas <= kPdlMaxGrid ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
 }
 
