@@ -1806,15 +1806,47 @@ __global__ __launch_bounds__(kSplitThreads, 4) void k_split_pack(SplitArgs a, Ba
                 pack_staged(c, es, table, si[v], i1, sj[v], j1, sp[v], clean ? nullptr : &later);
         }
         __syncthreads();
-        // write-out: consecutive lanes on consecutive positions
+        // write-out: consecutive lanes on consecutive positions, kOutBatch positions per thread
+        // with their loads in flight together (write_heavy / write_light's values; positions
+        // clamped into [0, n) so that every load is in bounds, only staged entries stored)
         const bool close_last = c.lcap == c.lc;
-        for (uint32_t q = threadIdx.x; q < es.hcnt; q += blockDim.x) {
-            const uint32_t r = es.w[q];
-            if (r != kNotStaged) write_heavy(c, table, es.h0 + q, __uint_as_float(r), close_last);
+        constexpr int kOutBatch = 4;
+        const uint32_t bd = blockDim.x, nm1 = c.n - 1u;
+        for (uint32_t q0 = threadIdx.x; q0 < es.hcnt; q0 += kOutBatch * bd) {
+            uint32_t r[kOutBatch], t[kOutBatch], al[kOutBatch];
+#pragma unroll
+            for (int u = 0; u < kOutBatch; ++u) {
+                const uint32_t q = q0 + u * bd;
+                r[u] = q < es.hcnt ? es.w[q] : kNotStaged;
+                const uint32_t j = min(es.h0 + q, nm1);
+                t[u] = __ldg(c.idx + j);
+                al[u] = __ldg(c.idx + min(j + 1u, nm1));
+            }
+#pragma unroll
+            for (int u = 0; u < kOutBatch; ++u) {
+                if (r[u] == kNotStaged || t[u] >= c.n) continue;
+                const bool last = close_last && es.h0 + q0 + u * bd + 1u == c.hc;
+                const float p = last ? 1.0f : __fdiv_rn(__uint_as_float(r[u]), c.mean);
+                table[t[u]] = make_uint2(__float_as_uint(p), last ? t[u] : al[u]);
+            }
         }
-        for (uint32_t q = threadIdx.x; q < es.lcnt; q += blockDim.x) {
-            const uint32_t J = es.w[es.hcnt + q];
-            if (J != kNotStaged) write_light(c, table, es.l0 + q, J);
+        for (uint32_t q0 = threadIdx.x; q0 < es.lcnt; q0 += kOutBatch * bd) {
+            uint32_t J[kOutBatch], t[kOutBatch], aj[kOutBatch];
+            float wt[kOutBatch];
+#pragma unroll
+            for (int u = 0; u < kOutBatch; ++u) {
+                const uint32_t q = q0 + u * bd;
+                J[u] = q < es.lcnt ? es.w[es.hcnt + q] : kNotStaged;
+                const uint32_t pos = nm1 - min(es.l0 + q, nm1);
+                t[u] = __ldg(c.idx + pos);
+                wt[u] = c.elems ? __ldg(c.elems + pos) : (t[u] < c.n ? __ldg(c.w + t[u]) : 0.f);
+                aj[u] = __ldg(c.idx + min(J[u], nm1));
+            }
+#pragma unroll
+            for (int u = 0; u < kOutBatch; ++u) {
+                if (J[u] == kNotStaged || t[u] >= c.n) continue;
+                table[t[u]] = make_uint2(__float_as_uint(__fdiv_rn(wt[u], c.mean)), aj[u]);
+            }
         }
         return;
     }
