@@ -456,17 +456,19 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
         ff fh{0.f, 0.f}, fl{0.f, 0.f};
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-            if (y[i] > pivot) {
+            if constexpr (FFOUT) {
+                // one float-float add on the selected accumulator (the operations of adding to
+                // it in a branch, without the two predicated paths)
+                const bool hv = y[i] > pivot;
+                tc += hv ? 1u : 0u;
+                const ff acc = ff_add_f(hv ? fh : fl, y[i]);
+                fh = hv ? acc : fh;
+                fl = hv ? fl : acc;
+            } else if (y[i] > pivot) {
                 ++tc;
-                if constexpr (FFOUT)
-                    fh = ff_add_f(fh, y[i]);
-                else
-                    th = __fadd_rn(th, y[i]);
+                th = __fadd_rn(th, y[i]);
             } else {
-                if constexpr (FFOUT)
-                    fl = ff_add_f(fl, y[i]);
-                else
-                    tl = __fadd_rn(tl, y[i]);
+                tl = __fadd_rn(tl, y[i]);
             }
         }
         const uint32_t ic = warp_incl_u(tc, lane);
@@ -631,26 +633,24 @@ __global__ __launch_bounds__(kTileThreads, kPartMinBlocks) void k_prefix_partiti
                     const float xv = yv[c];
                     uint32_t slot;
                     float hi;
-                    if (xv > pivot) {
+                    if constexpr (FFOUT) {
+                        // branch-free, as in phase A
+                        const bool hv = xv > pivot;
+                        slot = hv ? hc : kTileItems - 1u - (local - hc);
+                        hc += hv ? 1u : 0u;
+                        const ff acc = ff_add_f(hv ? rh : rl, xv);
+                        rh = hv ? acc : rh;
+                        rl = hv ? rl : acc;
+                        hi = acc.hi;
+                        lo_keep[4 * j + c] = acc.lo;
+                    } else if (xv > pivot) {
                         slot = hc++;
-                        if constexpr (FFOUT) {
-                            rh = ff_add_f(rh, xv);
-                            hi = rh.hi;
-                            lo_keep[4 * j + c] = rh.lo;
-                        } else {
-                            rh32 = __fadd_rn(rh32, xv);
-                            hi = carry_apply<COMP>(ex_h, rh32);
-                        }
+                        rh32 = __fadd_rn(rh32, xv);
+                        hi = carry_apply<COMP>(ex_h, rh32);
                     } else {
                         slot = kTileItems - 1u - (local - hc);
-                        if constexpr (FFOUT) {
-                            rl = ff_add_f(rl, xv);
-                            hi = rl.hi;
-                            lo_keep[4 * j + c] = rl.lo;
-                        } else {
-                            rl32 = __fadd_rn(rl32, xv);
-                            hi = carry_apply<COMP>(ex_l, rl32);
-                        }
+                        rl32 = __fadd_rn(rl32, xv);
+                        hi = carry_apply<COMP>(ex_l, rl32);
                     }
                     s_key[stage_idx(slot)] = static_cast<uint16_t>(local);
                     s_val[stage_idx(slot)] = hi;
