@@ -935,6 +935,26 @@ __device__ u128 scan_lookback_x(const ScanState* st, uint32_t tile, uint32_t* st
         [](u128 a, u128 b) { return a + b; });
 }
 
+// RN(k * 2^g + r), r the thread's FP32 running sum, decided from a float-float evaluation
+// where that is safe (Ziv's rounding test).  With kf = fx_to_ff(k, g) (kf.hi + kf.lo within
+// u^2 of k * 2^g, u = 2^-24 the unit roundoff), two_sum(kf.hi, r) exact, one rounding of u^2 in the low
+// words and fast_two_sum exact, v.hi + v.lo is within 3u^2 (1 + u) of the exact value X.  If
+// it lies more than 2^-44 v.hi (> 5 times that) from the midpoints between v.hi and its
+// neighbours, X rounds to v.hi; otherwise -- and for r < 0 or NaN, and values outside
+// [2^-100, 2^100], where the spacing arithmetic below is not exact -- the fixed-point path
+// rounds the exact sum, so the result is fx_round's in every case.
+__device__ __forceinline__ float cmf_round(u128 k, ff kf, float r, int g) {
+    const ff s = two_sum(kf.hi, r);
+    const ff v = fast_two_sum(s.hi, __fadd_rn(s.lo, kf.lo));
+    const uint32_t b = __float_as_uint(v.hi);
+    const float up = __fsub_rn(__uint_as_float(b + 1u), v.hi);    // spacing above v.hi
+    const float down = __fsub_rn(v.hi, __uint_as_float(b - 1u));  // spacing below v.hi
+    const float margin = __fsub_rn(__fmul_rn(0.5f, v.lo >= 0.0f ? up : down), fabsf(v.lo));
+    const bool ok = r >= 0.0f && v.hi >= 0x1p-100f && v.hi <= 0x1p100f &&
+                    margin > __fmul_rn(v.hi, 0x1p-44f);
+    return ok ? v.hi : fx_round(k + fx_from_float(r, g), g);
+}
+
 __global__ __launch_bounds__(kTileThreads) void k_scan_exact(const float* __restrict__ in,
                                                              uint32_t n, float* __restrict__ out,
                                                              BuildCtrl* __restrict__ ctrl,
@@ -1010,19 +1030,20 @@ __global__ __launch_bounds__(kTileThreads) void k_scan_exact(const float* __rest
     __syncthreads();
     {
         const u128 K = s_c + s_wt[warp] + s_e[threadIdx.x];
+        const ff kf = fx_to_ff(K, grid);
         float r = 0.f;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             float4& slot = s_x[park_slot(warp * 128 + lane * 4 + j)];
             float4 q = slot;
             r = __fadd_rn(r, q.x);
-            q.x = fx_round(K + fx_from_float(r, grid), grid);
+            q.x = cmf_round(K, kf, r, grid);
             r = __fadd_rn(r, q.y);
-            q.y = fx_round(K + fx_from_float(r, grid), grid);
+            q.y = cmf_round(K, kf, r, grid);
             r = __fadd_rn(r, q.z);
-            q.z = fx_round(K + fx_from_float(r, grid), grid);
+            q.z = cmf_round(K, kf, r, grid);
             r = __fadd_rn(r, q.w);
-            q.w = fx_round(K + fx_from_float(r, grid), grid);
+            q.w = cmf_round(K, kf, r, grid);
             slot = q;  // this thread's own chunks: no other thread touches them here
         }
     }
@@ -1501,9 +1522,17 @@ __device__ void pack(const PackIn& c, const PackWin& win, uint2* __restrict__ ta
 // step.  Decisions, arithmetic and the ownership of overlapping subproblems are pack()'s, so
 // the table is the same bit for bit.  A position outside the staged ranges (a split stepping
 // back past them) is written directly, as pack() writes it.
-constexpr uint32_t kStageEntries = 6144;  // heavy positions + light ranks staged per CTA
+// The inline split-pack stages one word per heavy position and light rank its CTA's walks
+// cover: kSplitPack * split_size items when the CTA's splits do not step back, plus the
+// walks' margins.  At most 48 KB (four CTAs of 512 threads per SM); split sizes that need
+// more stage nothing (0) and write their entries directly, rather than hold shared memory
+// that lowers occupancy without use.
+constexpr uint32_t kStageMaxEntries = 12288;
+__host__ __device__ inline uint32_t stage_entries_for(uint32_t split_size) {
+    const uint64_t e = static_cast<uint64_t>(kSplitPack) * split_size + 256u;
+    return e <= kStageMaxEntries ? static_cast<uint32_t>(e) : 0u;
+}
 constexpr uint32_t kNotStaged = 0xffffffffu;
-constexpr size_t kEntryStageBytes = kStageEntries * sizeof(uint32_t);
 // One 32-bit word per staged position: heavy positions [h0, h0 + hcnt) at words [0, hcnt) hold
 // the residual's bits (a NaN residual in its canonical form, so no residual equals kNotStaged;
 // the NaN table entry it gives is the same), light ranks [l0, l0 + lcnt) at words
@@ -1767,7 +1796,7 @@ __global__ __launch_bounds__(kSplitThreads, 4) void k_split_pack(SplitArgs a, Ba
         EntryStage es{reinterpret_cast<uint32_t*>(s_items), s_j[0], 0u, s_i[0], 0u};
         const uint32_t hext = (s_j[npack] > es.h0 ? s_j[npack] - es.h0 : 0u) + kMargin;
         const uint32_t lext = (s_i[npack] > es.l0 ? s_i[npack] - es.l0 : 0u) + kMargin;
-        if (hext + lext <= kStageEntries) {
+        if (hext + lext <= stage_entries_for(a.split_size)) {
             es.hcnt = hext;
             es.lcnt = lext;
         }
@@ -1891,9 +1920,15 @@ constexpr size_t kPackWinBytes = kPackWin * sizeof(uint2);
 template <bool R64, bool FF, bool BATCH, bool RECORDS>
 static void launch_split_kernel(cudaStream_t st, uint32_t grid, const SplitArgs& a,
                                 const BatchView& bv) {
-    if (!RECORDS) {  // the inline kernel stages its walks' results (below 48 KB)
-        launch_pdl(k_split_pack<R64, FF, BATCH, RECORDS>, grid, kSplitThreads, kEntryStageBytes,
-                   st, a, bv);
+    if (!RECORDS) {  // the inline kernel stages its walks' results (at most 48 KB)
+        const size_t bytes = stage_entries_for(a.split_size) * sizeof(uint32_t);
+        // with the kernel's static arrays, more than 40 KB needs the opt-in (set on the current
+        // device's context, for every such launch; a failure shows as the launch's error)
+        if (bytes > (40u << 10))
+            cudaFuncSetAttribute(k_split_pack<R64, FF, BATCH, RECORDS>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(bytes));
+        launch_pdl(k_split_pack<R64, FF, BATCH, RECORDS>, grid, kSplitThreads, bytes, st, a, bv);
         return;
     }
     if (!a.stage) {

@@ -10,6 +10,8 @@ Bar (stated per test):
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 import pytest
 
@@ -388,6 +390,68 @@ def test_compensated_cmf_is_exactly_monotone(pkg, cuda, oracle, N):
     assert not np.any(w[s] == 0)
     ref = oracle.prefix_f64(w)
     assert np.abs(a.cmf.astype(np.float64) - ref).max() <= 1e-6 * ref[-1]
+
+
+def _fx(x: np.float32, g: int) -> int:
+    """An FP32 value >= 0 on the fixed-point grid 2^g (bits below the grid dropped)."""
+    b = int(np.float32(x).view(np.uint32))
+    e, m = b >> 23, b & 0x7FFFFF
+    ex = -149
+    if e:
+        m |= 1 << 23
+        ex = e - 150
+    sh = ex - g
+    return m << sh if sh >= 0 else m >> -sh
+
+
+def _round_f32(k: int, g: int) -> np.float32:
+    """k * 2^g rounded to nearest FP32 (ties to even), for normal results."""
+    if k == 0:
+        return np.float32(0.0)
+    nb = k.bit_length()
+    q, e = k, g
+    if nb > 24:
+        sh = nb - 24
+        q, rem, half = k >> sh, k & ((1 << sh) - 1), 1 << (sh - 1)
+        if rem > half or (rem == half and q & 1):
+            q += 1
+        e = g + sh
+    return np.float32(math.ldexp(q, e))
+
+
+def exact_cmf(w: np.ndarray, total: float) -> np.ndarray:
+    """The compensated CMF's definition: element i of thread t (16 consecutive weights per
+    thread) is RN(K_t + r_i) -- K_t the exact fixed-point sum of the FP32 totals of all threads
+    before t, r_i the thread's FP32 running sum through i, both on the grid 2^g that the
+    distribution's FP64 total sets (its exponent minus 123)."""
+    g = math.frexp(total)[1] - 123
+    pad = (-w.size) % 16
+    run = np.cumsum(np.concatenate([w, np.zeros(pad, np.float32)]).reshape(-1, 16), axis=1,
+                    dtype=np.float32)
+    out = np.empty(w.size, np.float32)
+    K = 0
+    for t in range(run.shape[0]):
+        for c in range(16):
+            i = 16 * t + c
+            if i < w.size:
+                out[i] = _round_f32(K + _fx(run[t, c], g), g)
+        K += _fx(run[t, 15], g)
+    return out
+
+
+@pytest.mark.parametrize("N", [4097, 3 * 4096 + 5, 65536 + 77])
+@pytest.mark.parametrize("gen", ["uniform", "lognormal", "precision"])
+def test_compensated_cmf_bit_exact(pkg, cuda, N, gen):
+    """Every element of the compensated CMF equals its definition computed on the CPU with
+    exact integers (the GPU decides most roundings from a float-float evaluation and the
+    rest in fixed point; both must give the correctly rounded sum)."""
+    w = {"uniform": weights_uniform, "lognormal": weights_lognormal,
+         "precision": weights_precision}[gen](N, 3 * N + 1)
+    w[0] = max(w[0], np.float32(1e-3))  # keep the first values normal
+    b = Built(pkg, w, pkg.ITSConfig(scan_precision=1))
+    assert b.status == 0
+    total = float(d2h(b.buffers.internals.views()["total"], 1, np.float64)[0])
+    assert np.array_equal(b.cmf.view(np.uint32), exact_cmf(w, total).view(np.uint32))
 
 
 @pytest.mark.parametrize("rng,coop,parray", [(RNG_REFERENCE, 0, False),
