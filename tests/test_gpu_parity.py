@@ -114,12 +114,14 @@ def test_prefix_partition(pkg, cuda, oracle, N, gen, comp):
 
 # --------------------------------------------------------------- split + pack ---
 
-@pytest.mark.parametrize("split_size", [1, 2, 3, 32])
+@pytest.mark.parametrize("split_size", [1, 2, 3, 16, 24, 32])
 @pytest.mark.parametrize("flags", [0, 1, 2, 3])
 @pytest.mark.parametrize("gen", list(GENS))
 def test_split_pack_bit_exact(pkg, cuda, oracle, split_size, flags, gen):
     """The GPU alias table equals the oracle's split+pack (shader.comp:81-223) fed the GPU's
-    own partition, prefix, heavy count and mean: p bits and alias indices identical."""
+    own partition, prefix, heavy count and mean: p bits and alias indices identical (split
+    sizes up to 24 stage their walks in shared memory sized by the split size; 32 writes its
+    entries directly)."""
     N = 65536 + 123
     w = GENS[gen](N, split_size * 10 + flags)
     cfg = pkg.AliasTableConfig(split_size=split_size, split_residual_f64=bool(flags & 1),
@@ -133,7 +135,7 @@ def test_split_pack_bit_exact(pkg, cuda, oracle, split_size, flags, gen):
 
 @pytest.mark.parametrize("N", [(1 << 20) + 5, (1 << 22) + 17])
 @pytest.mark.parametrize("gen", list(GENS))
-@pytest.mark.parametrize("split_size", [2, 32])
+@pytest.mark.parametrize("split_size", [2, 16, 32])
 def test_float_float_prefix_mode(pkg, cuda, oracle, N, gen, split_size):
     """WRS_SCAN_FLOAT_FLOAT: high + low words of the partition prefix carry only the
     tile-local FP32 rounding (<= 4096 * max w * 2^-20 absolute), the table equals the oracle's
