@@ -1191,107 +1191,15 @@ __device__ __forceinline__ void compute_split(const PackIn& c, uint32_t nsplit, 
     jo = j;
 }
 
-// compute_split for kSplitPerThread splits at once: the bisections advance in lockstep so the
-// probes of all of them are in flight together (the search is latency-bound); each split
-// follows exactly compute_split's probe sequence and arithmetic.
+// compute_split's probe sequence and arithmetic for the split-pack's one split per thread,
+// started from (a, b): the bisection state after the levels every split of the CTA decides
+// alike (split_descent), or (0, hc - 1) from the top.
 //
-// (a0, b0): the bisection state after the levels every split of the CTA decides alike (see
-// split_descent); (0, hc - 1) starts from the top.
-template <bool R64, bool FF, int V>
-__device__ __forceinline__ void compute_splits(const PackIn& c, const uint32_t (&nsplit)[V],
-                                               const bool (&on)[V], uint32_t (&io)[V],
-                                               uint32_t (&jo)[V], float (&spill)[V], int a0,
-                                               int b0) {
-    int a[V], b[V];
-    float target[V];
-    ff tff[V];
-    const uint32_t lcm1 = c.lcap;
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-        a[v] = a0;
-        b[v] = on[v] ? b0 : -1;
-        target[v] = __fmul_rn(c.mean, __uint2float_rn(nsplit[v]));
-        tff[v] = FF ? ff_target(c.mean, c.mean_lo, nsplit[v]) : ff{0.f, 0.f};
-    }
-    for (;;) {
-        bool any = false;
-        float heavy[V], light[V], hl[V], ll[V];
-        uint32_t jv[V];
-        uint32_t iv[V];
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-            heavy[v] = light[v] = hl[v] = ll[v] = 0.f;
-            jv[v] = iv[v] = 0;
-            if (a[v] <= b[v]) {
-                any = true;
-                const uint32_t j = static_cast<uint32_t>(a[v] + ((b[v] - a[v]) >> 1));
-                const uint32_t i = j > nsplit[v] ? lcm1 : min(nsplit[v] - j, lcm1);
-                jv[v] = j;
-                iv[v] = i;
-                if (j) heavy[v] = __ldg(c.prefix + j - 1);
-                if (i) light[v] = __ldg(c.prefix + c.n - i);
-            }
-        }
-        if (!any) break;
-#pragma unroll
-        for (int v = 0; v < V; ++v) {
-            if (a[v] <= b[v]) {
-                bool le;
-                if constexpr (FF) {
-                    // FP32 pre-test: d = (h + l) - t differs from the float-float value
-                    // (h + hl) + (l + ll) - (t + tl) by at most 3u(h + l) + 2u t (u = 2^-24,
-                    // |lo| <= u |hi|), and the float-float evaluation is accurate to O(u^2);
-                    // beyond 8u(h + l + t) both have d's sign, so the low words are only
-                    // read near the split point and the result is unchanged.
-                    const float d = __fsub_rn(__fadd_rn(heavy[v], light[v]), tff[v].hi);
-                    const float m = __fmul_rn(4.76837158203125e-07f,  // 8 * 2^-24
-                                              __fadd_rn(__fadd_rn(heavy[v], light[v]), tff[v].hi));
-                    if (d > m) {
-                        le = false;
-                    } else if (d < -m) {
-                        le = true;
-                    } else {
-                        const uint32_t j = jv[v], i = iv[v];
-                        if (j) hl[v] = __ldg(c.prefix_lo + j - 1);
-                        if (i) ll[v] = __ldg(c.prefix_lo + c.n - i);
-                        le = ff_sigma_minus(heavy[v], hl[v], light[v], ll[v], tff[v].hi,
-                                            tff[v].lo) <= 0.0f;
-                    }
-                } else {
-                    le = __fadd_rn(light[v], heavy[v]) <= target[v];
-                }
-                if (le)
-                    a[v] = static_cast<int>(jv[v]) + 1;
-                else
-                    b[v] = static_cast<int>(jv[v]) - 1;
-            }
-        }
-    }
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-        if (!on[v]) continue;
-        const uint32_t j = b[v] < 0 ? 0u : static_cast<uint32_t>(b[v]);
-        const uint32_t i = j > nsplit[v] ? lcm1 : min(nsplit[v] - j, lcm1);
-        const float light = i == 0 ? 0.f : __ldg(c.prefix + c.n - i);
-        const float heavy2 = __ldg(c.prefix + j);
-        if constexpr (FF) {
-            const float hl2 = __ldg(c.prefix_lo + j);
-            const float l2 = i == 0 ? 0.f : __ldg(c.prefix_lo + c.n - i);
-            spill[v] = ff_sigma_minus(heavy2, hl2, light, l2, tff[v].hi, tff[v].lo);
-        } else if constexpr (R64) {
-            const double target64 =
-                __dmul_rn(static_cast<double>(c.mean), static_cast<double>(nsplit[v]));
-            spill[v] = __double2float_rn(__dsub_rn(
-                __dadd_rn(static_cast<double>(heavy2), static_cast<double>(light)), target64));
-        } else {
-            spill[v] = __fsub_rn(__fadd_rn(heavy2, light), target[v]);
-        }
-        io[v] = i;
-        jo[v] = j;
-    }
-}
-
-// one split per thread: compute_splits's probe sequence, FP32 pre-test and arithmetic for V = 1
+// FF: an FP32 pre-test decides most levels without the low words.  d = (h + l) - t differs
+// from the float-float value (h + hl) + (l + ll) - (t + tl) by at most 3u(h + l) + 2u t
+// (u = 2^-24, |lo| <= u |hi|), and the float-float evaluation is accurate to O(u^2); beyond
+// 8u(h + l + t) both have d's sign, so the low words are only read near the split point and
+// every decision is the float-float one.
 template <bool R64, bool FF>
 __device__ __forceinline__ void bisect_one(const PackIn& c, uint32_t nsplit, bool on, uint32_t& io,
                                            uint32_t& jo, float& spill, int a, int b) {
@@ -1776,6 +1684,7 @@ __global__ __launch_bounds__(kSplitThreads, 4) void k_split_pack(SplitArgs a, Ba
         int2 d0 = make_int2(0, static_cast<int>(hc) - 1);
         const int2* desc = BATCH ? bv.descent : a.descent;
         if (desc) d0 = desc[BATCH ? blockIdx.x : blk];
+        static_assert(kSplitPerThread == 1, "one bisection per thread");
         bisect_one<R64, FF>(c, nsplit[0], on[0], si[0], sj[0], sp[0], d0.x, d0.y);
     }
 #pragma unroll

@@ -17,10 +17,9 @@ constexpr int kTileWarps = kTileThreads / 32;
 constexpr int kTileItems = 4096;
 constexpr int kWarpItems = kTileItems / kTileWarps;  // 512 contiguous items per warp
 
-// Split+pack: kSplitPerThread splits per thread (their bisections interleaved; 2 measured
-// slower than 1 on GB300 at N = 2^26: the kernel is partly issue-bound);
-// kSplitSlots - kSplitLook - 1 subproblems packed per CTA, the remaining slots hold look-ahead
-// splits (see k_split_pack).
+// Split+pack: one split per thread (two bisections interleaved per thread measured slower on
+// GB300 at N = 2^26: the kernel is issue-bound); kSplitSlots - kSplitLook - 1 subproblems
+// packed per CTA, the remaining slots hold look-ahead splits (see k_split_pack).
 constexpr int kSplitThreads = 512;
 constexpr int kSplitPerThread = 1;
 constexpr int kSplitSlots = kSplitThreads * kSplitPerThread;
