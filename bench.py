@@ -1361,6 +1361,11 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
     rec("cutpoint_sample",
         timed(lambda: cp.cutpoint_sample(stream, cmf, n, guide, s, 99, 0, samples)), 4 * s, s,
         "samples")
+    # the reference's PRNG operator (wrs_philox): S uniform floats into the samples buffer,
+    # 4 B written per element
+    prng = W.PRNG()
+    floats = samples.view(torch.float32)
+    rec("philox_uniform", timed(lambda: prng.run(stream, floats, s, 7)), 4 * s, s, "elements")
     assert not internals.status() & W.DEVICE_TIMEOUT
     return out
 
