@@ -937,10 +937,10 @@ __device__ u128 scan_lookback_x(const ScanState* st, uint32_t tile, uint32_t* st
 
 // RN(k * 2^g + r), r the thread's FP32 running sum, decided from a float-float evaluation
 // where that is safe (Ziv's rounding test).  With kf = fx_to_ff(k, g) (kf.hi + kf.lo within
-// u^2 of k * 2^g, u = 2^-24 the unit roundoff), two_sum(kf.hi, r) exact, one rounding of u^2 in the low
-// words and fast_two_sum exact, v.hi + v.lo is within 3u^2 (1 + u) of the exact value X.  If
-// it lies more than 2^-44 v.hi (> 5 times that) from the midpoints between v.hi and its
-// neighbours, X rounds to v.hi; otherwise -- and for r < 0 or NaN, and values outside
+// u^2 of k * 2^g, u = 2^-24 the unit roundoff), two_sum(kf.hi, r) exact, one rounding of u^2
+// in the low words and fast_two_sum exact, v.hi + v.lo is within 3u^2 (1 + u) of the exact
+// value X.  If it lies more than 2^-44 v.hi (> 5 times that) from the midpoints between v.hi
+// and its neighbours, X rounds to v.hi; otherwise -- and for r < 0 or NaN, and values outside
 // [2^-100, 2^100], where the spacing arithmetic below is not exact -- the fixed-point path
 // rounds the exact sum, so the result is fx_round's in every case.
 __device__ __forceinline__ float cmf_round(u128 k, ff kf, float r, int g) {
