@@ -1055,6 +1055,7 @@ def small_leg(W, dev, steps: int = 20) -> dict:
     graph_build_s = e[0].elapsed_time(e[1]) / (steps * per_graph) / 1e3
     assert bufs.internals.status() == 0
     st = sample_statistics(W.Statistics(n), samples, s, w, n)  # histogram etc. on the device
+    cpu = small_cpu_path(w.cpu().numpy(), samples.cpu().numpy().view(np.uint32), s)
     return {"workload": "plain path, small: N=65,536 uniform(0,1] (seed 1), PSA build (split 2) "
                         "+ S=2^20 Philox4x32-10 samples (seed 1)",
             "builds_per_s": 1.0 / build_s, "samples_per_s": s / sample_s,
@@ -1065,7 +1066,41 @@ def small_leg(W, dev, steps: int = 20) -> dict:
             "chi2": st["chi2"], "df": st["df"], "p_value": st["p_value"],
             "z_score": st["z_score"], "rmse": st["rmse"], "rmse_ideal": st["rmse_ideal"],
             "zero_weight_draws": st["zero_weight_draws"], "binned": st["binned"],
-            "statistics": "wrs_histogram + wrs_sample_statistics on the device"}
+            "statistics": "wrs_histogram + wrs_sample_statistics on the device",
+            "cpu_baseline": cpu}
+
+
+def small_cpu_path(w_host, gpu_samples, s: int) -> dict:
+    """The small configuration's CPU path on the host: the oracle's port of the PSA build at
+    split size 2 (FP32, as the GPU's) and its Philox4x32-10 alias sampler (seed 1), on one
+    thread as the reference's CPU code runs; builds/s and samples/s, the chi-square / RMSE of
+    its histogram against the weights, and the RMSE between the GPU's and the CPU's normalised
+    histograms (two independent-looking draws of the same distribution: about sqrt(2) times
+    the ideal RMSE; the tables differ in the last bits, as the FP32 prefix sums run in
+    different orders)."""
+    import numpy as np
+    from oracle.oracle import RNG_PHILOX4X32_10, Oracle
+    orc = Oracle()
+    n = w_host.size
+    t0 = time.perf_counter()
+    table, _, _ = orc.psa_build(w_host, 2, nthreads=1)
+    t1 = time.perf_counter()
+    cs = orc.alias_sample(table, s, 1, rng=RNG_PHILOX4X32_10, nthreads=1)
+    t2 = time.perf_counter()
+    p = w_host.astype(np.float64) / float(np.sum(w_host.astype(np.float64)))
+    hc = np.bincount(cs, minlength=n).astype(np.float64)
+    hg = np.bincount(gpu_samples, minlength=n).astype(np.float64)
+    e = p * s
+    nz = e > 0
+    out = {"kind": "port", "cores": 1,
+           "sample": "the whole configuration: one PSA build of the 65,536 weights and all "
+                     "2^20 samples, one thread",
+           "build_s": t1 - t0, "builds_per_s": 1.0 / (t1 - t0),
+           "sample_s": t2 - t1, "samples_per_s": s / (t2 - t1)}
+    out.update(chi2_report(float(np.sum((hc[nz] - e[nz]) ** 2 / e[nz])), int(nz.sum()) - 1))
+    out["rmse"] = float(np.sqrt(np.mean((hc / s - p) ** 2)))
+    out["rmse_gpu_vs_cpu_histogram"] = float(np.sqrt(np.mean((hg / s - hc / s) ** 2)))
+    return out
 
 
 def chi2_report(chi2: float, df: int) -> dict:
