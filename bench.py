@@ -1075,9 +1075,9 @@ def small_cpu_path(w_host, gpu_samples, s: int) -> dict:
     split size 2 (FP32, as the GPU's) and its Philox4x32-10 alias sampler (seed 1), on one
     thread as the reference's CPU code runs; builds/s and samples/s, the chi-square / RMSE of
     its histogram against the weights, and the RMSE between the GPU's and the CPU's normalised
-    histograms (two independent-looking draws of the same distribution: about sqrt(2) times
-    the ideal RMSE; the tables differ in the last bits, as the FP32 prefix sums run in
-    different orders)."""
+    histograms (the same Philox stream over nearly the same table -- the FP32 prefix sums run
+    in different orders, so a few entries differ in their last bits -- hence far below the
+    RMSE of two independent draws)."""
     import numpy as np
     from oracle.oracle import RNG_PHILOX4X32_10, Oracle
     orc = Oracle()
