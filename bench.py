@@ -218,6 +218,25 @@ def cpu_step(w_host, n: int, s: int, nthreads: int) -> tuple[float, dict]:
     return t2 - t0, {"build_s": t1 - t0, "sample_s": t2 - t1}
 
 
+def cpu_scan_its(w_host, nthreads: int, s: int = 1 << 24) -> dict:
+    """The large configuration's other two CPU paths beside the GPU's: the Kahan inclusive
+    prefix sum of the N weights on one thread (the oracle's restatement of the reference's
+    host prefix_sum, src/host/reference/prefix_sum.hpp:17-74) and the lower-bound ITS sampler
+    (Philox4x32-10) over that CMF on all threads, on a bounded sample of s draws."""
+    from oracle.oracle import RNG_PHILOX4X32_10, Oracle
+    orc = Oracle()
+    n = w_host.size
+    t0 = time.perf_counter()
+    cmf = orc.prefix_kahan(w_host)
+    t1 = time.perf_counter()
+    orc.its_sample(cmf.astype("float32"), s, 7, rng=RNG_PHILOX4X32_10, nthreads=nthreads)
+    t2 = time.perf_counter()
+    return {"kind": "port", "scan_cores": 1, "its_cores": nthreads,
+            "sample": f"the whole N-weight scan; {s} ITS draws (a bounded sample of the 2^28)",
+            "scan_s": t1 - t0, "weights_scanned_per_s": n / (t1 - t0),
+            "its_sample_s": t2 - t1, "its_samples_per_s": s / (t2 - t1)}
+
+
 def reference_cpu(w_host, split_size: int = 32) -> dict:
     """The reference's own CPU code (oracle/_ref, compiled from its sources where the
     reference checkout is present), single-threaded as it is written: the PSA alias table
@@ -582,6 +601,7 @@ def main() -> None:
                       f"uniform weights ({desc['build_s']:.2f} s) + S=2^{args.log2s} "
                       f"Philox4x32-10 alias samples ({desc['sample_s']:.2f} s); {nthreads} "
                       "threads (the oracle's threaded port of the path)",
+            "scan_and_its": cpu_scan_its(w0, nthreads),
             "reference_cpu": reference_cpu(w0)}
     if rank == 0:
         print(json.dumps(line), flush=True)
