@@ -76,11 +76,18 @@ def max_over_ranks(x: float, dist, device) -> float:
 
 
 def headline_config(n: int, s: int, world: int) -> dict:
-    """The headline configuration, the same for both arms."""
-    return {"workload": WORKLOAD, "N": n, "S": s, "split_size": SPLIT_SIZE,
+    """The headline configuration, the same for both arms (other sizes, from --log2n /
+    --log2s, are named as what they are)."""
+    workload = WORKLOAD
+    l2 = "inputs larger than L2 (256 MB weights, 512 MB table, 1 GB samples)"
+    if (n, s) != (1 << LOG2_N, 1 << LOG2_S):
+        workload = WORKLOAD.replace("N=2^26", f"N=2^{n.bit_length() - 1}").replace(
+            "S=2^28", f"S=2^{s.bit_length() - 1}")
+        l2 = (f"{4 * n >> 20} MB weights, {8 * n >> 20} MB table, {4 * s >> 20} MB samples "
+              "(L2: 129 MB)")
+    return {"workload": workload, "N": n, "S": s, "split_size": SPLIT_SIZE,
             "rng": "philox4x32-10", "precision": "float-float partition prefix",
-            "split": "float-float residual, light cap fixed",
-            "l2": "inputs larger than L2 (256 MB weights, 512 MB table, 1 GB samples)",
+            "split": "float-float residual, light cap fixed", "l2": l2,
             "parallelism": f"replicas x{world}"}
 
 
