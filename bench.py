@@ -778,6 +778,7 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int, cpu: bool = True) 
     # p-value, the RMSE of the normalised histogram and the RMSE a multinomial draw has in
     # expectation; aggregated as the sum of the chi-squares over the sum of the dfs
     rmse, rmse_ratio, chi2s, dfs, pvals, bchi2, bdfs, bpvals = [], [], [], [], [], [], [], []
+    vars_, pvals_m, bvars = [], [], []
     for d in range(D):
         n, s = int(sizes[d]), int(counts[d])
         if s == 0:
@@ -794,13 +795,18 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int, cpu: bool = True) 
         rmse_ratio.append(r / float(torch.sqrt(torch.mean(p * (1 - p) / s))))
         chi2s.append(chi2)
         dfs.append(int(pos.sum()) - 1)
-        pvals.append(chi2_report(chi2, dfs[-1])["p_value"])
+        vars_.append(multinomial_chi2_var(p, s))
+        rep = chi2_report(chi2, dfs[-1], vars_[-1])
+        pvals.append(rep["p_value"])
+        pvals_m.append(rep.get("p_value_multinomial"))
         b = binned_chi2(o, e, 256.0)
         if b["df"] > 0:
             bchi2.append(b["chi2"])
             bdfs.append(b["df"])
+            bvars.append(multinomial_chi2_var(p_binned(e, b["bin_items"]), s))
             bpvals.append(b["p_value"])
     pv = [x for x in pvals if x is not None]
+    pvm = [x for x in pvals_m if x is not None]
     bpv = [x for x in bpvals if x is not None]
     total_s = int(counts.sum())
     return {
@@ -824,17 +830,20 @@ def batched_leg(W, cfg, dev, stream, steps: int, warmup: int, cpu: bool = True) 
         "samples_bitwise_equal": identical,
         "rmse_mean": statistics.mean(rmse), "rmse_max": max(rmse),
         "statistics": {
-            **chi2_report(sum(chi2s), sum(dfs)),
+            **chi2_report(sum(chi2s), sum(dfs), sum(vars_)),
             "what": "sum over the distributions of the reference's chi-square (its items with "
                     "nonzero expectation, df = items - 1 each) and its p-value; per "
-                    "distribution p-values summarised",
+                    "distribution p-values summarised; *_multinomial: against the statistic's "
+                    "exact multinomial variance (the sum over the distributions)",
             "rmse_mean": statistics.mean(rmse),
             "rmse_over_ideal_mean": statistics.mean(rmse_ratio),
             "rmse_over_ideal_max": max(rmse_ratio),
             "p_value_min": min(pv) if pv else None,
             "p_below_0.01_fraction": (sum(x < 0.01 for x in pv) / len(pv)) if pv else None,
+            "p_multinomial_below_0.01_fraction": (sum(x < 0.01 for x in pvm) / len(pvm))
+            if pvm else None,
             "distributions": len(chi2s),
-            "binned": {**chi2_report(sum(bchi2), sum(bdfs)),
+            "binned": {**chi2_report(sum(bchi2), sum(bdfs), sum(bvars)),
                        "what": "per distribution the chi-square over bins of consecutive items "
                                "with a mean expectation of >= 256 samples (a distribution "
                                "that fills one bin has none), summed",
@@ -897,7 +906,7 @@ def served_leg(W, cfg, dev, n_requests: int = SERVED_REQUESTS) -> dict:
     tab = torch.empty(2 * int(wl["n"].max()), dtype=torch.int32, device=dev)
     alone = torch.empty(int(wl["s"].max()), dtype=torch.int32, device=dev)
     equal = 0
-    chi2s, dfs, ratios, bchi2, bdfs = [], [], [], [], []
+    chi2s, dfs, ratios, bchi2, bdfs, vars_, bvars = [], [], [], [], [], [], []
     for i in pick:
         n, s_i = int(wl["n"][i]), int(wl["s"][i])
         batch.set(None, [(wp + 4 * int(wl["w_off"][i]), tab, alone, n, s_i, int(wl["seeds"][i]))])
@@ -913,10 +922,12 @@ def served_leg(W, cfg, dev, n_requests: int = SERVED_REQUESTS) -> dict:
         pos = e > 0
         chi2s.append(float((((o - e) ** 2)[pos] / e[pos]).sum()))
         dfs.append(int(pos.sum()) - 1)
+        vars_.append(multinomial_chi2_var(p, s_i))
         b = binned_chi2(o, e, 64.0)
         if b["df"] > 0:
             bchi2.append(b["chi2"])
             bdfs.append(b["df"])
+            bvars.append(multinomial_chi2_var(p_binned(e, b["bin_items"]), s_i))
         ratios.append(float(torch.sqrt(torch.mean((o / s_i - p) ** 2))) /
                       float(torch.sqrt(torch.mean(p * (1 - p) / s_i))))
     return {
@@ -935,14 +946,16 @@ def served_leg(W, cfg, dev, n_requests: int = SERVED_REQUESTS) -> dict:
         "scratch_bytes": st["scratch_bytes"], "device_status": st["device_status"],
         "alone_vs_mix_equal": f"{equal}/{len(pick)}",
         "statistics": {
-            **chi2_report(sum(chi2s), sum(dfs)),
+            **chi2_report(sum(chi2s), sum(dfs), sum(vars_)),
             "what": f"the {len(pick)} alone-vs-mix requests' served samples: sum of the "
                     "reference's chi-squares over their items (df = items - 1 each) and its "
-                    "p-value (most requests draw far fewer samples than they have items, so "
-                    "the RMSE ratio is the sharper check)",
+                    "p-value; most requests draw far fewer samples than they have items, where "
+                    "the chi-square distribution does not describe the statistic: "
+                    "*_multinomial holds it against its exact multinomial variance (summed "
+                    "over the requests) instead",
             "rmse_over_ideal_mean": statistics.mean(ratios),
             "rmse_over_ideal_max": max(ratios),
-            "binned": {**chi2_report(sum(bchi2), sum(bdfs)),
+            "binned": {**chi2_report(sum(bchi2), sum(bdfs), sum(bvars)),
                        "what": "per request the chi-square over bins of consecutive items with "
                                "a mean expectation of >= 64 samples (requests of fewer samples "
                                "fill one bin and have none), summed",
@@ -1130,22 +1143,42 @@ def small_cpu_path(w_host, gpu_samples, s: int) -> dict:
                      "2^20 samples, one thread",
            "build_s": t1 - t0, "builds_per_s": 1.0 / (t1 - t0),
            "sample_s": t2 - t1, "samples_per_s": s / (t2 - t1)}
-    out.update(chi2_report(float(np.sum((hc[nz] - e[nz]) ** 2 / e[nz])), int(nz.sum()) - 1))
+    out.update(chi2_report(float(np.sum((hc[nz] - e[nz]) ** 2 / e[nz])), int(nz.sum()) - 1,
+                           multinomial_chi2_var(p, s)))
     out["rmse"] = float(np.sqrt(np.mean((hc / s - p) ** 2)))
     out["rmse_gpu_vs_cpu_histogram"] = float(np.sqrt(np.mean((hg / s - hc / s) ** 2)))
     return out
 
 
-def chi2_report(chi2: float, df: int) -> dict:
+def multinomial_chi2_var(p, s: int) -> float:
+    """The exact variance of Pearson's chi-square over the k cells with p > 0 when s samples are
+    drawn from the probabilities p (a numpy array or torch tensor): 2 (k - 1) + (sum 1/p - k^2
+    - 2 k + 2) / s; its mean is k - 1 exactly.  Where the expected counts s p are small the
+    sum of 1/p dominates, and the chi-square distribution's variance 2 (k - 1) understates the
+    statistic's spread many times over."""
+    q = p[p > 0]
+    k = float(q.shape[0])
+    inv = float((1.0 / q).sum())
+    return 2.0 * (k - 1.0) + (inv - k * k - 2.0 * k + 2.0) / float(s)
+
+
+def chi2_report(chi2: float, df: int, var: float | None = None) -> dict:
     """The chi-square statistic with its degrees of freedom, upper-tail p-value (scipy) and the
-    reference's z-score (chi2 - df) / sqrt(2 df) (src/host/statistics/chi_square.hpp:11-15)."""
+    reference's z-score (chi2 - df) / sqrt(2 df) (src/host/statistics/chi_square.hpp:11-15).
+    With `var`, the statistic's exact multinomial variance (multinomial_chi2_var, summed over
+    independent draws), also the z-score against that spread and its normal upper-tail
+    p-value: the check that stays valid where items' expected counts are far below 5."""
     try:
         from scipy.stats import chi2 as chi2_dist
         p = float(chi2_dist.sf(chi2, df)) if df > 0 else None
     except ImportError:
         p = None
-    return {"chi2": chi2, "df": df, "p_value": p,
-            "z_score": (chi2 - df) / math.sqrt(2.0 * df) if df > 0 else None}
+    out = {"chi2": chi2, "df": df, "p_value": p,
+           "z_score": (chi2 - df) / math.sqrt(2.0 * df) if df > 0 else None}
+    if var is not None and var > 0 and df > 0:
+        z = (chi2 - df) / math.sqrt(var)
+        out.update({"z_multinomial": z, "p_value_multinomial": 0.5 * math.erfc(z / math.sqrt(2.0))})
+    return out
 
 
 def binned_chi2(o, e, target: float) -> dict:
@@ -1154,23 +1187,35 @@ def binned_chi2(o, e, target: float) -> dict:
     least `target`: the chi-square distribution describes the statistic only where expected
     counts are large, which item by item they are not for skewed weights.  Bins with no
     expectation are left out; df = bins - 1."""
-    import torch
     n = int(e.numel())
     mean_e = float(e.sum()) / max(n, 1)
     G = 1
     while G < n and G * mean_e < target:
         G *= 2
-    pad = (-n) % G
-    if pad:
-        o = torch.cat([o, o.new_zeros(pad)])
-        e = torch.cat([e, e.new_zeros(pad)])
-    O = o.view(-1, G).sum(1)
-    E = e.view(-1, G).sum(1)
+    O = bin_sums(o, G)
+    E = bin_sums(e, G)
     keep = E > 0
     chi2 = float((((O - E) ** 2)[keep] / E[keep]).sum())
     bins = int(keep.sum())
-    return {**chi2_report(chi2, bins - 1), "bin_items": G,
+    total = float(E.sum())
+    var = multinomial_chi2_var(E / total, round(total)) if bins > 1 else None
+    return {**chi2_report(chi2, bins - 1, var), "bin_items": G,
             "min_expected": float(E[keep].min()) if bins else None}
+
+
+def bin_sums(x, G: int):
+    """Sums of G consecutive entries of the device tensor x (the last bin zero-padded)."""
+    import torch
+    pad = (-int(x.numel())) % G
+    if pad:
+        x = torch.cat([x, x.new_zeros(pad)])
+    return x.view(-1, G).sum(1)
+
+
+def p_binned(e, G: int):
+    """The bin probabilities of binned_chi2's bins of G items, from expected counts e."""
+    E = bin_sums(e, G)
+    return E / E.sum()
 
 
 def sample_statistics(stats, samples, s: int, w, n: int, bin_target: float = 1024.0) -> dict:
@@ -1186,7 +1231,7 @@ def sample_statistics(stats, samples, s: int, w, n: int, bin_target: float = 102
     w64 = w[:n].double()
     total = w64.sum()
     p = w64 / total
-    out = chi2_report(r["chi2"], int((w64 > 0).sum()) - 1)
+    out = chi2_report(r["chi2"], int((w64 > 0).sum()) - 1, multinomial_chi2_var(p, s))
     out.update({"rmse": r["rmse"], "rmse_ideal": float(torch.sqrt(torch.mean(p * (1 - p) / s))),
                 "zero_weight_draws": r["zero_weight_draws"],
                 "binned": binned_chi2(stats.hist[:n].double(), p * s, bin_target)})

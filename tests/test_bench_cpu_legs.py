@@ -41,3 +41,48 @@ def test_headline_config_names_its_sizes():
     assert "N=2^20" in small["workload"] and "S=2^22" in small["workload"]
     assert "2^26" not in small["workload"] and small["parallelism"] == "replicas x2"
     assert np.all([small["N"] == 1 << 20, small["S"] == 1 << 22])
+
+
+def test_multinomial_chi2_variance():
+    """The exact variance of Pearson's chi-square matches simulated multinomial draws at
+    expected counts far below 5 (about 0.1 per item), where the chi-square distribution's
+    2 (k - 1) is about half the true spread."""
+    import bench
+    rng = np.random.default_rng(3)
+    k, s, reps = 200, 20, 20000
+    p = rng.uniform(0.2, 1.0, k)
+    p /= p.sum()
+    e = s * p
+    x2 = ((rng.multinomial(s, p, size=reps) - e) ** 2 / e).sum(1)
+    var = bench.multinomial_chi2_var(p, s)
+    assert var > 1.5 * 2 * (k - 1)
+    assert abs(x2.mean() - (k - 1)) < 4 * np.sqrt(var / reps)
+    assert abs(x2.var(ddof=1) / var - 1.0) < 0.08
+    # zero-probability cells are left out, as the chi-square leaves them out
+    assert bench.multinomial_chi2_var(np.concatenate([p, [0.0, 0.0]]), s) == var
+
+
+def test_chi2_report_multinomial_fields():
+    import bench
+    r = bench.chi2_report(99.0, 99, 400.0)
+    assert r["z_multinomial"] == 0.0 and abs(r["p_value_multinomial"] - 0.5) < 1e-12
+    r = bench.chi2_report(99.0 + 2 * 20.0, 99, 400.0)
+    assert abs(r["z_multinomial"] - 2.0) < 1e-12
+    assert abs(r["p_value_multinomial"] - 0.022750131948179) < 1e-9
+    assert "z_multinomial" not in bench.chi2_report(99.0, 99)
+
+
+def test_binned_chi2_bins_and_variance():
+    """Bins of G consecutive items with a mean expectation of at least the target; the bin
+    probabilities p_binned gives are those the statistic uses."""
+    import torch
+    import bench
+    n, s = 1000, 4000
+    p = torch.full((n,), 1.0 / n, dtype=torch.float64)
+    o = torch.bincount(torch.randint(0, n, (s,), generator=torch.Generator().manual_seed(1)),
+                       minlength=n).double()
+    r = bench.binned_chi2(o, p * s, 64.0)
+    assert r["bin_items"] == 16 and r["df"] == (n + 15) // 16 - 1
+    pb = bench.p_binned(p * s, 16)
+    assert abs(float(pb.sum()) - 1.0) < 1e-12 and pb.numel() == 63
+    assert "p_value_multinomial" in r
