@@ -1045,7 +1045,9 @@ def precision_leg(W, dev, log2n: int = 28, log2s: int = 30) -> dict:
         tables[name] = {"max_abs_err_mean_units": float(err.max()),
                         "max_rel_err_w_ge_mean": float((err / mean_units)[mean_units >= 1].max()),
                         "alias_rmse": r["rmse"], "chi2": r["chi2"], "df": r["df"],
-                        "p_value": r["p_value"], "z_score": r["z_score"], "binned": r["binned"],
+                        "p_value": r["p_value"], "z_score": r["z_score"],
+                        "z_multinomial": r.get("z_multinomial"),
+                        "p_value_multinomial": r.get("p_value_multinomial"), "binned": r["binned"],
                         "zero_weight_draws": r["zero_weight_draws"],
                         "zero_weight_mass": float(imp[w == 0].sum()),
                         "status": internals.status()}
@@ -1110,7 +1112,9 @@ def small_leg(W, dev, steps: int = 20) -> dict:
             "graph_note": "per-call builds from a Python loop over the C ABI include the host's "
                           "launch gaps; graph_* replays 8 builds captured in one CUDA graph",
             "chi2": st["chi2"], "df": st["df"], "p_value": st["p_value"],
-            "z_score": st["z_score"], "rmse": st["rmse"], "rmse_ideal": st["rmse_ideal"],
+            "z_score": st["z_score"], "z_multinomial": st.get("z_multinomial"),
+            "p_value_multinomial": st.get("p_value_multinomial"),
+            "rmse": st["rmse"], "rmse_ideal": st["rmse_ideal"],
             "zero_weight_draws": st["zero_weight_draws"], "binned": st["binned"],
             "statistics": "wrs_histogram + wrs_sample_statistics on the device",
             "cpu_baseline": cpu}
