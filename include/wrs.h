@@ -418,7 +418,7 @@ wrs_status wrs_server_run_trace(wrs_server* s, const wrs_request* reqs,
 /* ---- sample statistics on the device (src/device/statistics) --------------------------
  * wrs_histogram: hist[samples[i]] += 1 for i < s (Histogram / AtomicHistogram,
  * statistics/histogram/atomic/shader.comp); hist is n device uint64 counters the caller zeroes
- * first; an index >= n is counted nowhere and sets bit 4 of *device_status (a device word).
+ * first; an index >= n is counted nowhere and ORs 4 into *device_status (a device word).
  * wrs_sample_statistics: from a histogram of s samples and the n weights, writes four device
  * doubles to out: the chi-square statistic sum over e_i > 0 of (o_i - e_i)^2 / e_i with
  * e_i = w_i * s / total (ChiSquare, statistics/chi_square/reduce/shader.comp), the RMSE
