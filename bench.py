@@ -61,6 +61,7 @@ METRIC = "samples/s"
 SPLIT_SIZE = 12
 # end-to-end: the samples of a step leave the device in this many pieces
 E2E_CHUNKS = 8
+E2E_PASSES = 5
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "alias_sample_n26_s28.md")
 
 
@@ -519,10 +520,14 @@ def main() -> None:
         torch.cuda.synchronize()
         return max_over_ranks(t0.elapsed_time(t1), dist, dev)
 
-    # three timed passes of the pipelined loop, the median reported (one transient stall of the
-    # host loop took a pass to about the serial figure once); the passes are in the line
-    e2e_passes = sorted(e2e_time(e2e_step) for _ in range(3))
-    e2e_ms = e2e_passes[1]
+    # five timed passes of the pipelined loop, the median reported: run alone the loop repeats
+    # to 0.1 % (16 passes in two processes, 41.28-41.36 G samples/s on one box), but inside
+    # the benchmark one or two of three passes have fallen to 24-38 G while the others ran at
+    # 41.3 G, so one or two disturbed passes do not set the figure; all passes are in the
+    # line, in the order they ran
+    e2e_order = [e2e_time(e2e_step) for _ in range(E2E_PASSES)]
+    e2e_passes = sorted(e2e_order)
+    e2e_ms = e2e_passes[len(e2e_passes) // 2]
     e2e_value = world * args.steps * s / (e2e_ms / 1e3)
     e2e_k2h_value = world * args.steps * s / (e2e_time(e2e_kernel_to_host_step) / 1e3)
     e2e_serial_value = world * args.steps * s / (e2e_time(e2e_serial_step) / 1e3)
@@ -570,9 +575,9 @@ def main() -> None:
                           f"{E2E_CHUNKS} pieces into one of two device buffers, each piece "
                           "copied to pinned host memory on an output stream as soon as it is "
                           "drawn (overlaps the rest of the step and the next build); the median "
-                          f"of three timed passes of {args.steps} steps",
+                          f"of {E2E_PASSES} timed passes of {args.steps} steps",
                 "passes_samples_per_s": [world * args.steps * s / (ms / 1e3)
-                                         for ms in e2e_passes],
+                                         for ms in e2e_order],
                 "kernel_to_host_value": e2e_k2h_value,
                 "serial_value": e2e_serial_value,
                 "host_link": link},
