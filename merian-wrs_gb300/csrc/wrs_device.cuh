@@ -77,12 +77,6 @@ __device__ __forceinline__ float carry_apply(ff c, float x) {
     }
 }
 
-// carry + x as a float-float pair; .hi equals carry_apply<true>(c, x)
-__device__ __forceinline__ ff carry_apply_ff(ff c, float x) {
-    ff s = two_sum(c.hi, x);
-    return fast_two_sum(s.hi, __fadd_rn(s.lo, c.lo));
-}
-
 __device__ __forceinline__ ff shfl_xor_ff(ff v, int m) {
     return {__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
 }
@@ -353,23 +347,12 @@ __device__ __forceinline__ uint2 ld_entry(const uint2* p) {
     return v;
 }
 
-// L2 eviction policies (createpolicy) and read-only loads that carry one: data read once at
-// random (a large CMF) is marked evict-first so that it does not push a small table read by
-// every sample (a guiding table) out of L2, which is marked evict-last.
+// An L2 eviction policy (createpolicy) and read-only loads that carry it: data read once at
+// random (a large CMF, the ITS cell blocks) is marked evict-first.
 __device__ __forceinline__ uint64_t l2_policy_evict_first() {
     uint64_t p;
     asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
     return p;
-}
-__device__ __forceinline__ uint64_t l2_policy_evict_last() {
-    uint64_t p;
-    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-    return p;
-}
-__device__ __forceinline__ uint32_t ld_u32_policy(const uint32_t* p, uint64_t pol) {
-    uint32_t v;
-    asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
-    return v;
 }
 __device__ __forceinline__ float ld_f32_policy(const float* p, uint64_t pol) {
     float v;
@@ -395,10 +378,6 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 // makes initialised mbarriers visible to the async proxy (the bulk copies)
 __device__ __forceinline__ void mbar_init_fence() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-// orders this thread's earlier shared-memory accesses before later async-proxy ones
-__device__ __forceinline__ void fence_proxy_async_smem() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
@@ -440,20 +419,6 @@ __device__ __forceinline__ void ld_u32x8(const uint32_t* p, uint4& a, uint4& b) 
                  : "=r"(a.x), "=r"(a.y), "=r"(a.z), "=r"(a.w), "=r"(b.x), "=r"(b.y), "=r"(b.z),
                    "=r"(b.w)
                  : "l"(p));
-}
-__device__ __forceinline__ uint4 ld_u32x4_policy(const uint32_t* p, uint64_t pol) {
-    uint4 v;
-    asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(p), "l"(pol));
-    return v;
-}
-__device__ __forceinline__ float4 ld_f32x4_policy(const float4* p, uint64_t pol) {
-    float4 v;
-    asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
-                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-                 : "l"(p), "l"(pol));
-    return v;
 }
 
 }  // namespace wrs
