@@ -132,12 +132,13 @@ def peaks() -> dict:
 
 
 def profiled_traffic(l2_fetch: int) -> float | None:
-    """DRAM bytes of one headline alias-sampling launch at the given L2 fetch granularity,
-    from the committed ncu summary (a line `dram_bytes_per_launch[l2=B]: X` per granularity),
-    if it holds that granularity."""
+    """DRAM bytes of one headline alias-sampling launch (with the tables' coin filters, the
+    mean over the three distributions' launches) at the given L2 fetch granularity, from the
+    committed ncu summary (a line `dram_bytes_per_launch_coin_filter[l2=B]: X` per captured
+    granularity), if it holds that granularity."""
     if not os.path.exists(PROFILE_TRAFFIC):
         return None
-    key = f"dram_bytes_per_launch[l2={l2_fetch}]:"
+    key = f"dram_bytes_per_launch_coin_filter[l2={l2_fetch}]:"
     for line in open(PROFILE_TRAFFIC):
         if line.strip().startswith(key):
             return float(line.split(":", 1)[1].split()[0])
@@ -544,10 +545,15 @@ def main() -> None:
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
                 "traffic_l2_fetch": tune["l2_fetch"],
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
-                                  "headline launch at this run's L2 fetch granularity "
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per "
+                                  "headline launch (mean of the uniform, Zipf and log-normal "
+                                  "launches, coin filters in use) at this run's L2 fetch "
+                                  "granularity, null where none was captured at it "
                                   "(profiles/alias_sample_n26_s28.md)",
-                "kernel": "k_alias_sample", "bytes_model": "12 B/sample (8 B entry + 4 B index)",
+                "kernel": "k_alias_sample",
+                "bytes_model": "12 B/sample (8 B entry + 4 B index), as without the coin "
+                               "filter; with it the entry is read only where the coin does "
+                               "not decide (plus 1 B of filter from L2)",
                 "peak_source": pk["source"],
                 "sector_model_frac": (36.0 * s / samp_s / 1e9) / pk["hbm_gbs"],
                 "random_gather": {
@@ -1400,6 +1406,11 @@ def kernel_breakdown(W, pkg, wrs, internals, weights, samples, n, s, stream, pea
     rec("alias_sample",
         timed(lambda: wrs.alias_sample(stream, table, n, s, 99, 0, samples)), 12 * s, s,
         "samples")
+    # the same draws through the buffers after a build, i.e. with the table's coin filter
+    ab = W.WRSBuffers(w, samples, internals)
+    wrs.build(stream, ab, n)
+    rec("alias_sample_coin_filter",
+        timed(lambda: wrs.sample(stream, ab, n, s, seed=99)), 12 * s, s, "samples")
     # serial split-pack (split records + pack from them), the two pack strategies, against the
     # inline split-pack at the same split size
     serial = {}

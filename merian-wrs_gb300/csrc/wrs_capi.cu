@@ -54,6 +54,8 @@ struct wrs_buffers {
     TreeBlock* tree = nullptr;   // ITS bisection: the probe tree's stored block levels
     uint32_t tree_n = 0;         // the n the last build stored them for (0: none)
     uint32_t cells_n = 0;        // the n the last build wrote the ITS cell blocks for (0: none)
+    uint8_t* coins = nullptr;    // alias: the table's coin filter (n bytes, kCoinMinN < n)
+    uint32_t coins_n = 0;        // the n the last build wrote the coin filter for (0: none)
     uint32_t* coarse = nullptr;  // scratch of the guiding-table / cell construction
     uint32_t* tile_scratch = nullptr;  // block-wise baselines: 3 words per tile
     int2* descent = nullptr;           // split-pack: shared bisection tops per CTA
@@ -85,7 +87,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct Layout {
     size_t ctrl, partials, part_states, scan_states, idx, prefix, elems, prefix_lo, table, records,
-        cmf, guide, cells, tree, coarse, tile_scratch, descent, total;
+        coins, cmf, guide, cells, tree, coarse, tile_scratch, descent, total;
 };
 
 // ITS bisects the whole CMF with the non-cooperative sampler, and its CMF is deep enough for
@@ -124,6 +126,7 @@ Layout layout_for(const wrs_config& cfg, uint32_t max_n) {
                           ? take(sizeof(float) * static_cast<size_t>(max_n))
                           : 0;
         L.table = take(sizeof(uint2) * static_cast<size_t>(max_n));
+        L.coins = max_n > kCoinMinN ? take(std::min(max_n, kCoinMaxN)) : 0;
         L.descent = take(sizeof(int2) * static_cast<size_t>(descent_entries(max_n)));
         L.records = cfg.split_pack_mode != WRS_SPLITPACK_INLINE
                         ? take(sizeof(SplitRecord) * records_for(max_n, cfg.split_size))
@@ -275,6 +278,7 @@ wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers**
                            ? reinterpret_cast<float*>(p + L.prefix_lo)
                            : nullptr;
         b->table = reinterpret_cast<uint2*>(p + L.table);
+        b->coins = L.coins ? reinterpret_cast<uint8_t*>(p + L.coins) : nullptr;
         b->descent = reinterpret_cast<int2*>(p + L.descent);
         b->records = L.records ? reinterpret_cast<SplitRecord*>(p + L.records) : nullptr;
     } else {
@@ -384,6 +388,7 @@ wrs_status wrs_split_pack(const wrs_handle* h, void* stream, const float* weight
     wrs_status s = check_n(b, n);
     if (s != WRS_OK) return s;
     if (h->cfg.split_size == 0) return fail(WRS_ERR_INVALID_ARG, "split_size must be >= 1");
+    b->coins_n = 0;  // the table may be the buffers' own: its coin filter no longer holds
     WRS_CUDA(launch_split_pack(as_stream(stream), h->cfg.split_residual_f64 != 0,
                                h->cfg.split_full_light != 0, weights, partition_indices,
                                partition_elements, partition_prefix, partition_prefix_lo, b->ctrl,
@@ -452,6 +457,7 @@ wrs_status wrs_pack(const wrs_handle* h, void* stream, const float* weights,
     if (h->cfg.split_size == 0) return fail(WRS_ERR_INVALID_ARG, "split_size must be >= 1");
     const SplitRecord* r = reinterpret_cast<const SplitRecord*>(records);
     uint2* t = reinterpret_cast<uint2*>(table);
+    b->coins_n = 0;  // the table may be the buffers' own: its coin filter no longer holds
     const bool fl = h->cfg.split_full_light != 0;
     WRS_CUDA(h->cfg.split_pack_mode == WRS_SPLITPACK_SERIAL_SUBGROUP
                  ? launch_pack_records_warp(as_stream(stream), fl, weights, partition_indices,
@@ -471,7 +477,8 @@ wrs_status wrs_alias_sample(const wrs_handle* h, void* stream, const wrs_alias_e
     if (n == 0 || n > kMaxN) return fail(WRS_ERR_INVALID_ARG, "n out of range");
     if (s == 0) return WRS_OK;
     WRS_CUDA(launch_alias_sample(as_stream(stream), h->cfg.rng, h->cfg.coop_size,
-                                 reinterpret_cast<const uint2*>(table), n, s, seed, offset, samples),
+                                 reinterpret_cast<const uint2*>(table), nullptr, nullptr, n, s,
+                                 seed, offset, samples),
              "alias sample");
     return WRS_OK;
 }
@@ -560,6 +567,7 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
         return fail(WRS_ERR_INVALID_ARG, "buffers were created without the float-float prefix");
     float* elems = h->cfg.use_partition_elements ? b->elems : nullptr;
     float* lo = float_float(h) ? b->prefix_lo : nullptr;
+    b->coins_n = 0;
     WRS_CUDA(launch_total_mass(st, weights, n, b->partials, b->ctrl), "total mass");
     WRS_CUDA(launch_prefix_partition(st, comp, weights, n, b->ctrl, b->part_states, b->cap_tiles,
                                      b->idx, b->prefix, elems, lo),
@@ -582,12 +590,17 @@ wrs_status wrs_build(const wrs_handle* h, void* stream, const float* weights, ui
                                            &b->ctrl->status, n, h->cfg.split_size, b->records,
                                            b->table),
                  "pack");
-        return WRS_OK;
+    } else {
+        WRS_CUDA(launch_split_pack(st, h->cfg.split_residual_f64 != 0,
+                                   h->cfg.split_full_light != 0, weights, b->idx, elems, b->prefix,
+                                   lo, b->ctrl, &b->ctrl->status, n, h->cfg.split_size, b->table,
+                                   b->descent),
+                 "split pack");
     }
-    WRS_CUDA(launch_split_pack(st, h->cfg.split_residual_f64 != 0, h->cfg.split_full_light != 0,
-                               weights, b->idx, elems, b->prefix, lo, b->ctrl, &b->ctrl->status, n,
-                               h->cfg.split_size, b->table, b->descent),
-             "split pack");
+    if (b->coins && n > kCoinMinN && n <= kCoinMaxN) {
+        WRS_CUDA(launch_coin_filter(st, b->table, n, b->coins, &b->ctrl->coin_sum), "coin filter");
+        b->coins_n = n;
+    }
     return WRS_OK;
 }
 
@@ -628,6 +641,15 @@ wrs_status wrs_sample_at(const wrs_handle* h, void* stream, const wrs_buffers* b
     }
     if (h->cfg.method == WRS_METHOD_CUTPOINT)
         return wrs_cutpoint_sample(h, stream, b->cmf, n, b->guide, s, seed, offset, samples);
+    if (b->coins && b->coins_n == n && s) {
+        // the table's coin filter, written by the last build for this n: the same samples with
+        // the table read only where the coin does not decide
+        if (!samples) return fail(WRS_ERR_INVALID_ARG, "NULL argument");
+        WRS_CUDA(launch_alias_sample(as_stream(stream), h->cfg.rng, h->cfg.coop_size, b->table,
+                                     b->coins, &b->ctrl->coin_sum, n, s, seed, offset, samples),
+                 "alias sample");
+        return WRS_OK;
+    }
     return wrs_alias_sample(h, stream, reinterpret_cast<const wrs_alias_entry*>(b->table), n, s,
                             seed, offset, samples);
 }

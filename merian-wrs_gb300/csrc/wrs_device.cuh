@@ -346,6 +346,14 @@ __device__ __forceinline__ uint2 ld_entry(const uint2* p) {
                  : "l"(p));
     return v;
 }
+// ld_entry carrying an L2 eviction policy (createpolicy)
+__device__ __forceinline__ uint2 ld_entry_policy(const uint2* p, uint64_t pol) {
+    uint2 v;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+                 : "=r"(v.x), "=r"(v.y)
+                 : "l"(p), "l"(pol));
+    return v;
+}
 
 // An L2 eviction policy (createpolicy) and read-only loads that carry it: data read once at
 // random (a large CMF, the ITS cell blocks) is marked evict-first.

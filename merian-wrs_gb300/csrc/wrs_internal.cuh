@@ -53,7 +53,9 @@ struct alignas(64) BuildCtrl {
     LbCtrl scan;         // scan launches
     double mean64;       // total / N in FP64
     float mean_lo;       // (float)(mean64 - mean): mean64 as the float-float pair (mean, mean_lo)
-    uint32_t pad[15];
+    uint32_t pad0;
+    unsigned long long coin_sum;  // sum of the table's coin-filter codes (k_coin_filter)
+    uint32_t pad[12];
 };
 static_assert(sizeof(BuildCtrl) == 128, "BuildCtrl layout");
 
@@ -188,9 +190,24 @@ cudaError_t launch_split_pack(cudaStream_t st, bool r64, bool full_light, const 
                               const uint32_t* idx, const float* elems, const float* prefix,
                               const float* prefix_lo, const BuildCtrl* ctrl, uint32_t* status,
                               uint32_t n, uint32_t split_size, uint2* table, int2* descent);
+// coins / coin_sum: the table's coin filter and the sum of its codes (k_coin_filter), or
+// nullptr; samples are the same either way
 cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, const uint2* table,
+                                const uint8_t* coins, const unsigned long long* coin_sum,
                                 uint32_t n, uint64_t s, uint64_t seed, uint64_t offset,
                                 uint32_t* out);
+// the filter and, into *coin_sum (zeroed first, on the stream), the sum of its codes
+cudaError_t launch_coin_filter(cudaStream_t st, const uint2* table, uint32_t n, uint8_t* coins,
+                               unsigned long long* coin_sum);
+// Tables of kCoinMinN < n <= kCoinMaxN weights get a coin filter (n bytes): a smaller table
+// stays in L2 by itself, and a larger filter would not.  The sampler consults it when the
+// codes average at least kCoinMinMean (out of 255): then at most ~78 % of the samples read
+// their entry.  Measured at N = 2^26 on a box whose plain sampler takes 5.13 ms for 2^28
+// samples, the filtered one took 0.66 + 5.45 f ms with f the share of samples reading their
+// entry (f = 0.42 uniform, 0.75 log-normal(0, 2), 0.88 Zipf(1.1): 2.94 / 4.77 / 5.59 ms).
+constexpr uint32_t kCoinMinN = 1u << 22;
+constexpr uint32_t kCoinMaxN = 1u << 26;
+constexpr uint64_t kCoinMinMean = 56;
 // The non-cooperative ITS sampler's bisection probes one implicit binary tree (node k, root
 // 1: the range left by the decisions spelled by the bits of k below its leading one).  The
 // build stores the tree's levels as blocks of three levels -- a node and its 6 descendants, 7

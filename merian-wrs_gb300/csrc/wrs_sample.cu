@@ -28,16 +28,34 @@ __device__ __forceinline__ float mix_rn(float x, float y, float a) {
     return __fadd_rn(__fmul_rn(x, __fsub_rn(1.0f, a)), __fmul_rn(y, a));
 }
 
-// Samples [block * 1024 + 4t, +4) of one distribution (thread t of the CTA).
-template <uint32_t RNG, bool COOP>
-__device__ __forceinline__ void alias_block(const uint2* __restrict__ table, uint32_t n,
-                                            uint64_t S, uint64_t seed, uint64_t offset,
-                                            uint32_t coop, uint32_t* __restrict__ out,
-                                            uint64_t block) {
+// The coin filter of a table: per bucket one byte q = floor(256 p) (255 for p >= 1, 0 for
+// p <= 0 or NaN), a lower bound of the bucket's keep threshold in both generator modes: a
+// coin below it (x1 < q * 2^24, or u < q / 256 for the shader's float coin) keeps the bucket
+// whatever its entry holds.  The sampler then reads the 8-byte entry only for the other
+// samples -- the share of the mass that the table aliases (1/4 for uniform weights) plus
+// 1/256 -- while the filter (N bytes: 64 MB at N = 2^26) stays in L2 and the table does not.
+// Every decision is the unfiltered one, so the samples are identical.
+__device__ __forceinline__ uint32_t coin_code(uint32_t pbits) {
+    const float p = __uint_as_float(pbits);
+    if (!(p > 0.0f)) return 0u;
+    if (p >= 1.0f) return 255u;
+    return static_cast<uint32_t>(__fmul_rn(p, 256.0f));  // exact product; truncation = floor
+}
+
+// Samples [block * 1024 + 4t, +4) of one distribution (thread t of the CTA).  FILTER: coins is
+// the table's coin filter, read where `use` holds.
+template <uint32_t RNG, bool COOP, bool FILTER>
+__device__ __forceinline__ void alias_block(const uint2* __restrict__ table,
+                                            const uint8_t* __restrict__ coins, bool use,
+                                            uint32_t n, uint64_t S, uint64_t seed,
+                                            uint64_t offset, uint32_t coop,
+                                            uint32_t* __restrict__ out, uint64_t block) {
     const uint64_t t = block * kSampleThreads + threadIdx.x;
     const uint64_t s0 = t * kAliasPerThread;
     if (s0 >= S) return;
     uint32_t r[kAliasPerThread];
+    uint64_t pol = 0;
+    if constexpr (FILTER) pol = l2_policy_evict_first();  // table entries: keep the filter in L2
     if constexpr (RNG == RNG_REF) {
         const uint32_t key = static_cast<uint32_t>(seed);
         const float fn = __uint2float_rn(n);
@@ -66,11 +84,30 @@ __device__ __forceinline__ void alias_block(const uint2* __restrict__ table, uin
             ix = ix > static_cast<int>(n - 1u) ? static_cast<int>(n - 1u) : ix;
             ixs[v] = ix;
         }
+        if constexpr (FILTER) {
+            bool need[kAliasPerThread];
 #pragma unroll
-        for (int v = 0; v < kAliasPerThread; ++v) ent[v] = ld_entry(table + ixs[v]);
+            for (int v = 0; v < kAliasPerThread; ++v) need[v] = true;
+            if (use) {
 #pragma unroll
-        for (int v = 0; v < kAliasPerThread; ++v)
-            r[v] = uys[v] >= __uint_as_float(ent[v].x) ? ent[v].y : static_cast<uint32_t>(ixs[v]);
+                for (int v = 0; v < kAliasPerThread; ++v)
+                    need[v] = !(uys[v] <
+                                __fmul_rn(__uint2float_rn(__ldg(coins + ixs[v])), 0.00390625f));
+            }
+#pragma unroll
+            for (int v = 0; v < kAliasPerThread; ++v)
+                ent[v] = need[v] ? ld_entry_policy(table + ixs[v], pol) : make_uint2(0u, 0u);
+#pragma unroll
+            for (int v = 0; v < kAliasPerThread; ++v)
+                r[v] = need[v] && uys[v] >= __uint_as_float(ent[v].x) ? ent[v].y
+                                                                      : static_cast<uint32_t>(ixs[v]);
+        } else {
+#pragma unroll
+            for (int v = 0; v < kAliasPerThread; ++v) ent[v] = ld_entry(table + ixs[v]);
+#pragma unroll
+            for (int v = 0; v < kAliasPerThread; ++v)
+                r[v] = uys[v] >= __uint_as_float(ent[v].x) ? ent[v].y : static_cast<uint32_t>(ixs[v]);
+        }
     } else {
         uint2 ks[10];
         philox4x32_10_keys(seed, ks);
@@ -85,12 +122,26 @@ __device__ __forceinline__ void alias_block(const uint2* __restrict__ table, uin
             ixs[v] = __umulhi(x.x, n);
             coin[v] = x.y;
         }
+        bool need[kAliasPerThread];
 #pragma unroll
-        for (int v = 0; v < kAliasPerThread; ++v) ent[v] = ld_entry(table + ixs[v]);
+        for (int v = 0; v < kAliasPerThread; ++v) need[v] = true;
+        if (FILTER && use) {
+#pragma unroll
+            for (int v = 0; v < kAliasPerThread; ++v)
+                need[v] = coin[v] >= (static_cast<uint32_t>(__ldg(coins + ixs[v])) << 24);
+        }
+#pragma unroll
+        for (int v = 0; v < kAliasPerThread; ++v) {
+            if constexpr (FILTER)
+                ent[v] = need[v] ? ld_entry_policy(table + ixs[v], pol) : make_uint2(0u, 0u);
+            else
+                ent[v] = ld_entry(table + ixs[v]);
+        }
 #pragma unroll
         for (int v = 0; v < kAliasPerThread; ++v) {
             const float p = __uint_as_float(ent[v].x);
-            const bool keep = p >= 1.0f || coin[v] < __float2uint_ru(__fmul_rn(p, 4294967296.0f));
+            const bool keep = !need[v] || p >= 1.0f ||
+                              coin[v] < __float2uint_ru(__fmul_rn(p, 4294967296.0f));
             r[v] = keep ? ixs[v] : ent[v].y;
         }
     }
@@ -103,14 +154,15 @@ __device__ __forceinline__ void alias_block(const uint2* __restrict__ table, uin
     }
 }
 
-template <uint32_t RNG, bool COOP>
-__global__ __launch_bounds__(kSampleThreads) void k_alias_sample(const uint2* __restrict__ table,
-                                                                 uint32_t n, uint64_t S,
-                                                                 uint64_t seed, uint64_t offset,
-                                                                 uint32_t coop,
-                                                                 uint32_t* __restrict__ out) {
+template <uint32_t RNG, bool COOP, bool FILTER>
+__global__ __launch_bounds__(kSampleThreads) void k_alias_sample(
+    const uint2* __restrict__ table, const uint8_t* __restrict__ coins,
+    const unsigned long long* __restrict__ coin_sum, uint32_t n, uint64_t S, uint64_t seed,
+    uint64_t offset, uint32_t coop, uint32_t* __restrict__ out) {
     pdl_entry();
-    alias_block<RNG, COOP>(table, n, S, seed, offset, coop, out, blockIdx.x);
+    bool use = false;
+    if constexpr (FILTER) use = __ldg(coin_sum) >= kCoinMinMean * n;
+    alias_block<RNG, COOP, FILTER>(table, coins, use, n, S, seed, offset, coop, out, blockIdx.x);
 }
 
 // All distributions of a batch in one launch: CTA b samples block b - sample0 of the
@@ -122,8 +174,48 @@ __global__ __launch_bounds__(kSampleThreads) void k_alias_sample_batch(BatchView
     pdl_entry();
     const uint32_t d = __ldg(bv.sample_map + blockIdx.x);
     const DistDesc* D = bv.dist + d;
-    alias_block<RNG, COOP>(D->table, D->n, D->s, D->seed, 0ull, coop, D->out,
-                           blockIdx.x - D->sample0);
+    alias_block<RNG, COOP, false>(D->table, nullptr, false, D->n, D->s, D->seed, 0ull, coop,
+                                  D->out, blockIdx.x - D->sample0);
+}
+
+// The coin filter of table[0, n) (coin_code per entry, four entries per thread per step of a
+// grid-striding loop) and the sum of its codes, added into *coin_sum once per CTA.
+__global__ __launch_bounds__(kSampleThreads) void k_coin_filter(const uint2* __restrict__ table,
+                                                                uint32_t n,
+                                                                uint8_t* __restrict__ coins,
+                                                                unsigned long long* coin_sum) {
+    pdl_entry();
+    __shared__ unsigned long long s_sum[kSampleThreads / 32];
+    const uint64_t groups = (static_cast<uint64_t>(n) + 3u) / 4u;
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * kSampleThreads;
+    unsigned long long sum = 0;
+    for (uint64_t t = static_cast<uint64_t>(blockIdx.x) * kSampleThreads + threadIdx.x;
+         t < groups; t += stride) {
+        const uint64_t e0 = 4ull * t;
+        if (e0 + 4u <= n) {
+            const uint4 a = __ldcs(reinterpret_cast<const uint4*>(table + e0));
+            const uint4 b = __ldcs(reinterpret_cast<const uint4*>(table + e0 + 2u));
+            const uint32_t c0 = coin_code(a.x), c1 = coin_code(a.z), c2 = coin_code(b.x),
+                           c3 = coin_code(b.z);
+            reinterpret_cast<uint32_t*>(coins)[t] = c0 | c1 << 8 | c2 << 16 | c3 << 24;
+            sum += c0 + c1 + c2 + c3;
+        } else {
+            for (uint64_t e = e0; e < n; ++e) {
+                const uint32_t c = coin_code(table[e].x);
+                coins[e] = static_cast<uint8_t>(c);
+                sum += c;
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, m);
+    if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long tot = 0;
+        for (int w = 0; w < kSampleThreads / 32; ++w) tot += s_sum[w];
+        atomicAdd(coin_sum, tot);
+    }
 }
 
 // its/sampling/shader.comp:80-94
@@ -1107,6 +1199,7 @@ cudaError_t launch_cutpoint_sample(cudaStream_t st, uint32_t rng, const float* c
 }
 
 cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, const uint2* table,
+                                const uint8_t* coins, const unsigned long long* coin_sum,
                                 uint32_t n, uint64_t S, uint64_t seed, uint64_t offset,
                                 uint32_t* out) {
     const uint64_t threads = (S + kAliasPerThread - 1) / kAliasPerThread;
@@ -1114,14 +1207,32 @@ cudaError_t launch_alias_sample(cudaStream_t st, uint32_t rng, uint32_t coop, co
     if (blocks == 0) return cudaSuccess;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
     const dim3 grid(static_cast<unsigned>(blocks));
+    const uint8_t* c = coop || !coin_sum ? nullptr : coins;  // cooperative: the table alone
     if (rng == RNG_REF) {
         if (coop)
-            launch_pdl(k_alias_sample<RNG_REF, true>, grid, kSampleThreads, 0, st, table, n, S, seed, offset, coop, out);
+            launch_pdl(k_alias_sample<RNG_REF, true, false>, grid, kSampleThreads, 0, st, table, c, coin_sum, n, S, seed, offset, coop, out);
+        else if (c)
+            launch_pdl(k_alias_sample<RNG_REF, false, true>, grid, kSampleThreads, 0, st, table, c, coin_sum, n, S, seed, offset, coop, out);
         else
-            launch_pdl(k_alias_sample<RNG_REF, false>, grid, kSampleThreads, 0, st, table, n, S, seed, offset, coop, out);
+            launch_pdl(k_alias_sample<RNG_REF, false, false>, grid, kSampleThreads, 0, st, table, c, coin_sum, n, S, seed, offset, coop, out);
+    } else if (c) {
+        launch_pdl(k_alias_sample<RNG_PHILOX, false, true>, grid, kSampleThreads, 0, st, table, c, coin_sum, n, S, seed, offset, coop, out);
     } else {
-        launch_pdl(k_alias_sample<RNG_PHILOX, false>, grid, kSampleThreads, 0, st, table, n, S, seed, offset, coop, out);
+        launch_pdl(k_alias_sample<RNG_PHILOX, false, false>, grid, kSampleThreads, 0, st, table, c, coin_sum, n, S, seed, offset, coop, out);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coin_filter(cudaStream_t st, const uint2* table, uint32_t n, uint8_t* coins,
+                               unsigned long long* coin_sum) {
+    const uint64_t groups = (static_cast<uint64_t>(n) + 3u) / 4u;
+    const uint64_t blocks = (groups + kSampleThreads - 1) / kSampleThreads;
+    if (blocks == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(coin_sum, 0, sizeof(*coin_sum), st);
+    if (e != cudaSuccess) return e;
+    // a few CTAs per SM, striding over the table: one atomic per CTA
+    const unsigned grid = static_cast<unsigned>(blocks < 8u * 152u ? blocks : 8u * 152u);
+    launch_pdl(k_coin_filter, grid, kSampleThreads, 0, st, table, n, coins, coin_sum);
     return cudaGetLastError();
 }
 

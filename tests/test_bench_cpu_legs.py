@@ -86,3 +86,12 @@ def test_binned_chi2_bins_and_variance():
     pb = bench.p_binned(p * s, 16)
     assert abs(float(pb.sum()) - 1.0) < 1e-12 and pb.numel() == 63
     assert "p_value_multinomial" in r
+
+
+def test_profiled_traffic_reads_the_committed_capture():
+    """The roofline's traffic comes from the committed ncu summary of the sampler with its coin
+    filters, at the granularities captured there (64 B), and is absent at the others."""
+    import bench
+    t = bench.profiled_traffic(64)
+    assert t is not None and 1e10 < t < 2e10
+    assert bench.profiled_traffic(128) is None

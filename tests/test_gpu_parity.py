@@ -282,6 +282,44 @@ def test_alias_sample_bit_exact(pkg, cuda, oracle, rng, coop, offset):
     assert np.array_equal(got, ref)
 
 
+@pytest.mark.parametrize("N", [(1 << 22) + 1, (1 << 23) + 6])
+@pytest.mark.parametrize("rng,coop", [(RNG_REFERENCE, 0), (RNG_PHILOX4X32_10, 0),
+                                      (RNG_REFERENCE, 64)])
+@pytest.mark.parametrize("gen", ["uniform", "lognormal"])
+def test_alias_sample_coin_filter(pkg, cuda, oracle, N, rng, coop, gen):
+    """Tables of more than 2^22 entries are sampled through their coin filter (the table read
+    only where the coin does not decide); the samples equal the oracle's full evaluation on
+    the GPU's table in both generator modes, and the cooperative mode (no filter) too."""
+    w = GENS[gen](N, 9)
+    b = Built(pkg, w, pkg.AliasTableConfig(split_size=12, rng=rng, coop_size=coop,
+                                           scan_precision=pkg.wrs.SCAN_FLOAT_FLOAT,
+                                           split_residual_f64=True, split_full_light=True))
+    S = (1 << 21) + 5
+    got = b.sample(S, 77, offset=(1 << 20) + 3)
+    ref = oracle.alias_sample(b.table, S, 77, rng=rng, coop=coop, offset=(1 << 20) + 3,
+                              nthreads=16)
+    assert np.array_equal(got, ref)
+
+
+def test_coin_filter_follows_the_table(pkg, cuda, oracle):
+    """A table rewritten in the buffers by the split-pack primitive (another split size) is
+    sampled from its new entries, not through the coin filter of the table the build made."""
+    W = pkg.wrs
+    N = (1 << 22) + 9
+    w = weights_uniform(N, 3)
+    b = Built(pkg, w, pkg.AliasTableConfig(split_size=12, rng=RNG_PHILOX4X32_10))
+    other = W.WRS(pkg.AliasTableConfig(split_size=2, rng=RNG_PHILOX4X32_10))
+    v = b.buffers.internals.views()
+    other.split_pack(None, b.buffers.weights, v["partition_indices"], v["partition_prefix"],
+                     v["partition_elements"], N, v["alias_table"], b.buffers.internals)
+    table = d2h(v["alias_table"], N, ENTRY_DTYPE)
+    assert not same_table(table, b.table)
+    S = 1 << 21
+    got = b.sample(S, 5)
+    assert np.array_equal(got, oracle.alias_sample(table, S, 5, rng=RNG_PHILOX4X32_10,
+                                                   nthreads=16))
+
+
 @pytest.mark.parametrize("n", [1, 3, 4, 1023, 1024, 1025, (1 << 20) + 3, (1 << 24) + 1])
 @pytest.mark.parametrize("seed", [0, 12345, 0xFFFFFFFF])
 @pytest.mark.parametrize("shift", [0, 1])
