@@ -131,6 +131,14 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+def launches_per_step(n: int) -> int:
+    """The library's kernel launches in one headline step (wrs_build + wrs_sample): total mass,
+    partition, the split descent (split-pack grids of >= 512 CTAs of 479 subproblems), the
+    split-pack, the coin filter (2^22 < N <= 2^26) and the sampler."""
+    blocks = -(-(n // SPLIT_SIZE) // 479)
+    return 4 + (blocks >= 512) + ((1 << 22) < n <= (1 << 26))
+
+
 def profiled_traffic(l2_fetch: int) -> float | None:
     """DRAM bytes of one headline alias-sampling launch (with the tables' coin filters, the
     mean over the three distributions' launches) at the given L2 fetch granularity, from the
@@ -592,7 +600,7 @@ def main() -> None:
         "build_ms_mean": statistics.mean(build_ms),
         "sample_ms_mean": statistics.mean(sample_ms),
         "clocks": clk,
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": launches_per_step(n) * args.steps,
         "device_status": {"timeout": bool(dev_status & W.DEVICE_TIMEOUT),
                           "split_overlap_beyond_window": bool(dev_status & W.DEVICE_NONMONOTONE_SPLIT)},
     }

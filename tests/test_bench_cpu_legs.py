@@ -95,3 +95,12 @@ def test_profiled_traffic_reads_the_committed_capture():
     t = bench.profiled_traffic(64)
     assert t is not None and 1e10 < t < 2e10
     assert bench.profiled_traffic(128) is None
+
+
+def test_launches_per_step():
+    """Six launches per headline step at N = 2^26 (mass, partition, split descent, split-pack,
+    coin filter, sampling); no filter above 2^26, no descent for small grids."""
+    import bench
+    assert bench.launches_per_step(1 << 26) == 6
+    assert bench.launches_per_step((1 << 26) + 5) == 5
+    assert bench.launches_per_step(65536) == 4
