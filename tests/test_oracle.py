@@ -392,3 +392,28 @@ def test_serial_split_pack_equals_inline_when_n_divides(oracle, gen, s):
             assert np.array_equal(table.view(np.uint64), inline.view(np.uint64))
         implied = oracle.alias_to_weights(table)
         assert np.abs(implied - w / w.astype(np.float64).mean()).max() < 1e-3
+
+
+def test_coin_filter_bound_never_changes_a_decision():
+    """The alias sampler's coin filter stores q = floor(256 p) per bucket (255 for p >= 1, 0 for
+    p <= 0 or NaN) and keeps a bucket early when the coin lies below q's bound.  The bound is
+    below the keep threshold in both generator modes -- q * 2^24 <= ceil(p * 2^32) for the 32-bit
+    Philox coin and q / 256 <= p for the shader's float coin -- so no early decision differs
+    from the full one; checked over random FP32 bit patterns in [0, 2) and the edge values."""
+    rng = np.random.default_rng(11)
+    p = rng.integers(0, 0x40000000, 1 << 21, dtype=np.uint32).view(np.float32)
+    edges = np.array([0.0, -0.0, 1.0, np.nextafter(np.float32(1), np.float32(0)), 1.0 / 256,
+                      np.nextafter(np.float32(1.0 / 256), np.float32(0)), np.inf, np.nan, -1.0,
+                      1e-45], dtype=np.float32)
+    p = np.concatenate([p, edges])
+    with np.errstate(invalid="ignore"):
+        q = np.where(~(p > 0), 0, np.where(p >= 1, 255, np.floor(p.astype(np.float64) * 256)))
+    q = q.astype(np.int64)
+    assert q.min() >= 0 and q.max() <= 255
+    with np.errstate(invalid="ignore"):
+        below_one = (p > 0) & (p < 1)
+    ceil_p = np.ceil(p[below_one].astype(np.float64) * 2.0 ** 32).astype(np.int64)
+    assert np.all((q[below_one] << 24) <= ceil_p)
+    assert np.all(q[below_one] / 256.0 <= p[below_one].astype(np.float64))
+    # p >= 1 keeps every coin; its code's bound stays below 2^32 and below 1
+    assert (255 << 24) < 2 ** 32 and 255 / 256 < 1
