@@ -204,7 +204,9 @@ cudaError_t launch_coin_filter(cudaStream_t st, const uint2* table, uint32_t n, 
 // codes average at least kCoinMinMean (out of 255): then at most ~78 % of the samples read
 // their entry.  Measured at N = 2^26 on a box whose plain sampler takes 5.13 ms for 2^28
 // samples, the filtered one took 0.66 + 5.45 f ms with f the share of samples reading their
-// entry (f = 0.42 uniform, 0.75 log-normal(0, 2), 0.88 Zipf(1.1): 2.94 / 4.77 / 5.59 ms).
+// entry (f = 0.42 uniform, 0.75 log-normal(0, 2), 0.88 Zipf(1.1): 2.94 / 4.77 / 5.59 ms); on a
+// box whose plain sampler takes 3.77 ms the uniform table took 2.56 ms and the log-normal one
+// 4.06 ms, so tables near the threshold gain on the one and lose on the other.
 constexpr uint32_t kCoinMinN = 1u << 22;
 constexpr uint32_t kCoinMaxN = 1u << 26;
 constexpr uint64_t kCoinMinMean = 56;

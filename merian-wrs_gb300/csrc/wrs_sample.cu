@@ -32,8 +32,9 @@ __device__ __forceinline__ float mix_rn(float x, float y, float a) {
 // p <= 0 or NaN), a lower bound of the bucket's keep threshold in both generator modes: a
 // coin below it (x1 < q * 2^24, or u < q / 256 for the shader's float coin) keeps the bucket
 // whatever its entry holds.  The sampler then reads the 8-byte entry only for the other
-// samples -- the share of the mass that the table aliases (1/4 for uniform weights) plus
-// 1/256 -- while the filter (N bytes: 64 MB at N = 2^26) stays in L2 and the table does not.
+// samples -- 1 - mean(q) / 256 of them: 0.42 for uniform weights, whose PSA buckets keep 58 %
+// of their draws -- while the filter (N bytes: 64 MB at N = 2^26) stays in L2 and the table
+// does not.
 // Every decision is the unfiltered one, so the samples are identical.
 __device__ __forceinline__ uint32_t coin_code(uint32_t pbits) {
     const float p = __uint_as_float(pbits);
