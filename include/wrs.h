@@ -179,7 +179,11 @@ void wrs_destroy(wrs_handle* h);
 /* Internals for distributions of up to max_n weights (one cudaMalloc).  For ITS on the FP32
  * CMF above 2^16 weights they include the bisection's stored probe-tree blocks (at most ~2/7
  * of the CMF's bytes), which wrs_build writes and wrs_sample reads for the n built last; the
- * primitive wrs_its_sample probes the CMF alone (same samples). */
+ * primitive wrs_its_sample probes the CMF alone (same samples).  For the alias method above
+ * 2^22 weights they include the table's coin filter (one byte per weight up to 2^26): wrs_build
+ * writes it after the table and wrs_sample reads it for the n built last, so that samples whose
+ * coin decides skip the table read (same samples; wrs_split_pack and wrs_pack into the buffers
+ * retire it until the next build, and the primitive wrs_alias_sample reads the table alone). */
 size_t wrs_buffers_bytes(const wrs_handle* h, uint32_t max_n);
 wrs_status wrs_buffers_create(const wrs_handle* h, uint32_t max_n, wrs_buffers** out);
 void wrs_buffers_destroy(wrs_buffers* b);
